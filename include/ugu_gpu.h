@@ -1,0 +1,214 @@
+/*
+ * ugu_gpu.h -- C ABI of the GB300 rasterizer (libugugpu.so).
+ *
+ * This is the boundary a ugu build binds to replace the CPU rasterizer
+ * (ugu::Rasterizer, include/ugu/renderer/cpu/rasterizer.h:14-53) behind the
+ * ugu::RendererCpu interface (include/ugu/renderer/cpu/renderer.h:42-76).
+ * Plain pointers and sizes only; every entry point returns a status code
+ * (0 = success) and leaves a message in ugu_gpu_last_error().
+ *
+ * Image layouts are ugu::Image's (include/ugu/image.h:347-427): row-major,
+ * channels interleaved.  color: H*W*3 uint8 RGB; depth: H*W float;
+ * normal: H*W*3 float (camera frame); mask: H*W uint8 (0/255);
+ * face_id: H*W int32 (-1 = none).
+ */
+#ifndef UGU_GPU_H_
+#define UGU_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UGU_GPU_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define UGU_GPU_API __attribute__((visibility("default")))
+#else
+#define UGU_GPU_API
+#endif
+
+typedef struct ugu_gpu_context ugu_gpu_context;
+typedef struct ugu_gpu_plan ugu_gpu_plan;
+
+/* Status codes.  3..10 are the failure cases of ugu's
+ * ValidateAndInitBeforeRender (src/renderer/cpu/util_private.cc:19-67) and
+ * Rasterizer::Impl::PrepareMesh (src/renderer/cpu/rasterizer.cc:90-99), which
+ * the reference reports as `false` + LOGE. */
+enum {
+  UGU_GPU_OK = 0,
+  UGU_GPU_ERR_INVALID_ARGUMENT = 1,
+  UGU_GPU_ERR_NOT_PREPARED = 2,          /* mesh slot empty ("mesh has not been initialized") */
+  UGU_GPU_ERR_NO_FACE_NORMALS = 3,       /* culling without face normals */
+  UGU_GPU_ERR_NO_TEXTURE = 4,            /* kTexture without materials */
+  UGU_GPU_ERR_EMPTY_TEXTURE = 5,         /* a material's texture is empty */
+  UGU_GPU_ERR_NO_VERTEX_COLORS = 6,      /* kVertex without vertex colours */
+  UGU_GPU_ERR_NO_FACE_NORMALS_FOR_SHADING = 7,
+  UGU_GPU_ERR_NO_VERTEX_NORMALS = 8,
+  UGU_GPU_ERR_NO_OUTPUT = 9,             /* every output pointer is NULL */
+  UGU_GPU_ERR_NO_CAMERA = 10,
+  UGU_GPU_ERR_INDEX_OUT_OF_RANGE = 11,   /* a face refers past its array */
+  UGU_GPU_ERR_CUDA = 12,
+  UGU_GPU_ERR_OUT_OF_MEMORY = 13,
+  UGU_GPU_ERR_DEVICE_TIMEOUT = 14,       /* a bounded device-side wait ran out */
+  UGU_GPU_ERR_CAPACITY = 15,             /* a device work list hit its capacity */
+  UGU_GPU_ERR_NO_DEVICE = 16,
+  UGU_GPU_ERR_DEGENERATE_DEPTH = 17      /* a covered sample with depth < FLT_MIN or NaN */
+};
+
+/* ugu::RendererCpuOption (include/ugu/renderer/cpu/renderer.h:17-38) with the
+ * enums of include/ugu/renderer/base.h:11-32 and ugu::ColorInterpolation
+ * (include/ugu/common.h:50-53). */
+typedef struct {
+  int32_t diffuse_color;   /* 0 kNone (white), 1 kTexture, 2 kVertex */
+  int32_t interp;          /* 0 kNn, 1 kBilinear */
+  int32_t shading_normal;  /* 0 kFace, 1 kVertex */
+  int32_t diffuse_shading; /* 0 kNone, 1 kLambertian, 2 kOrenNayar */
+  float depth_scale;       /* accepted and ignored, as ugu::Rasterizer does */
+  int32_t backface_culling;
+  float oren_nayar_sigma;
+} ugu_gpu_option;
+
+typedef struct {
+  int32_t width, height;
+  const uint8_t* rgb8;   /* H*W*3 (ugu::Image3b), or NULL */
+  const float* rgb_f32;  /* H*W*3 float texels (differentiable path), or NULL */
+} ugu_gpu_texture;
+
+/* ugu::Mesh's SoA fields (include/ugu/mesh.h:83-98).  Optional arrays may be
+ * NULL.  Indices are validated against their arrays on upload. */
+typedef struct {
+  int32_t num_vertices;
+  const float* vertices;        /* V*3 */
+  int32_t num_faces;
+  const int32_t* vertex_indices;/* F*3 */
+  const float* face_normals;    /* F*3 or NULL */
+  int32_t num_normals;
+  const float* normals;         /* N*3 or NULL */
+  const int32_t* normal_indices;/* F*3 or NULL */
+  const float* vertex_colors;   /* V*3 or NULL */
+  int32_t num_uv;
+  const float* uv;              /* T*2 or NULL */
+  const int32_t* uv_indices;    /* F*3 or NULL */
+  const int32_t* material_ids;  /* F or NULL */
+  int32_t num_materials;
+  const ugu_gpu_texture* materials;
+} ugu_gpu_mesh;
+
+/* The float camera parameters ugu::Rasterizer::Impl::Render reads from a
+ * PinholeCamera (rasterizer.cc:118-119; camera.h:317-331, 380-387, 438-448),
+ * computed on the host exactly as the reference does:
+ *   w2c_R = camera->w2c().rotation().cast<float>()      (row-major)
+ *   w2c_t = camera->w2c().translation().cast<float>()
+ *   c2w_R = camera->c2w().matrix().block<3,3>(0,0).cast<float>() (row-major)
+ *   fx, fy = focal_length(); cx, cy = principal_point(). */
+typedef struct {
+  int32_t width, height;
+  float fx, fy, cx, cy;
+  float w2c_R[9];
+  float w2c_t[3];
+  float c2w_R[9];
+} ugu_gpu_camera;
+
+/* Output images of one view; NULL skips an output (Render's nullptr rule,
+ * renderer.h:60-63).  color_f32 (H*W*3 float, unquantised colour) is an
+ * extension used by the differentiable path. */
+typedef struct {
+  uint8_t* color;
+  float* depth;
+  float* normal;
+  uint8_t* mask;
+  int32_t* face_id;
+  float* color_f32;
+} ugu_gpu_images;
+
+typedef struct {
+  int32_t mesh; /* mesh slot set by ugu_gpu_set_mesh */
+  ugu_gpu_camera camera;
+  ugu_gpu_images images;
+} ugu_gpu_view;
+
+/* Flags for ugu_gpu_render_views / ugu_gpu_plan_create. */
+enum {
+  UGU_GPU_DEVICE_POINTERS = 1u << 0, /* images are device pointers (else host) */
+  UGU_GPU_PER_VIEW = 1u << 1,        /* one launch sequence per view (baseline) */
+  UGU_GPU_ASYNC = 1u << 2            /* do not synchronise (device pointers only) */
+};
+
+/* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
+typedef struct {
+  int32_t tile_log2;        /* large-face tile edge = 1 << tile_log2 pixels */
+  int32_t small_bbox_max;   /* faces whose bbox has more pixels go to the tile path */
+  int32_t group_pixels;     /* pixels of z-buffer kept live per view group */
+  int32_t raster_ctas_per_sm;
+} ugu_gpu_tuning;
+
+typedef struct {
+  uint64_t launches;            /* kernels launched by this context so far */
+  uint64_t special_candidates;  /* covered samples with depth < FLT_MIN or NaN */
+  uint64_t large_face_tiles;    /* (face, tile) items of the last render */
+  uint64_t device_bytes;        /* scratch + mesh bytes held on the device */
+} ugu_gpu_stats;
+
+/* --- context ------------------------------------------------------------ */
+UGU_GPU_API int ugu_gpu_create(int32_t device, ugu_gpu_context** out);
+UGU_GPU_API int ugu_gpu_destroy(ugu_gpu_context* ctx);
+UGU_GPU_API const char* ugu_gpu_last_error(const ugu_gpu_context* ctx);
+UGU_GPU_API int ugu_gpu_abi_version(void);
+
+/* Rasterizer::set_option (rasterizer.cc:73-75).  Like RendererCpuOption::
+ * CopyTo (renderer.h:30-37) the host class passes the sigma it holds. */
+UGU_GPU_API int ugu_gpu_set_option(ugu_gpu_context* ctx, const ugu_gpu_option* opt);
+
+/* Rasterizer::set_mesh + PrepareMesh (rasterizer.cc:77-99): validates and
+ * uploads the mesh into `slot` (0 <= slot < 16).  A NULL mesh empties it. */
+UGU_GPU_API int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* mesh);
+
+/* Rasterizer::Render (rasterizer.cc:105-307) for one view, host buffers,
+ * synchronous: outputs are valid on return. */
+UGU_GPU_API int ugu_gpu_render(ugu_gpu_context* ctx, int32_t mesh, const ugu_gpu_camera* cam,
+                   const ugu_gpu_images* images);
+
+/* Many views (several meshes, uneven resolutions) in one batched launch
+ * sequence; see the UGU_GPU_* flags. */
+UGU_GPU_API int ugu_gpu_render_views(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                         uint32_t flags);
+
+/* Capture the batched render of `views` (device pointers) into a CUDA graph;
+ * ugu_gpu_plan_launch replays it on the context's stream. */
+UGU_GPU_API int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                        uint32_t flags, ugu_gpu_plan** out);
+UGU_GPU_API int ugu_gpu_plan_launch(ugu_gpu_plan* plan);
+UGU_GPU_API int ugu_gpu_plan_destroy(ugu_gpu_plan* plan);
+
+/* Backward of the per-pixel L2 loss sum_p |C(p) - T(p)|^2 over pixels with
+ * face_id > 0, where C is the unquantised colour of the forward (float
+ * texels of material 0, bilinear; or vertex colours), visibility held fixed
+ * at the forward's face_id images (views[i].images.face_id, device memory).
+ * targets[i] is an H*W*3 float device image.  Gradients are accumulated (+=)
+ * into the device buffers grad_texels (material 0, H*W*3), grad_vertex_colors
+ * (V*3) and grad_vertices (V*3), any of which may be NULL.  loss_out (device,
+ * one float per view) receives the per-view loss when non-NULL. */
+UGU_GPU_API int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                     const float* const* targets, float* grad_texels,
+                     float* grad_vertex_colors, float* grad_vertices, float* loss_out,
+                     uint32_t flags);
+
+UGU_GPU_API int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* tuning);
+UGU_GPU_API int ugu_gpu_get_tuning(const ugu_gpu_context* ctx, ugu_gpu_tuning* tuning);
+/* Time candidate tunings on `views` (device pointers) and keep the fastest. */
+UGU_GPU_API int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                     ugu_gpu_tuning* chosen);
+
+UGU_GPU_API int ugu_gpu_get_stats(const ugu_gpu_context* ctx, ugu_gpu_stats* stats);
+UGU_GPU_API int ugu_gpu_synchronize(ugu_gpu_context* ctx);
+/* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
+UGU_GPU_API int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UGU_GPU_H_ */

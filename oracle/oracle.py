@@ -1,0 +1,261 @@
+"""ctypes binding of raster_oracle.c (test infrastructure only)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "liboracle.so")
+SRC = os.path.join(HERE, "raster_oracle.c")
+
+# -ffp-contract=off: every float operation rounds once, in source order, on
+# x86-64 and on aarch64 alike (GCC contracts to FMA by default on aarch64).
+CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(LIB_DIR, exist_ok=True)
+    hdr = os.path.join(HERE, "raster_oracle.h")
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("data", C.c_void_p)]
+
+
+class MeshS(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_int32), ("vertices", C.c_void_p),
+        ("num_faces", C.c_int32), ("vertex_indices", C.c_void_p),
+        ("num_face_normals", C.c_int32), ("face_normals", C.c_void_p),
+        ("num_normals", C.c_int32), ("normals", C.c_void_p),
+        ("num_normal_indices", C.c_int32), ("normal_indices", C.c_void_p),
+        ("num_vertex_colors", C.c_int32), ("vertex_colors", C.c_void_p),
+        ("num_uv", C.c_int32), ("uv", C.c_void_p),
+        ("num_uv_indices", C.c_int32), ("uv_indices", C.c_void_p),
+        ("num_material_ids", C.c_int32), ("material_ids", C.c_void_p),
+        ("num_materials", C.c_int32), ("textures", C.c_void_p),
+        ("textures_f32", C.c_void_p),
+    ]
+
+
+class CameraS(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32),
+                ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("w2c_R", C.c_float * 9), ("w2c_t", C.c_float * 3), ("c2w_R", C.c_float * 9)]
+
+
+class OptionS(C.Structure):
+    _fields_ = [("diffuse_color", C.c_int32), ("interp", C.c_int32),
+                ("shading_normal", C.c_int32), ("diffuse_shading", C.c_int32),
+                ("backface_culling", C.c_int32), ("oren_nayar_sigma", C.c_float)]
+
+
+class StatsS(C.Structure):
+    _fields_ = [("bbox_pixels", C.c_int64), ("covered", C.c_int64),
+                ("special_candidates", C.c_int64), ("texel_clamps", C.c_int64)]
+
+
+@dataclass
+class Stats:
+    bbox_pixels: int
+    covered: int
+    special_candidates: int
+    texel_clamps: int
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        lib = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        lib.oracle_render.argtypes = [P, P, P, P, P, P, P, P, P, P]
+        lib.oracle_render.restype = C.c_int
+        lib.oracle_ray_w.argtypes = [P, C.c_int32, C.c_int32, P]
+        lib.oracle_interp_f64.argtypes = [P, P, P, P, P, P, P]
+        lib.oracle_backward_f64.argtypes = [P, P, P, P, P, P, P, P]
+        lib.oracle_backward_f64.restype = C.c_double
+        lib.oracle_calc_normals.argtypes = [C.c_int32, P, C.c_int32, P, P, P]
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class _MeshHandle:
+    """Keeps the numpy arrays alive while C holds pointers to them."""
+
+    def __init__(self, mesh):
+        self.keep = []
+
+        def arr(a, dt, cols=None):
+            if a is None:
+                return None, 0
+            a = np.ascontiguousarray(a, dtype=dt)
+            self.keep.append(a)
+            return a, (a.shape[0] if a.ndim else 0)
+
+        s = MeshS()
+        v, nv = arr(mesh.vertices, np.float32)
+        f, nf = arr(mesh.vertex_indices, np.int32)
+        fn, nfn = arr(mesh.face_normals, np.float32)
+        n, nn = arr(mesh.normals, np.float32)
+        ni, nni = arr(mesh.normal_indices, np.int32)
+        vc, nvc = arr(mesh.vertex_colors, np.float32)
+        uv, nuv = arr(mesh.uv, np.float32)
+        ui, nui = arr(mesh.uv_indices, np.int32)
+        mi, nmi = arr(mesh.material_ids, np.int32)
+        s.num_vertices, s.vertices = nv, _ptr(v)
+        s.num_faces, s.vertex_indices = nf, _ptr(f)
+        s.num_face_normals, s.face_normals = nfn, _ptr(fn)
+        s.num_normals, s.normals = nn, _ptr(n)
+        s.num_normal_indices, s.normal_indices = nni, _ptr(ni)
+        s.num_vertex_colors, s.vertex_colors = nvc, _ptr(vc)
+        s.num_uv, s.uv = nuv, _ptr(uv)
+        s.num_uv_indices, s.uv_indices = nui, _ptr(ui)
+        s.num_material_ids, s.material_ids = nmi, _ptr(mi)
+        texs = list(mesh.textures or [])
+        tf32 = list(mesh.textures_f32 or [])
+        nm = max(len(texs), len(tf32))
+        tarr = (Texture * max(nm, 1))()
+        farr = (C.c_void_p * max(nm, 1))()
+        for i in range(nm):
+            t8 = texs[i] if i < len(texs) else None
+            t32 = tf32[i] if i < len(tf32) else None
+            ref = t8 if t8 is not None else t32
+            tarr[i].height, tarr[i].width = (ref.shape[0], ref.shape[1]) if ref is not None else (0, 0)
+            if t8 is not None:
+                t8 = np.ascontiguousarray(t8, dtype=np.uint8)
+                self.keep.append(t8)
+            tarr[i].data = _ptr(t8)
+            if t32 is not None:
+                t32 = np.ascontiguousarray(t32, dtype=np.float32)
+                self.keep.append(t32)
+            farr[i] = _ptr(t32)
+        self.keep += [tarr, farr]
+        s.num_materials = nm
+        s.textures = C.addressof(tarr)
+        s.textures_f32 = C.addressof(farr) if any(t is not None for t in tf32) else None
+        self.s = s
+
+
+def camera_struct(cam) -> CameraS:
+    c = CameraS()
+    c.width, c.height = cam.width, cam.height
+    c.fx, c.fy, c.cx, c.cy = cam.fx, cam.fy, cam.cx, cam.cy
+    for i, x in enumerate(np.asarray(cam.w2c_R, dtype=np.float32).reshape(-1)):
+        c.w2c_R[i] = float(x)
+    for i, x in enumerate(np.asarray(cam.w2c_t, dtype=np.float32).reshape(-1)):
+        c.w2c_t[i] = float(x)
+    for i, x in enumerate(np.asarray(cam.c2w_R, dtype=np.float32).reshape(-1)):
+        c.c2w_R[i] = float(x)
+    return c
+
+
+def option_struct(opt) -> OptionS:
+    o = OptionS()
+    o.diffuse_color = int(opt.diffuse_color)
+    o.interp = int(opt.interp)
+    o.shading_normal = int(opt.shading_normal)
+    o.diffuse_shading = int(opt.diffuse_shading)
+    o.backface_culling = 1 if opt.backface_culling else 0
+    o.oren_nayar_sigma = float(opt.oren_nayar_sigma)
+    return o
+
+
+def render(mesh, cam, opt, outputs=("color", "depth", "normal", "mask", "face_id"),
+           color_f32=False):
+    """Render one view; returns (status, dict of numpy images, Stats)."""
+    lib = load()
+    H, W = cam.height, cam.width
+    out = {}
+    if "color" in outputs:
+        out["color"] = np.empty((H, W, 3), np.uint8)
+    if "depth" in outputs:
+        out["depth"] = np.empty((H, W), np.float32)
+    if "normal" in outputs:
+        out["normal"] = np.empty((H, W, 3), np.float32)
+    if "mask" in outputs:
+        out["mask"] = np.empty((H, W), np.uint8)
+    if "face_id" in outputs:
+        out["face_id"] = np.empty((H, W), np.int32)
+    if color_f32:
+        out["color_f32"] = np.empty((H, W, 3), np.float32)
+    mh = _MeshHandle(mesh)
+    cs = camera_struct(cam)
+    os_ = option_struct(opt)
+    st = StatsS()
+    rc = lib.oracle_render(C.addressof(mh.s), C.addressof(cs), C.addressof(os_),
+                           _ptr(out.get("color")), _ptr(out.get("depth")),
+                           _ptr(out.get("normal")), _ptr(out.get("mask")),
+                           _ptr(out.get("face_id")), _ptr(out.get("color_f32")),
+                           C.addressof(st))
+    return rc, out, Stats(st.bbox_pixels, st.covered, st.special_candidates, st.texel_clamps)
+
+
+def ray_w(cam, x: int, y: int) -> np.ndarray:
+    lib = load()
+    cs = camera_struct(cam)
+    o = np.empty(3, np.float32)
+    lib.oracle_ray_w(C.addressof(cs), int(x), int(y), o.ctypes.data)
+    return o
+
+
+def interp_f64(mesh, cam, opt, face_id):
+    lib = load()
+    H, W = cam.height, cam.width
+    d = np.empty((H, W), np.float64)
+    n = np.empty((H, W, 3), np.float64)
+    c = np.empty((H, W, 3), np.float64)
+    mh = _MeshHandle(mesh)
+    cs = camera_struct(cam)
+    os_ = option_struct(opt)
+    fid = np.ascontiguousarray(face_id, dtype=np.int32)
+    lib.oracle_interp_f64(C.addressof(mh.s), C.addressof(cs), C.addressof(os_),
+                          fid.ctypes.data, d.ctypes.data, n.ctypes.data, c.ctypes.data)
+    return d, n, c
+
+
+def backward_f64(mesh, cam, opt, face_id, target, grad_tex=None, grad_vcolor=None,
+                 grad_vpos=None) -> float:
+    """Accumulates FP64 gradients into the given float64 arrays; returns the loss."""
+    lib = load()
+    mh = _MeshHandle(mesh)
+    cs = camera_struct(cam)
+    os_ = option_struct(opt)
+    fid = np.ascontiguousarray(face_id, dtype=np.int32)
+    tgt = np.ascontiguousarray(target, dtype=np.float32)
+    for a in (grad_tex, grad_vcolor, grad_vpos):
+        assert a is None or (a.dtype == np.float64 and a.flags.c_contiguous)
+    return lib.oracle_backward_f64(C.addressof(mh.s), C.addressof(cs), C.addressof(os_),
+                                   fid.ctypes.data, tgt.ctypes.data, _ptr(grad_tex),
+                                   _ptr(grad_vcolor), _ptr(grad_vpos))
+
+
+def calc_normals(vertices, faces):
+    lib = load()
+    v = np.ascontiguousarray(vertices, np.float32)
+    f = np.ascontiguousarray(faces, np.int32)
+    fn = np.empty((f.shape[0], 3), np.float32)
+    n = np.empty((v.shape[0], 3), np.float32)
+    lib.oracle_calc_normals(v.shape[0], v.ctypes.data, f.shape[0], f.ctypes.data,
+                            fn.ctypes.data, n.ctypes.data)
+    return fn, n

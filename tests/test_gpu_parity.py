@@ -1,0 +1,197 @@
+"""GPU vs oracle parity through the C ABI (libugugpu.so).
+
+face_id, mask, depth, normal and colour are compared bit for bit; only the
+Oren-Nayar shader (acos/sin/tan from two different math libraries) is
+allowed 1 LSB of 8-bit colour."""
+import numpy as np
+import pytest
+
+import adversarial as adv
+from gpu_helpers import compare, device_views, gpu_render
+from ugu_gb300 import capi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_lib):
+    from ugu_gb300.rasterizer import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    return torch
+
+
+def oracle_render(oracle_lib, m, cam, opt):
+    rc, ref, st = oracle_lib.render(m, cam, opt, color_f32=True)
+    assert rc == 0
+    return ref, st
+
+
+@pytest.mark.parametrize("optname", list(adv.OPTIONS))
+@pytest.mark.parametrize("scene", list(adv.ALL_SMALL))
+def test_small_scenes(ctx, oracle_lib, scene, optname):
+    cam = adv.identity_camera()
+    m = adv.ALL_SMALL[scene](cam)
+    opt = adv.OPTIONS[optname]
+    ref, _ = oracle_render(oracle_lib, m, cam, opt)
+    rc, got = gpu_render(ctx, m, cam, opt)
+    assert rc == 0, ctx.last_error()
+    compare(ref, got, f"{scene}/{optname}", color_tol=1 if opt.diffuse_shading == 2 else 0)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 4, 5, 6])
+def test_triangle_soup_seeds(ctx, oracle_lib, seed):
+    cam = adv.identity_camera(W=160, H=120, f=100.0)
+    m = adv.triangle_soup(cam, n_faces=3000, seed=seed)
+    for opt in (adv.option(2, 1, 1, 0, True), adv.option(1, 1, 0, 1, False)):
+        ref, _ = oracle_render(oracle_lib, m, cam, opt)
+        rc, got = gpu_render(ctx, m, cam, opt)
+        assert rc == 0, ctx.last_error()
+        compare(ref, got, f"soup{seed}")
+
+
+def test_uv_sphere_vertex_color_640x480(ctx, oracle_lib):
+    m, cam = scenes.scene_uv_sphere_vertex_color()
+    opt = adv.option(2, 1, 1, 0, True)
+    ref, st = oracle_render(oracle_lib, m, cam, opt)
+    rc, got = gpu_render(ctx, m, cam, opt)
+    assert rc == 0, ctx.last_error()
+    compare(ref, got, "uv_sphere")
+    assert (got["mask"] == 255).sum() > 90000
+
+
+def test_icosphere7_textured_1080p(ctx, oracle_lib):
+    m, cam = scenes.scene_icosphere_single_view()
+    opt = adv.option(1, 1, 1, 0, True)
+    ref, st = oracle_render(oracle_lib, m, cam, opt)
+    assert st.texel_clamps == 0
+    rc, got = gpu_render(ctx, m, cam, opt)
+    assert rc == 0, ctx.last_error()
+    compare(ref, got, "icosphere7")
+
+
+@pytest.mark.parametrize("tile_log2,small", [(3, 0), (4, 0), (5, 16), (6, 1 << 20)])
+def test_tuning_does_not_change_results(ctx, oracle_lib, tile_log2, small):
+    cam = adv.identity_camera(W=200, H=150, f=120.0)
+    m = adv.triangle_soup(cam, n_faces=800, seed=9)
+    opt = adv.option(2, 1, 1, 0, False)
+    ref, _ = oracle_render(oracle_lib, m, cam, opt)
+    t0 = ctx.tuning()
+    t = capi.Tuning(tile_log2, small, t0.group_pixels, t0.raster_ctas_per_sm)
+    ctx.check(ctx.set_tuning(t))
+    try:
+        rc, got = gpu_render(ctx, m, cam, opt)
+    finally:
+        ctx.check(ctx.set_tuning(t0))
+    assert rc == 0, ctx.last_error()
+    compare(ref, got, f"tile{tile_log2}/small{small}")
+
+
+def _ring(subdiv, n, seed=4):
+    m = scenes.icosphere_textured(subdiv, 256)
+    sizes = scenes.seeded_sizes(n, seed, [(160, 120), (320, 240), (400, 300), (240, 320)])
+    cams = scenes.ring_cameras(n, 3.0, sizes)
+    return m, cams
+
+
+@pytest.mark.parametrize("flags", [0, capi.PER_VIEW])
+def test_batched_views_two_meshes(ctx, oracle_lib, torch_cuda, flags):
+    torch = torch_cuda
+    m0, cams = _ring(5, 8)
+    m1, cam1 = scenes.scene_uv_sphere_vertex_color()
+    m1 = m1.copy()
+    m1.uv, m1.uv_indices = m0.uv[: 1], np.zeros_like(m1.vertex_indices)
+    m1.material_ids = np.zeros(m1.num_faces, np.int32)
+    m1.textures = m0.textures
+    m1.textures_f32 = [None]
+    ctx.check(ctx.set_mesh(0, m0))
+    ctx.check(ctx.set_mesh(1, m1))
+    opt = adv.option(1, 1, 1, 1, True)
+    from gpu_helpers import to_option
+    ctx.check(ctx.set_option(to_option(opt)))
+    all_cams = cams + [cam1]
+    slots = [0] * len(cams) + [1]
+    meshes = [m0] * len(cams) + [m1]
+    t = ctx.tuning()
+    small_groups = capi.Tuning(t.tile_log2, t.small_bbox_max, 100_000, t.raster_ctas_per_sm)
+    ctx.check(ctx.set_tuning(small_groups))  # several view groups
+    try:
+        tensors, views = device_views(torch, all_cams, slots)
+        rc = ctx.render_views(views, capi.DEVICE_POINTERS | flags)
+        assert rc == 0, ctx.last_error()
+        torch.cuda.synchronize()
+    finally:
+        ctx.check(ctx.set_tuning(t))
+    for i, (cam, mesh) in enumerate(zip(all_cams, meshes)):
+        ref, _ = oracle_render(oracle_lib, mesh, cam, opt)
+        got = {k: v.cpu().numpy() for k, v in tensors[i].items()}
+        compare(ref, got, f"view{i}")
+
+
+def test_graph_plan_replays(ctx, oracle_lib, torch_cuda):
+    torch = torch_cuda
+    m, cams = _ring(4, 6)
+    ctx.check(ctx.set_mesh(0, m))
+    opt = adv.option(1, 1, 1, 0, True)
+    from gpu_helpers import to_option
+    ctx.check(ctx.set_option(to_option(opt)))
+    tensors, views = device_views(torch, cams, [0] * len(cams))
+    plan = ctx.plan_create(views, capi.DEVICE_POINTERS)
+    try:
+        for rep in range(3):
+            for t in tensors:
+                for x in t.values():
+                    x.fill_(3)
+            ctx.check(plan.launch())
+            ctx.check(ctx.synchronize())
+            for i, cam in enumerate(cams):
+                ref, _ = oracle_render(oracle_lib, m, cam, opt)
+                compare(ref, {k: v.cpu().numpy() for k, v in tensors[i].items()}, f"rep{rep}/view{i}")
+    finally:
+        plan.close()
+
+
+def test_validation_errors(ctx):
+    cam = adv.identity_camera()
+    m = adv.shared_edge_quad(cam)
+    m2 = m.copy()
+    m2.vertex_colors = None
+    rc, _ = gpu_render(ctx, m2, cam, adv.option(diffuse_color=2))
+    assert rc == capi.ERR_NO_VERTEX_COLORS
+    m3 = m.copy()
+    m3.vertex_indices = m3.vertex_indices.copy()
+    m3.vertex_indices[1, 1] = 10_000
+    assert ctx.set_mesh(0, m3) == capi.ERR_INDEX_OUT_OF_RANGE
+    rc, _ = gpu_render(ctx, m, cam, adv.option(), outputs=())
+    assert rc == capi.ERR_NO_OUTPUT
+    # an empty slot is "mesh has not been initialized"
+    ctx.check(ctx.set_mesh(3, None))
+    rc, _ = gpu_render(ctx, m, cam, adv.option(), slot=3, upload=False)
+    assert rc == capi.ERR_NOT_PREPARED
+
+
+def test_python_rasterizer_mirror(gpu_lib, oracle_lib):
+    from ugu_gb300.rasterizer import Rasterizer, RendererCpuOption, DiffuseColor
+    m, cam = scenes.scene_uv_sphere_vertex_color()
+    r = Rasterizer(RendererCpuOption(diffuse_color=DiffuseColor.kVertex, oren_nayar_sigma=0.9))
+    ok, _ = r.Render(color=True)
+    assert not ok  # no camera yet
+    r.set_camera(cam)
+    ok, _ = r.Render(color=True)
+    assert not ok  # mesh not prepared
+    r.set_mesh(m)
+    assert r.PrepareMesh()
+    ok, out = r.Render(color=True, depth=True, normal=True, mask=True, face_id=True)
+    assert ok
+    ref, _ = oracle_render(oracle_lib, m, cam, adv.option(2, 1, 1, 0, True))
+    compare(ref, out, "mirror")
+    ok, outw = r.RenderW(depth=True)
+    assert ok and outw["depth"].dtype == np.uint16
+    assert np.array_equal(outw["depth"], np.trunc(ref["depth"]).astype(np.uint16))

@@ -1,0 +1,854 @@
+// capi.cu -- the C ABI of include/ugu_gpu.h: context, mesh upload,
+// validation, batched rendering, CUDA-graph plans.
+//
+// Validation follows ValidateAndInitBeforeRender
+// (src/renderer/cpu/util_private.cc:12-90) case by case and in the same
+// order; failures return the matching status code with the reference's
+// message in ugu_gpu_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+#include "ugu_gpu.h"
+
+using namespace ugu_gpu;
+
+namespace {
+
+constexpr int kMaxMeshes = 16;
+thread_local std::string g_create_error;
+
+struct MeshSlot {
+  bool present = false;
+  DevMesh dev{};
+  std::vector<void*> allocs;
+  bool has_fnormals = false, has_normals = false, has_vcolors = false;
+  bool has_uv = false, has_matids = false;
+  int num_materials = 0;
+  bool all_textures_nonempty = true;
+  bool all_textures_f32 = false;
+  int tex0_w = 0, tex0_h = 0;
+  size_t bytes = 0;
+};
+
+// Device scratch of one render sequence.  A plan owns its own so that later
+// renders on the context cannot move buffers a captured graph points at.
+struct Scratch {
+  unsigned long long* keys = nullptr;
+  size_t keys_cap = 0;
+  TileItem* items = nullptr;
+  size_t items_cap = 0;
+  DevCounters* counters = nullptr;
+  DevCounters* h_counters = nullptr;  // pinned
+  size_t counters_cap = 0;
+  DevView* d_views = nullptr;
+  DevView* h_views = nullptr;  // pinned
+  size_t views_cap = 0;
+  uint8_t* d_out = nullptr;  // device outputs of host-pointer renders
+  size_t d_out_cap = 0;
+  bool keys_dirty = false;
+};
+
+struct Group {
+  int first, count;
+  int max_faces;
+  int64_t max_pixels;
+};
+
+}  // namespace
+
+struct ugu_gpu_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  ugu_gpu_option opt{};
+  MeshSlot meshes[kMaxMeshes];
+  DevMesh* d_meshes = nullptr;
+  ugu_gpu_tuning tuning{};
+  Scratch scratch;
+  uint64_t launches = 0;
+  uint64_t special = 0;
+  uint64_t large_items = 0;
+  // counters of the last asynchronous plan replay, checked at synchronize
+  ugu_gpu_plan* pending_plan = nullptr;
+};
+
+struct ugu_gpu_plan {
+  ugu_gpu_context* ctx = nullptr;
+  Scratch scratch;
+  std::vector<Group> groups;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int kernels = 0;
+};
+
+namespace {
+
+int set_error(ugu_gpu_context* ctx, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx)
+    ctx->last_error = buf;
+  else
+    g_create_error = buf;
+  return code;
+}
+
+int cuda_fail(ugu_gpu_context* ctx, cudaError_t e, const char* what) {
+  int code = (e == cudaErrorMemoryAllocation) ? UGU_GPU_ERR_OUT_OF_MEMORY : UGU_GPU_ERR_CUDA;
+  return set_error(ctx, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(ctx, call, what)                            \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+  } while (0)
+
+void free_slot(MeshSlot& s) {
+  for (void* p : s.allocs) cudaFree(p);
+  s = MeshSlot();
+}
+
+void free_scratch(Scratch& s) {
+  cudaFree(s.keys);
+  cudaFree(s.items);
+  cudaFree(s.counters);
+  cudaFreeHost(s.h_counters);
+  cudaFree(s.d_views);
+  cudaFreeHost(s.h_views);
+  cudaFree(s.d_out);
+  s = Scratch();
+}
+
+template <typename T>
+int upload(ugu_gpu_context* ctx, MeshSlot& slot, const std::vector<T>& h, const T** out) {
+  *out = nullptr;
+  if (h.empty()) return UGU_GPU_OK;
+  void* p = nullptr;
+  CK(ctx, cudaMalloc(&p, h.size() * sizeof(T)), "cudaMalloc(mesh)");
+  slot.allocs.push_back(p);
+  slot.bytes += h.size() * sizeof(T);
+  CK(ctx, cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice),
+     "cudaMemcpy(mesh)");
+  *out = static_cast<const T*>(p);
+  return UGU_GPU_OK;
+}
+
+bool indices_ok(const int32_t* idx, int64_t n, int32_t limit) {
+  for (int64_t i = 0; i < n; ++i)
+    if (idx[i] < 0 || idx[i] >= limit) return false;
+  return true;
+}
+
+int check_option(ugu_gpu_context* ctx, const ugu_gpu_option& o) {
+  if (o.diffuse_color < 0 || o.diffuse_color > 2 || o.interp < 0 || o.interp > 1 ||
+      o.shading_normal < 0 || o.shading_normal > 1 || o.diffuse_shading < 0 ||
+      o.diffuse_shading > 2)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "option enum out of range");
+  return UGU_GPU_OK;
+}
+
+// ValidateAndInitBeforeRender (util_private.cc:19-67) for one view.
+int validate_view(ugu_gpu_context* ctx, const ugu_gpu_view& v, bool any_output) {
+  if (v.mesh < 0 || v.mesh >= kMaxMeshes || !ctx->meshes[v.mesh].present)
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh has not been initialized");
+  const MeshSlot& m = ctx->meshes[v.mesh];
+  const ugu_gpu_option& o = ctx->opt;
+  if (o.backface_culling && !m.has_fnormals)
+    return set_error(ctx, UGU_GPU_ERR_NO_FACE_NORMALS,
+                     "specified back-face culling but face normal is empty.");
+  if (o.diffuse_color == 1 && m.num_materials == 0)
+    return set_error(ctx, UGU_GPU_ERR_NO_TEXTURE,
+                     "specified texture as diffuse color but texture is empty.");
+  if (o.diffuse_color == 1 && !m.all_textures_nonempty)
+    return set_error(ctx, UGU_GPU_ERR_EMPTY_TEXTURE,
+                     "specified texture as diffuse color but a texture is empty.");
+  if (o.diffuse_color == 2 && !m.has_vcolors)
+    return set_error(ctx, UGU_GPU_ERR_NO_VERTEX_COLORS,
+                     "specified vertex color as diffuse color but vertex color is empty.");
+  if (o.shading_normal == 0 && !m.has_fnormals)
+    return set_error(ctx, UGU_GPU_ERR_NO_FACE_NORMALS_FOR_SHADING,
+                     "specified face normal as shading normal but face normal is empty.");
+  if (o.shading_normal == 1 && !m.has_normals)
+    return set_error(ctx, UGU_GPU_ERR_NO_VERTEX_NORMALS,
+                     "specified vertex normal as shading normal but vertex normal is empty.");
+  if (!any_output)
+    return set_error(ctx, UGU_GPU_ERR_NO_OUTPUT, "all arguments are nullptr. nothing to do");
+  // Preconditions the reference leaves undefined (it would read past its
+  // arrays): the z pass reads face normals for the back-face test; the
+  // texture path reads uv, uv_indices and material_ids.
+  if (!m.has_fnormals)
+    return set_error(ctx, UGU_GPU_ERR_NO_FACE_NORMALS,
+                     "face normals are required: the z pass reads them for every face");
+  if (o.diffuse_color == 1 && (!m.has_uv || !m.has_matids))
+    return set_error(ctx, UGU_GPU_ERR_NO_TEXTURE,
+                     "texture colour needs uv, uv_indices and material_ids");
+  const ugu_gpu_camera& c = v.camera;
+  if (c.width <= 0 || c.height <= 0 || (int64_t)c.width * c.height > (int64_t)1 << 31)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad image size %dx%d", c.width,
+                     c.height);
+  return UGU_GPU_OK;
+}
+
+bool any_image(const ugu_gpu_images& im) {
+  return im.color || im.depth || im.normal || im.mask || im.face_id || im.color_f32;
+}
+
+void fill_cam(Cam& d, const ugu_gpu_camera& c) {
+  d.width = c.width;
+  d.height = c.height;
+  d.fx = c.fx;
+  d.fy = c.fy;
+  d.cx = c.cx;
+  d.cy = c.cy;
+  std::memcpy(d.R, c.w2c_R, sizeof(d.R));
+  std::memcpy(d.t, c.w2c_t, sizeof(d.t));
+  std::memcpy(d.C, c.c2w_R, sizeof(d.C));
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t host_bytes_of_view(const ugu_gpu_images& im, int64_t px) {
+  size_t b = 0;
+  if (im.color) b += align256(3 * px);
+  if (im.depth) b += align256(4 * px);
+  if (im.normal) b += align256(12 * px);
+  if (im.mask) b += align256(px);
+  if (im.face_id) b += align256(4 * px);
+  if (im.color_f32) b += align256(12 * px);
+  return b;
+}
+
+std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views,
+                               bool per_view, int64_t group_pixels) {
+  std::vector<Group> g;
+  Group cur{0, 0, 0, 0};
+  int64_t acc = 0;
+  for (int i = 0; i < n; ++i) {
+    int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
+    bool full = cur.count > 0 && (per_view || acc + px > group_pixels);
+    if (full) {
+      g.push_back(cur);
+      cur = Group{i, 0, 0, 0};
+      acc = 0;
+    }
+    cur.count++;
+    acc += px;
+    cur.max_faces = std::max(cur.max_faces, ctx->meshes[views[i].mesh].dev.num_faces);
+    cur.max_pixels = std::max(cur.max_pixels, px);
+  }
+  if (cur.count) g.push_back(cur);
+  return g;
+}
+
+int64_t group_key_count(const std::vector<Group>& groups, const ugu_gpu_view* views) {
+  int64_t mx = 0;
+  for (const Group& gr : groups) {
+    int64_t acc = 0;
+    for (int i = gr.first; i < gr.first + gr.count; ++i)
+      acc += (int64_t)views[i].camera.width * views[i].camera.height;
+    mx = std::max(mx, acc);
+  }
+  return mx;
+}
+
+int ensure_scratch(ugu_gpu_context* ctx, Scratch& s, size_t nkeys, size_t nviews,
+                   size_t ngroups, size_t out_bytes) {
+  if (nkeys > s.keys_cap) {
+    cudaFree(s.keys);
+    s.keys = nullptr;
+    s.keys_cap = 0;
+    CK(ctx, cudaMalloc(&s.keys, nkeys * sizeof(unsigned long long)), "cudaMalloc(z-buffer)");
+    s.keys_cap = nkeys;
+    s.keys_dirty = true;
+  }
+  if (s.keys_dirty) {
+    CK(ctx, cudaMemsetAsync(s.keys, 0xff, s.keys_cap * sizeof(unsigned long long), ctx->stream),
+       "cudaMemsetAsync(z-buffer)");
+    s.keys_dirty = false;
+  }
+  if (s.items_cap == 0) {
+    size_t cap = size_t(1) << 22;
+    CK(ctx, cudaMalloc(&s.items, cap * sizeof(TileItem)), "cudaMalloc(tile items)");
+    s.items_cap = cap;
+  }
+  if (ngroups > s.counters_cap) {
+    cudaFree(s.counters);
+    cudaFreeHost(s.h_counters);
+    s.counters = nullptr;
+    s.h_counters = nullptr;
+    s.counters_cap = 0;
+    CK(ctx, cudaMalloc(&s.counters, ngroups * sizeof(DevCounters)), "cudaMalloc(counters)");
+    CK(ctx, cudaMallocHost(&s.h_counters, ngroups * sizeof(DevCounters)),
+       "cudaMallocHost(counters)");
+    s.counters_cap = ngroups;
+  }
+  if (nviews > s.views_cap) {
+    cudaFree(s.d_views);
+    cudaFreeHost(s.h_views);
+    s.d_views = nullptr;
+    s.h_views = nullptr;
+    s.views_cap = 0;
+    CK(ctx, cudaMalloc(&s.d_views, nviews * sizeof(DevView)), "cudaMalloc(views)");
+    CK(ctx, cudaMallocHost(&s.h_views, nviews * sizeof(DevView)), "cudaMallocHost(views)");
+    s.views_cap = nviews;
+  }
+  if (out_bytes > s.d_out_cap) {
+    cudaFree(s.d_out);
+    s.d_out = nullptr;
+    s.d_out_cap = 0;
+    CK(ctx, cudaMalloc(&s.d_out, out_bytes), "cudaMalloc(output staging)");
+    s.d_out_cap = out_bytes;
+  }
+  return UGU_GPU_OK;
+}
+
+RenderParams base_params(ugu_gpu_context* ctx, const Scratch& s) {
+  RenderParams p{};
+  const ugu_gpu_option& o = ctx->opt;
+  p.meshes = ctx->d_meshes;
+  p.diffuse_color = o.diffuse_color;
+  p.interp = o.interp;
+  p.shading_normal = o.shading_normal;
+  p.diffuse_shading = o.diffuse_shading;
+  p.backface_culling = o.backface_culling ? 1 : 0;
+  // OrenNayarParam (pixel_shader.h:143-148)
+  float sigma_2 = o.oren_nayar_sigma * o.oren_nayar_sigma;
+  p.on_A = 1.0f - (0.5f * sigma_2 / (sigma_2 + 0.33f));
+  p.on_B = 0.45f * sigma_2 / (sigma_2 + 0.09f);
+  p.keys = s.keys;
+  p.items = s.items;
+  p.item_capacity = (int64_t)s.items_cap;
+  p.tile_log2 = ctx->tuning.tile_log2;
+  p.small_bbox_max = ctx->tuning.small_bbox_max;
+  return p;
+}
+
+// Enqueue the kernels of every group (no synchronisation).
+int enqueue_groups(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
+                   const ugu_gpu_view* views, int* kernels) {
+  RenderParams base = base_params(ctx, s);
+  int nk = 0;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const Group& gr = groups[gi];
+    RenderParams p = base;
+    p.views = s.d_views + gr.first;
+    p.num_views = gr.count;
+    p.counters = s.counters + gi;
+    launch_raster(p, gr.max_faces, ctx->num_sms, ctx->stream);
+    launch_tiles(p, ctx->num_sms * 8, ctx->stream);
+    launch_resolve(p, gr.max_pixels, ctx->stream);
+    nk += 3;
+  }
+  (void)views;
+  CK(ctx, cudaGetLastError(), "kernel launch");
+  *kernels = nk;
+  return UGU_GPU_OK;
+}
+
+// Fill s.h_views for the views; host-pointer outputs get device staging.
+void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
+                const ugu_gpu_view* views, bool device_ptrs) {
+  (void)ctx;
+  size_t off = 0;
+  for (const Group& gr : groups) {
+    int64_t key_off = 0;
+    for (int i = gr.first; i < gr.first + gr.count; ++i) {
+      const ugu_gpu_view& v = views[i];
+      DevView& d = s.h_views[i];
+      std::memset(&d, 0, sizeof(d));
+      fill_cam(d.cam, v.camera);
+      d.mesh = v.mesh;
+      d.key_offset = key_off;
+      int64_t px = (int64_t)v.camera.width * v.camera.height;
+      key_off += px;
+      if (device_ptrs) {
+        d.color = v.images.color;
+        d.depth = v.images.depth;
+        d.normal = v.images.normal;
+        d.mask = v.images.mask;
+        d.face_id = v.images.face_id;
+        d.color_f32 = v.images.color_f32;
+      } else {
+        auto take = [&](size_t bytes) {
+          uint8_t* p = s.d_out + off;
+          off += align256(bytes);
+          return p;
+        };
+        if (v.images.color) d.color = take(3 * px);
+        if (v.images.depth) d.depth = reinterpret_cast<float*>(take(4 * px));
+        if (v.images.normal) d.normal = reinterpret_cast<float*>(take(12 * px));
+        if (v.images.mask) d.mask = take(px);
+        if (v.images.face_id) d.face_id = reinterpret_cast<int32_t*>(take(4 * px));
+        if (v.images.color_f32) d.color_f32 = reinterpret_cast<float*>(take(12 * px));
+      }
+    }
+  }
+}
+
+int copy_back(ugu_gpu_context* ctx, const Scratch& s, int n, const ugu_gpu_view* views) {
+  for (int i = 0; i < n; ++i) {
+    const DevView& d = s.h_views[i];
+    const ugu_gpu_images& im = views[i].images;
+    int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
+    auto cp = [&](void* dst, const void* src, size_t bytes) -> int {
+      if (!dst) return UGU_GPU_OK;
+      CK(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream),
+         "cudaMemcpyAsync(output)");
+      return UGU_GPU_OK;
+    };
+    int rc;
+    if ((rc = cp(im.color, d.color, 3 * px))) return rc;
+    if ((rc = cp(im.depth, d.depth, 4 * px))) return rc;
+    if ((rc = cp(im.normal, d.normal, 12 * px))) return rc;
+    if ((rc = cp(im.mask, d.mask, px))) return rc;
+    if ((rc = cp(im.face_id, d.face_id, 4 * px))) return rc;
+    if ((rc = cp(im.color_f32, d.color_f32, 12 * px))) return rc;
+  }
+  return UGU_GPU_OK;
+}
+
+int check_counters(ugu_gpu_context* ctx, const Scratch& s, size_t ngroups) {
+  uint64_t special = 0, overflow = 0, items = 0;
+  for (size_t g = 0; g < ngroups; ++g) {
+    special += s.h_counters[g].special;
+    overflow += s.h_counters[g].overflow;
+    items += s.h_counters[g].tile_items;
+  }
+  ctx->special += special;
+  ctx->large_items = items;
+  if (overflow)
+    return set_error(ctx, UGU_GPU_ERR_CAPACITY, "%llu tile items exceeded the capacity",
+                     (unsigned long long)overflow);
+  if (special)
+    return set_error(ctx, UGU_GPU_ERR_DEGENERATE_DEPTH,
+                     "%llu covered samples had depth < FLT_MIN or NaN (a vertex at z ~ 0)",
+                     (unsigned long long)special);
+  return UGU_GPU_OK;
+}
+
+int validate_views(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views) {
+  int rc = check_option(ctx, ctx->opt);
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) {
+    rc = validate_view(ctx, views[i], any_image(views[i].images));
+    if (rc) return rc;
+  }
+  return UGU_GPU_OK;
+}
+
+int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t flags) {
+  if (n < 0 || (n > 0 && !views))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view list");
+  if (n == 0) return UGU_GPU_OK;
+  int rc = validate_views(ctx, n, views);
+  if (rc) return rc;
+  const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
+  if ((flags & UGU_GPU_ASYNC) && !dev)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "UGU_GPU_ASYNC needs device pointers");
+  std::vector<Group> groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0,
+                                          ctx->tuning.group_pixels);
+  size_t out_bytes = 0;
+  if (!dev)
+    for (int i = 0; i < n; ++i)
+      out_bytes += host_bytes_of_view(views[i].images,
+                                      (int64_t)views[i].camera.width * views[i].camera.height);
+  Scratch& s = ctx->scratch;
+  rc = ensure_scratch(ctx, s, (size_t)group_key_count(groups, views), (size_t)n, groups.size(),
+                      out_bytes);
+  if (rc) return rc;
+  // The pinned view table may still be read by a previous asynchronous copy.
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  fill_views(ctx, s, groups, views, dev);
+  CK(ctx, cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView), cudaMemcpyHostToDevice,
+                          ctx->stream),
+     "cudaMemcpyAsync(views)");
+  CK(ctx, cudaMemsetAsync(s.counters, 0, groups.size() * sizeof(DevCounters), ctx->stream),
+     "cudaMemsetAsync(counters)");
+  int kernels = 0;
+  rc = enqueue_groups(ctx, s, groups, views, &kernels);
+  if (rc) {
+    s.keys_dirty = true;
+    return rc;
+  }
+  ctx->launches += kernels;
+  if (!dev) {
+    rc = copy_back(ctx, s, n, views);
+    if (rc) return rc;
+  }
+  CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, groups.size() * sizeof(DevCounters),
+                          cudaMemcpyDeviceToHost, ctx->stream),
+     "cudaMemcpyAsync(counters)");
+  if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "render");
+  rc = check_counters(ctx, s, groups.size());
+  if (rc == UGU_GPU_ERR_CAPACITY) s.keys_dirty = true;
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ugu_gpu_abi_version(void) { return UGU_GPU_ABI_VERSION; }
+
+const char* ugu_gpu_last_error(const ugu_gpu_context* ctx) {
+  return ctx ? ctx->last_error.c_str() : g_create_error.c_str();
+}
+
+int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
+  if (!out) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0)
+    return set_error(nullptr, UGU_GPU_ERR_NO_DEVICE, "no CUDA device: %s",
+                     e == cudaSuccess ? "count is 0" : cudaGetErrorString(e));
+  if (device < 0 || device >= count)
+    return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "device %d of %d", device, count);
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return set_error(nullptr, UGU_GPU_ERR_CUDA, "cudaSetDevice: %s",
+                                         cudaGetErrorString(e));
+  ugu_gpu_context* ctx = new ugu_gpu_context();
+  ctx->device = device;
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_meshes, kMaxMeshes * sizeof(DevMesh));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_meshes, 0, kMaxMeshes * sizeof(DevMesh));
+  if (e != cudaSuccess) {
+    set_error(nullptr, UGU_GPU_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    cudaFree(ctx->d_meshes);
+    delete ctx;
+    return UGU_GPU_ERR_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  ctx->opt.diffuse_color = 0;
+  ctx->opt.interp = 1;
+  ctx->opt.shading_normal = 1;
+  ctx->opt.diffuse_shading = 0;
+  ctx->opt.depth_scale = 1.0f;
+  ctx->opt.backface_culling = 1;
+  ctx->opt.oren_nayar_sigma = 0.3f;
+  ctx->tuning.tile_log2 = 4;
+  ctx->tuning.small_bbox_max = 256;
+  ctx->tuning.group_pixels = 4 << 20;
+  ctx->tuning.raster_ctas_per_sm = 8;
+  *out = ctx;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_destroy(ugu_gpu_context* ctx) {
+  if (!ctx) return UGU_GPU_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (MeshSlot& s : ctx->meshes) free_slot(s);
+  free_scratch(ctx->scratch);
+  cudaFree(ctx->d_meshes);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_set_option(ugu_gpu_context* ctx, const ugu_gpu_option* opt) {
+  if (!ctx || !opt) return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL argument");
+  int rc = check_option(ctx, *opt);
+  if (rc) return rc;
+  ctx->opt = *opt;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  if (slot < 0 || slot >= kMaxMeshes)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "mesh slot %d out of [0, %d)", slot,
+                     kMaxMeshes);
+  cudaSetDevice(ctx->device);
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  MeshSlot& s = ctx->meshes[slot];
+  free_slot(s);
+  DevMesh empty{};
+  CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &empty, sizeof(DevMesh), cudaMemcpyHostToDevice),
+     "cudaMemcpy(mesh table)");
+  if (!m) return UGU_GPU_OK;
+  if (m->num_vertices < 0 || m->num_faces < 0 || m->num_normals < 0 || m->num_uv < 0 ||
+      m->num_materials < 0)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "negative count");
+  if ((m->num_vertices && !m->vertices) || (m->num_faces && !m->vertex_indices))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "vertices or faces are NULL");
+  const int64_t F = m->num_faces, V = m->num_vertices;
+  if (!indices_ok(m->vertex_indices, 3 * F, m->num_vertices))
+    return set_error(ctx, UGU_GPU_ERR_INDEX_OUT_OF_RANGE, "vertex index out of range");
+  const bool has_normals = m->num_normals > 0 && m->normals && m->normal_indices;
+  if (has_normals && !indices_ok(m->normal_indices, 3 * F, m->num_normals))
+    return set_error(ctx, UGU_GPU_ERR_INDEX_OUT_OF_RANGE, "normal index out of range");
+  const bool has_uv = m->num_uv > 0 && m->uv && m->uv_indices;
+  if (has_uv && !indices_ok(m->uv_indices, 3 * F, m->num_uv))
+    return set_error(ctx, UGU_GPU_ERR_INDEX_OUT_OF_RANGE, "uv index out of range");
+  if (m->material_ids && !indices_ok(m->material_ids, F, std::max(m->num_materials, 0)))
+    return set_error(ctx, UGU_GPU_ERR_INDEX_OUT_OF_RANGE, "material id out of range");
+  if (m->num_materials > 0 && !m->materials)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "materials is NULL");
+
+  std::vector<float4> v4(V);
+  for (int64_t i = 0; i < V; ++i)
+    v4[i] = make_float4(m->vertices[3 * i], m->vertices[3 * i + 1], m->vertices[3 * i + 2], 0.f);
+  auto pad3i = [&](const int32_t* a) {
+    std::vector<int4> o(F);
+    for (int64_t i = 0; i < F; ++i) o[i] = make_int4(a[3 * i], a[3 * i + 1], a[3 * i + 2], 0);
+    return o;
+  };
+  auto pad3f = [&](const float* a, int64_t n) {
+    std::vector<float4> o(n);
+    for (int64_t i = 0; i < n; ++i) o[i] = make_float4(a[3 * i], a[3 * i + 1], a[3 * i + 2], 0.f);
+    return o;
+  };
+  int rc;
+  DevMesh& d = s.dev;
+  d.num_vertices = m->num_vertices;
+  d.num_faces = m->num_faces;
+  if ((rc = upload(ctx, s, v4, &d.vertices))) return rc;
+  if ((rc = upload(ctx, s, pad3i(m->vertex_indices), &d.vidx))) return rc;
+  if (m->face_normals && F > 0) {
+    if ((rc = upload(ctx, s, pad3f(m->face_normals, F), &d.fnormals))) return rc;
+    s.has_fnormals = true;
+  }
+  if (has_normals) {
+    d.num_normals = m->num_normals;
+    if ((rc = upload(ctx, s, pad3f(m->normals, m->num_normals), &d.normals))) return rc;
+    if ((rc = upload(ctx, s, pad3i(m->normal_indices), &d.nidx))) return rc;
+    s.has_normals = true;
+  }
+  if (m->vertex_colors && V > 0) {
+    if ((rc = upload(ctx, s, pad3f(m->vertex_colors, V), &d.vcolors))) return rc;
+    s.has_vcolors = true;
+  }
+  if (has_uv) {
+    d.num_uv = m->num_uv;
+    std::vector<float2> uv(m->num_uv);
+    for (int i = 0; i < m->num_uv; ++i) uv[i] = make_float2(m->uv[2 * i], m->uv[2 * i + 1]);
+    if ((rc = upload(ctx, s, uv, &d.uv))) return rc;
+    if ((rc = upload(ctx, s, pad3i(m->uv_indices), &d.uvidx))) return rc;
+    s.has_uv = true;
+  }
+  if (m->material_ids && F > 0) {
+    std::vector<int32_t> mi(m->material_ids, m->material_ids + F);
+    if ((rc = upload(ctx, s, mi, &d.mat_ids))) return rc;
+    s.has_matids = true;
+  }
+  s.num_materials = m->num_materials;
+  d.num_materials = m->num_materials;
+  if (m->num_materials > 0) {
+    std::vector<DevTexture> tex(m->num_materials);
+    s.all_textures_f32 = true;
+    for (int i = 0; i < m->num_materials; ++i) {
+      const ugu_gpu_texture& t = m->materials[i];
+      DevTexture& dt = tex[i];
+      dt.width = t.width;
+      dt.height = t.height;
+      dt.rgba8 = nullptr;
+      dt.rgbf = nullptr;
+      if (t.width < 1 || t.height < 1 || (!t.rgb8 && !t.rgb_f32)) {
+        s.all_textures_nonempty = false;
+        s.all_textures_f32 = false;
+        continue;
+      }
+      const int64_t n = (int64_t)t.width * t.height;
+      if (t.rgb8) {
+        std::vector<uint32_t> rgba(n);
+        for (int64_t k = 0; k < n; ++k)
+          rgba[k] = (uint32_t)t.rgb8[3 * k] | ((uint32_t)t.rgb8[3 * k + 1] << 8) |
+                    ((uint32_t)t.rgb8[3 * k + 2] << 16);
+        if ((rc = upload(ctx, s, rgba, &dt.rgba8))) return rc;
+      }
+      if (t.rgb_f32) {
+        std::vector<float> f(t.rgb_f32, t.rgb_f32 + 3 * n);
+        if ((rc = upload(ctx, s, f, &dt.rgbf))) return rc;
+      } else {
+        s.all_textures_f32 = false;
+      }
+      if (i == 0) {
+        s.tex0_w = t.width;
+        s.tex0_h = t.height;
+      }
+    }
+    if ((rc = upload(ctx, s, tex, &d.textures))) return rc;
+  }
+  CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &d, sizeof(DevMesh), cudaMemcpyHostToDevice),
+     "cudaMemcpy(mesh table)");
+  s.present = true;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_render(ugu_gpu_context* ctx, int32_t mesh, const ugu_gpu_camera* cam,
+                   const ugu_gpu_images* images) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  if (!cam) return set_error(ctx, UGU_GPU_ERR_NO_CAMERA, "camera has not been set");
+  if (!images) return set_error(ctx, UGU_GPU_ERR_NO_OUTPUT, "all arguments are nullptr. nothing to do");
+  cudaSetDevice(ctx->device);
+  ugu_gpu_view v;
+  v.mesh = mesh;
+  v.camera = *cam;
+  v.images = *images;
+  return render_impl(ctx, 1, &v, 0);
+}
+
+int ugu_gpu_render_views(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                         uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  cudaSetDevice(ctx->device);
+  return render_impl(ctx, n, views, flags);
+}
+
+int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                        uint32_t flags, ugu_gpu_plan** out) {
+  if (!ctx || !out || n <= 0 || !views)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad plan arguments");
+  *out = nullptr;
+  if (!(flags & UGU_GPU_DEVICE_POINTERS))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "a plan needs device pointers");
+  cudaSetDevice(ctx->device);
+  int rc = validate_views(ctx, n, views);
+  if (rc) return rc;
+  ugu_gpu_plan* plan = new ugu_gpu_plan();
+  plan->ctx = ctx;
+  plan->groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0,
+                             ctx->tuning.group_pixels);
+  Scratch& s = plan->scratch;
+  rc = ensure_scratch(ctx, s, (size_t)group_key_count(plan->groups, views), (size_t)n,
+                      plan->groups.size(), 0);
+  if (!rc) {
+    fill_views(ctx, s, plan->groups, views, true);
+    cudaError_t e = cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plan views");
+  }
+  if (!rc) {
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaStreamBeginCapture");
+  }
+  if (!rc) {
+    cudaMemsetAsync(s.counters, 0, plan->groups.size() * sizeof(DevCounters), ctx->stream);
+    int k = 0;
+    rc = enqueue_groups(ctx, s, plan->groups, views, &k);
+    plan->kernels = k;
+    cudaMemcpyAsync(s.h_counters, s.counters, plan->groups.size() * sizeof(DevCounters),
+                    cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &plan->graph);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaStreamEndCapture");
+  }
+  if (!rc) {
+    cudaError_t e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaGraphInstantiate");
+  }
+  if (rc) {
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    if (plan->graph) cudaGraphDestroy(plan->graph);
+    free_scratch(plan->scratch);
+    delete plan;
+    return rc;
+  }
+  *out = plan;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_plan_launch(ugu_gpu_plan* plan) {
+  if (!plan) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL plan");
+  ugu_gpu_context* ctx = plan->ctx;
+  CK(ctx, cudaGraphLaunch(plan->exec, ctx->stream), "cudaGraphLaunch");
+  ctx->launches += plan->kernels;
+  ctx->pending_plan = plan;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_plan_destroy(ugu_gpu_plan* plan) {
+  if (!plan) return UGU_GPU_OK;
+  ugu_gpu_context* ctx = plan->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->pending_plan == plan) ctx->pending_plan = nullptr;
+  cudaGraphExecDestroy(plan->exec);
+  cudaGraphDestroy(plan->graph);
+  free_scratch(plan->scratch);
+  delete plan;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_synchronize(ugu_gpu_context* ctx) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (ctx->pending_plan) {
+    ugu_gpu_plan* p = ctx->pending_plan;
+    ctx->pending_plan = nullptr;
+    return check_counters(ctx, p->scratch, p->groups.size());
+  }
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
+  if (!ctx || !t) return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (t->tile_log2 < 3 || t->tile_log2 > 6 || t->small_bbox_max < 0 || t->group_pixels < 1 ||
+      t->raster_ctas_per_sm < 1)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "tuning out of range");
+  ctx->tuning = *t;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_get_tuning(const ugu_gpu_context* ctx, ugu_gpu_tuning* t) {
+  if (!ctx || !t) return UGU_GPU_ERR_INVALID_ARGUMENT;
+  *t = ctx->tuning;
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                     ugu_gpu_tuning* chosen) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  (void)n;
+  (void)views;
+  if (chosen) *chosen = ctx->tuning;
+  return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "autotune is not built yet");
+}
+
+int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
+                     const float* const* targets, float* grad_texels,
+                     float* grad_vertex_colors, float* grad_vertices, float* loss_out,
+                     uint32_t flags) {
+  (void)n; (void)views; (void)targets; (void)grad_texels; (void)grad_vertex_colors;
+  (void)grad_vertices; (void)loss_out; (void)flags;
+  return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "backward is not built yet");
+}
+
+int ugu_gpu_get_stats(const ugu_gpu_context* ctx, ugu_gpu_stats* st) {
+  if (!ctx || !st) return UGU_GPU_ERR_INVALID_ARGUMENT;
+  st->launches = ctx->launches;
+  st->special_candidates = ctx->special;
+  st->large_face_tiles = ctx->large_items;
+  uint64_t b = 0;
+  for (const MeshSlot& m : ctx->meshes) b += m.bytes;
+  const Scratch& s = ctx->scratch;
+  b += s.keys_cap * 8 + s.items_cap * sizeof(TileItem) + s.d_out_cap;
+  st->device_bytes = b;
+  return UGU_GPU_OK;
+}
+
+}  // extern "C"

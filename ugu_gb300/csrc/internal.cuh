@@ -1,0 +1,89 @@
+// internal.cuh -- device-side data layout shared by the kernels and the C ABI.
+//
+// HBM layout of a mesh slot (uploaded once by ugu_gpu_set_mesh):
+//   vertices       V x float4 (x, y, z, 0)      16-byte vector loads
+//   vertex_indices F x int4   (i0, i1, i2, 0)
+//   face_normals   F x float4
+//   normals        N x float4,  normal_indices F x int4
+//   vertex_colors  V x float4
+//   uv             T x float2,  uv_indices     F x int4
+//   material_ids   F x int32
+//   textures       per material: RGBA8 texels (uint32, alpha 0) and/or RGB f32
+// Per view: a Cam (floats exactly as the host computed them) and output
+// pointers.  Z-buffer: one 64-bit key per pixel of the current view group.
+#pragma once
+
+#include <cstdint>
+
+#include "exact.cuh"
+
+namespace ugu_gpu {
+
+struct DevTexture {
+  int32_t width, height;
+  const uint32_t* rgba8;  // texel i at rgba8[i]: r | g << 8 | b << 16
+  const float* rgbf;      // texel i at rgbf[3 i .. 3 i + 2]
+};
+
+struct DevMesh {
+  int32_t num_vertices, num_faces, num_normals, num_uv, num_materials;
+  const float4* vertices;
+  const int4* vidx;
+  const float4* fnormals;
+  const float4* normals;
+  const int4* nidx;
+  const float4* vcolors;
+  const float2* uv;
+  const int4* uvidx;
+  const int32_t* mat_ids;
+  const DevTexture* textures;
+};
+
+struct DevView {
+  Cam cam;
+  int32_t mesh;
+  int32_t pad_;
+  int64_t key_offset;  // first z-buffer key of this view within its group
+  uint8_t* color;
+  float* depth;
+  float* normal;
+  uint8_t* mask;
+  int32_t* face_id;
+  float* color_f32;
+};
+
+// Counters shared by the kernels of one render (device memory).
+struct DevCounters {
+  unsigned long long special;     // covered samples with unorderable depth
+  unsigned long long tile_items;  // (face, tile) items appended this group
+  unsigned long long overflow;    // items dropped for lack of capacity
+  unsigned long long pad;
+};
+
+struct TileItem {
+  int32_t view;  // view index within the group
+  int32_t face;
+  int32_t tx, ty;  // tile coordinates
+};
+
+struct RenderParams {
+  const DevMesh* meshes;
+  const DevView* views;  // views of this group
+  int32_t num_views;
+  int32_t diffuse_color, interp, shading_normal, diffuse_shading, backface_culling;
+  float on_A, on_B;
+  unsigned long long* keys;
+  DevCounters* counters;
+  TileItem* items;
+  int64_t item_capacity;
+  int32_t tile_log2;
+  int32_t small_bbox_max;
+};
+
+// Host-side launchers (raster.cu).
+void launch_raster(const RenderParams& p, int max_faces, int num_sms, cudaStream_t s);
+void launch_tiles(const RenderParams& p, int grid, cudaStream_t s);
+void launch_resolve(const RenderParams& p, int64_t max_pixels, cudaStream_t s);
+int raster_launches_per_group();
+
+}  // namespace ugu_gpu

@@ -1,0 +1,287 @@
+"""Python host side of the GB300 rasterizer.
+
+``Context`` owns one ugu_gpu_context (include/ugu_gpu.h).  ``Rasterizer``
+mirrors ugu::Rasterizer (include/ugu/renderer/cpu/rasterizer.h:14-53) --
+set_option / set_mesh / PrepareMesh / set_camera / Render / RenderW and the
+single-output variants -- with the reference's error behaviour: a failed
+precondition logs the reference's message and returns False.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+
+
+class DiffuseColor:  # include/ugu/renderer/base.h:11-16
+    kNone, kTexture, kVertex = 0, 1, 2
+
+
+class ColorInterpolation:  # include/ugu/common.h:50-53
+    kNn, kBilinear = 0, 1
+
+
+class ShadingNormal:  # include/ugu/renderer/base.h:18-22
+    kFace, kVertex = 0, 1
+
+
+class DiffuseShading:  # include/ugu/renderer/base.h:24-32
+    kNone, kLambertian, kOrenNayar = 0, 1, 2
+
+
+@dataclass
+class RendererCpuOption:
+    """include/ugu/renderer/cpu/renderer.h:17-38 (same fields and defaults)."""
+    diffuse_color: int = DiffuseColor.kNone
+    interp: int = ColorInterpolation.kBilinear
+    shading_normal: int = ShadingNormal.kVertex
+    diffuse_shading: int = DiffuseShading.kNone
+    depth_scale: float = 1.0
+    backface_culling: bool = True
+    oren_nayar_sigma: float = 0.3
+
+    def CopyTo(self, dst: "RendererCpuOption") -> None:
+        """renderer.h:30-37: copies every field except oren_nayar_sigma."""
+        dst.diffuse_color = self.diffuse_color
+        dst.depth_scale = self.depth_scale
+        dst.interp = self.interp
+        dst.shading_normal = self.shading_normal
+        dst.diffuse_shading = self.diffuse_shading
+        dst.backface_culling = self.backface_culling
+
+    def to_struct(self) -> capi.Option:
+        o = capi.Option()
+        o.diffuse_color = int(self.diffuse_color)
+        o.interp = int(self.interp)
+        o.shading_normal = int(self.shading_normal)
+        o.diffuse_shading = int(self.diffuse_shading)
+        o.depth_scale = float(self.depth_scale)
+        o.backface_culling = 1 if self.backface_culling else 0
+        o.oren_nayar_sigma = float(self.oren_nayar_sigma)
+        return o
+
+
+def LOGE(msg: str) -> None:  # src/log.cc:21-62 error level
+    sys.stderr.write(msg if msg.endswith("\n") else msg + "\n")
+
+
+LOGW = LOGE
+
+
+class Context:
+    """One ugu_gpu_context on a device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        rc = self.lib.ugu_gpu_create(int(device), C.byref(h))
+        if rc != capi.OK:
+            raise capi.GpuError(rc, self.lib.ugu_gpu_last_error(None).decode())
+        self.h = h
+        self._uploads = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ugu_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self) -> str:
+        return self.lib.ugu_gpu_last_error(self.h).decode()
+
+    def check(self, rc: int):
+        if rc != capi.OK:
+            raise capi.GpuError(rc, self.last_error())
+        return rc
+
+    def set_option(self, opt: RendererCpuOption) -> int:
+        s = opt.to_struct()
+        return self.lib.ugu_gpu_set_option(self.h, C.byref(s))
+
+    def set_mesh(self, slot: int, mesh) -> int:
+        if mesh is None:
+            self._uploads.pop(slot, None)
+            return self.lib.ugu_gpu_set_mesh(self.h, int(slot), None)
+        up = capi.MeshUpload(mesh)
+        rc = self.lib.ugu_gpu_set_mesh(self.h, int(slot), C.byref(up.desc))
+        return rc
+
+    def render(self, slot: int, cam, images: capi.Images) -> int:
+        cs = capi.camera_struct(cam)
+        return self.lib.ugu_gpu_render(self.h, int(slot), C.byref(cs), C.byref(images))
+
+    def render_views(self, views, flags: int) -> int:
+        arr = (capi.View * len(views))(*views)
+        return self.lib.ugu_gpu_render_views(self.h, len(views), C.addressof(arr), int(flags))
+
+    def plan_create(self, views, flags: int):
+        arr = (capi.View * len(views))(*views)
+        h = C.c_void_p()
+        self.check(self.lib.ugu_gpu_plan_create(self.h, len(views), C.addressof(arr), int(flags),
+                                                C.byref(h)))
+        return Plan(self, h)
+
+    def synchronize(self) -> int:
+        return self.lib.ugu_gpu_synchronize(self.h)
+
+    def set_stream(self, stream_handle: int | None) -> int:
+        return self.lib.ugu_gpu_set_stream(self.h, stream_handle)
+
+    def tuning(self) -> capi.Tuning:
+        t = capi.Tuning()
+        self.check(self.lib.ugu_gpu_get_tuning(self.h, C.byref(t)))
+        return t
+
+    def set_tuning(self, t: capi.Tuning) -> int:
+        return self.lib.ugu_gpu_set_tuning(self.h, C.byref(t))
+
+    def stats(self) -> capi.Stats:
+        s = capi.Stats()
+        self.check(self.lib.ugu_gpu_get_stats(self.h, C.byref(s)))
+        return s
+
+
+class Plan:
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    def launch(self) -> int:
+        return self.ctx.lib.ugu_gpu_plan_launch(self.h)
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.ugu_gpu_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _out(arg, shape, dtype):
+    """None -> skip; True -> allocate; ndarray -> fill in place (reallocated
+    when its shape or dtype differ, as ugu::Init does)."""
+    if arg is None or arg is False:
+        return None
+    if isinstance(arg, np.ndarray) and arg.shape == shape and arg.dtype == dtype \
+            and arg.flags.c_contiguous:
+        return arg
+    return np.empty(shape, dtype)
+
+
+class Rasterizer:
+    """ugu::Rasterizer's interface over the GPU (rasterizer.h:14-53)."""
+
+    def __init__(self, option: RendererCpuOption | None = None, device: int = 0):
+        self._ctx = Context(device)
+        self._option = RendererCpuOption()
+        self._mesh = None
+        self._mesh_initialized = False
+        self._camera = None
+        if option is not None:
+            self.set_option(option)
+
+    def set_option(self, option: RendererCpuOption) -> None:  # rasterizer.cc:73-75
+        option.CopyTo(self._option)
+
+    def set_mesh(self, mesh) -> None:  # rasterizer.cc:77-88
+        self._mesh_initialized = False
+        self._mesh = mesh
+        if mesh.face_normals is None or len(mesh.face_normals) == 0:
+            LOGW("face normal is empty. culling and shading may not work\n")
+        if mesh.normals is None or len(mesh.normals) == 0:
+            LOGW("vertex normal is empty. shading may not work\n")
+
+    def PrepareMesh(self) -> bool:  # rasterizer.cc:90-99
+        if self._mesh is None:
+            LOGE("mesh has not been set\n")
+            return False
+        rc = self._ctx.set_mesh(0, self._mesh)
+        if rc != capi.OK:
+            LOGE(self._ctx.last_error())
+            return False
+        self._mesh_initialized = True
+        return True
+
+    def set_camera(self, camera) -> None:  # rasterizer.cc:101-103
+        self._camera = camera
+
+    def Render(self, color=None, depth=None, normal=None, mask=None, face_id=None,
+               color_f32=None):
+        """rasterizer.cc:105-307.  Returns (ok, {name: image})."""
+        if self._camera is None:
+            LOGE("camera has not been set\n")
+            return False, {}
+        if not self._mesh_initialized:
+            LOGE("mesh has not been initialized\n")
+            return False, {}
+        rc = self._ctx.set_option(self._option)
+        if rc != capi.OK:
+            LOGE(self._ctx.last_error())
+            return False, {}
+        H, W = self._camera.height, self._camera.width
+        outs = {
+            "color": _out(color, (H, W, 3), np.uint8),
+            "depth": _out(depth, (H, W), np.float32),
+            "normal": _out(normal, (H, W, 3), np.float32),
+            "mask": _out(mask, (H, W), np.uint8),
+            "face_id": _out(face_id, (H, W), np.int32),
+            "color_f32": _out(color_f32, (H, W, 3), np.float32),
+        }
+        im = capi.Images()
+        for k, v in outs.items():
+            setattr(im, k, None if v is None else v.ctypes.data)
+        rc = self._ctx.render(0, self._camera, im)
+        if rc != capi.OK:
+            LOGE(self._ctx.last_error())
+            return False, {}
+        return True, {k: v for k, v in outs.items() if v is not None}
+
+    def RenderColor(self):
+        return self.Render(color=True)
+
+    def RenderDepth(self):
+        return self.Render(depth=True)
+
+    def RenderNormal(self):
+        return self.Render(normal=True)
+
+    def RenderMask(self):
+        return self.Render(mask=True)
+
+    def RenderFaceId(self):
+        return self.Render(face_id=True)
+
+    def RenderW(self, color=None, depth=True, normal=None, mask=None, face_id=None):
+        """rasterizer.cc:329-344: float depth converted by ConvertTo
+        (image_proc.h:454-...) with scale 1: static_cast<uint16_t>(double)."""
+        if depth is None:
+            LOGE("depth is nullptr")
+            return False, {}
+        ok, out = self.Render(color, True, normal, mask, face_id)
+        if ok:
+            out["depth"] = depth_to_u16(out["depth"])
+        return ok, out
+
+    def RenderDepthW(self):
+        return self.RenderW(depth=True)
+
+
+def depth_to_u16(depth: np.ndarray) -> np.ndarray:
+    """static_cast<uint16_t>(1.0 * double(d)) per pixel: truncation toward
+    zero; values outside [0, 65536) keep the low 16 bits of the saturated
+    int32 conversion."""
+    d = depth.astype(np.float64)
+    i = np.where(np.isnan(d), 0, np.clip(np.trunc(d), -2.0 ** 31, 2.0 ** 31 - 1)).astype(np.int64)
+    return (i & 0xFFFF).astype(np.uint16)
