@@ -1,0 +1,152 @@
+// ref_driver.cc -- TEST INFRASTRUCTURE ONLY.
+//
+// A C entry point around the reference's own ugu::Rasterizer
+// (src/renderer/cpu/rasterizer.cc, compiled unmodified from the reference
+// checkout against the Eigen-compatible shim), used to pin the oracle's
+// restatement and to generate golden fixtures.  It builds a ugu::Mesh and a
+// ugu::PinholeCamera from plain arrays, calls Rasterizer::Render, and copies
+// the images out together with the camera floats Render derived.
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "ugu/renderer/cpu/rasterizer.h"
+
+namespace ugu {
+// The camera classes' vtables name these camera_util functions
+// (src/util/camera_util.cc, not compiled here); the rasterizer never calls
+// them, so they are stubs.
+Eigen::Matrix4f GetProjectionMatrixOpenGlForPinhole(int, int, float, float, float, float,
+                                                   float, float) {
+  return Eigen::Matrix4f::Identity();
+}
+Eigen::Matrix4f GetProjectionMatrixOpenGlForOrtho(float, float, float, float, float, float) {
+  return Eigen::Matrix4f::Identity();
+}
+void UndistortPixelOpencv(float*, float*, float, float, float, float, float, float, float,
+                          float, float, float, float, float) {}
+}  // namespace ugu
+
+extern "C" {
+
+struct ref_mesh {
+  int num_vertices;
+  const float* vertices;
+  int num_faces;
+  const int* vertex_indices;
+  const float* face_normals;  // F*3 or NULL
+  int num_normals;
+  const float* normals;
+  const int* normal_indices;
+  const float* vertex_colors;  // V*3 or NULL
+  int num_uv;
+  const float* uv;
+  const int* uv_indices;
+  const int* material_ids;  // F or NULL
+  int num_materials;
+  const int* tex_wh;            // 2 per material
+  const unsigned char* const* tex;  // per material RGB8
+};
+
+struct ref_option {
+  int diffuse_color, interp, shading_normal, diffuse_shading, backface_culling;
+  float oren_nayar_sigma;
+};
+
+// c2w: 4x4 row-major double.  cam_out: w2c_R[9], w2c_t[3], c2w_R[9] (row-major
+// floats) as Render and the ray table use them.
+int ref_render(const ref_mesh* m, int width, int height, float fx, float fy, float cx,
+               float cy, const double* c2w, const ref_option* o, unsigned char* color,
+               float* depth, float* normal, unsigned char* mask, int* face_id,
+               float* cam_out) {
+  ugu::set_log_level(ugu::LogLevel::kError);
+  auto mesh = std::make_shared<ugu::Mesh>();
+  std::vector<Eigen::Vector3f> v(m->num_vertices);
+  for (int i = 0; i < m->num_vertices; ++i)
+    v[i] = Eigen::Vector3f(m->vertices[3 * i], m->vertices[3 * i + 1], m->vertices[3 * i + 2]);
+  mesh->set_vertices(v);
+  std::vector<Eigen::Vector3i> f(m->num_faces);
+  for (int i = 0; i < m->num_faces; ++i)
+    f[i] = Eigen::Vector3i(m->vertex_indices[3 * i], m->vertex_indices[3 * i + 1],
+                           m->vertex_indices[3 * i + 2]);
+  mesh->set_vertex_indices(f);
+  auto vec3 = [](const float* a, int n) {
+    std::vector<Eigen::Vector3f> r(n);
+    for (int i = 0; i < n; ++i) r[i] = Eigen::Vector3f(a[3 * i], a[3 * i + 1], a[3 * i + 2]);
+    return r;
+  };
+  auto idx3 = [](const int* a, int n) {
+    std::vector<Eigen::Vector3i> r(n);
+    for (int i = 0; i < n; ++i) r[i] = Eigen::Vector3i(a[3 * i], a[3 * i + 1], a[3 * i + 2]);
+    return r;
+  };
+  if (m->face_normals) mesh->set_face_normals(vec3(m->face_normals, m->num_faces));
+  if (m->normals) {
+    mesh->set_normals(vec3(m->normals, m->num_normals));
+    mesh->set_normal_indices(idx3(m->normal_indices, m->num_faces));
+  }
+  if (m->vertex_colors) mesh->set_vertex_colors(vec3(m->vertex_colors, m->num_vertices));
+  if (m->uv) {
+    std::vector<Eigen::Vector2f> uv(m->num_uv);
+    for (int i = 0; i < m->num_uv; ++i) uv[i] = Eigen::Vector2f(m->uv[2 * i], m->uv[2 * i + 1]);
+    mesh->set_uv(uv);
+    mesh->set_uv_indices(idx3(m->uv_indices, m->num_faces));
+  }
+  if (m->material_ids)
+    mesh->set_material_ids(std::vector<int>(m->material_ids, m->material_ids + m->num_faces));
+  std::vector<ugu::ObjMaterial> mats(m->num_materials);
+  for (int i = 0; i < m->num_materials; ++i) {
+    int w = m->tex_wh[2 * i], h = m->tex_wh[2 * i + 1];
+    mats[i].diffuse_tex = ugu::Image3b::zeros(h, w);
+    std::memcpy(mats[i].diffuse_tex.data, m->tex[i], (size_t)w * h * 3);
+  }
+  mesh->set_materials(mats);
+
+  Eigen::Matrix4d M;
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) M(r, c) = c2w[4 * r + c];
+  Eigen::Affine3d pose(M);
+  auto cam = std::make_shared<ugu::PinholeCamera>(width, height, pose, Eigen::Vector2f(cx, cy),
+                                                  Eigen::Vector2f(fx, fy));
+  ugu::RendererCpuOption opt;
+  opt.diffuse_color = static_cast<ugu::DiffuseColor>(o->diffuse_color);
+  opt.interp = static_cast<ugu::ColorInterpolation>(o->interp);
+  opt.shading_normal = static_cast<ugu::ShadingNormal>(o->shading_normal);
+  opt.diffuse_shading = static_cast<ugu::DiffuseShading>(o->diffuse_shading);
+  opt.backface_culling = o->backface_culling != 0;
+  opt.oren_nayar_sigma = o->oren_nayar_sigma;
+
+  ugu::Rasterizer r(opt);
+  r.set_mesh(mesh);
+  if (!r.PrepareMesh()) return 100;
+  r.set_camera(cam);
+  ugu::Image3b c_img;
+  ugu::Image1f d_img;
+  ugu::Image3f n_img;
+  ugu::Image1b m_img;
+  ugu::Image1i f_img;
+  bool ok = r.Render(color ? &c_img : nullptr, depth ? &d_img : nullptr,
+                     normal ? &n_img : nullptr, mask ? &m_img : nullptr,
+                     face_id ? &f_img : nullptr);
+  if (!ok) return 1;
+  const size_t px = (size_t)width * height;
+  if (color) std::memcpy(color, c_img.data, px * 3);
+  if (depth) std::memcpy(depth, d_img.data, px * 4);
+  if (normal) std::memcpy(normal, n_img.data, px * 12);
+  if (mask) std::memcpy(mask, m_img.data, px);
+  if (face_id) std::memcpy(face_id, f_img.data, px * 4);
+  if (cam_out) {
+    Eigen::Matrix3f R = cam->w2c().rotation().cast<float>();
+    Eigen::Vector3f t = cam->w2c().translation().cast<float>();
+    Eigen::Matrix3f C = cam->c2w().matrix().block<3, 3>(0, 0).cast<float>();
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        cam_out[3 * a + b] = R(a, b);
+        cam_out[12 + 3 * a + b] = C(a, b);
+      }
+    for (int a = 0; a < 3; ++a) cam_out[9 + a] = t[a];
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+"""Build and bind oracle/_ref/libugu_ref.so: the reference's own rasterizer
+sources compiled unmodified against the Eigen-compatible shim (TEST
+INFRASTRUCTURE ONLY).  Only possible where the reference checkout exists;
+everything here returns None / skips elsewhere."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("UGU_REFERENCE_DIR", "/root/reference")
+LIB = os.path.join(HERE, "_ref", "libugu_ref.so")
+
+
+def available() -> bool:
+    return os.path.exists(os.path.join(REF, "src", "renderer", "cpu", "rasterizer.cc"))
+
+
+def build_if_available() -> str | None:
+    if not available():
+        return None
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={REF}"],
+                          stdout=subprocess.DEVNULL)
+    return LIB
+
+
+class RefMesh(C.Structure):
+    _fields_ = [("num_vertices", C.c_int), ("vertices", C.c_void_p),
+                ("num_faces", C.c_int), ("vertex_indices", C.c_void_p),
+                ("face_normals", C.c_void_p),
+                ("num_normals", C.c_int), ("normals", C.c_void_p), ("normal_indices", C.c_void_p),
+                ("vertex_colors", C.c_void_p),
+                ("num_uv", C.c_int), ("uv", C.c_void_p), ("uv_indices", C.c_void_p),
+                ("material_ids", C.c_void_p),
+                ("num_materials", C.c_int), ("tex_wh", C.c_void_p), ("tex", C.c_void_p)]
+
+
+class RefOption(C.Structure):
+    _fields_ = [("diffuse_color", C.c_int), ("interp", C.c_int), ("shading_normal", C.c_int),
+                ("diffuse_shading", C.c_int), ("backface_culling", C.c_int),
+                ("oren_nayar_sigma", C.c_float)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            if build_if_available() is None:
+                return None
+        lib = C.CDLL(LIB)
+        lib.ref_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float,
+                                   C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ref_render.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def render(mesh, cam, opt):
+    """Render with the reference's Rasterizer.  Returns (rc, images, camera
+    floats) where the camera floats are the w2c_R / w2c_t / c2w_R the
+    reference derived from cam.c2w."""
+    lib = load()
+    keep = []
+
+    def a(x, dt):
+        if x is None:
+            return None
+        x = np.ascontiguousarray(x, dtype=dt)
+        keep.append(x)
+        return x.ctypes.data
+
+    m = RefMesh()
+    m.num_vertices, m.vertices = mesh.num_vertices, a(mesh.vertices, np.float32)
+    m.num_faces, m.vertex_indices = mesh.num_faces, a(mesh.vertex_indices, np.int32)
+    m.face_normals = a(mesh.face_normals, np.float32)
+    m.num_normals = 0 if mesh.normals is None else len(mesh.normals)
+    m.normals, m.normal_indices = a(mesh.normals, np.float32), a(mesh.normal_indices, np.int32)
+    m.vertex_colors = a(mesh.vertex_colors, np.float32)
+    m.num_uv = 0 if mesh.uv is None else len(mesh.uv)
+    m.uv, m.uv_indices = a(mesh.uv, np.float32), a(mesh.uv_indices, np.int32)
+    m.material_ids = a(mesh.material_ids, np.int32)
+    texs = list(mesh.textures or [])
+    m.num_materials = len(texs)
+    wh = np.array([[t.shape[1], t.shape[0]] for t in texs] or [[0, 0]], np.int32)
+    m.tex_wh = a(wh, np.int32)
+    ptrs = (C.c_void_p * max(1, len(texs)))(*[a(t, np.uint8) for t in texs])
+    keep.append(ptrs)
+    m.tex = C.addressof(ptrs)
+    o = RefOption(int(opt.diffuse_color), int(opt.interp), int(opt.shading_normal),
+                  int(opt.diffuse_shading), 1 if opt.backface_culling else 0,
+                  float(opt.oren_nayar_sigma))
+    H, W = cam.height, cam.width
+    out = {"color": np.zeros((H, W, 3), np.uint8), "depth": np.zeros((H, W), np.float32),
+           "normal": np.zeros((H, W, 3), np.float32), "mask": np.zeros((H, W), np.uint8),
+           "face_id": np.zeros((H, W), np.int32)}
+    c2w = np.ascontiguousarray(cam.c2w if cam.c2w is not None else np.eye(4), np.float64)
+    camf = np.zeros(21, np.float32)
+    rc = lib.ref_render(C.addressof(m), W, H, cam.fx, cam.fy, cam.cx, cam.cy, c2w.ctypes.data,
+                        C.addressof(o), out["color"].ctypes.data, out["depth"].ctypes.data,
+                        out["normal"].ctypes.data, out["mask"].ctypes.data,
+                        out["face_id"].ctypes.data, camf.ctypes.data)
+    return rc, out, {"w2c_R": camf[0:9].reshape(3, 3).copy(), "w2c_t": camf[9:12].copy(),
+                     "c2w_R": camf[12:21].reshape(3, 3).copy()}

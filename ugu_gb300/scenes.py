@@ -308,6 +308,7 @@ class Camera:
     w2c_R: np.ndarray  # 3x3 float32, row-major
     w2c_t: np.ndarray  # 3 float32
     c2w_R: np.ndarray  # 3x3 float32
+    c2w: np.ndarray | None = None  # the 4x4 double pose these came from
 
     @property
     def pixels(self) -> int:
@@ -342,7 +343,10 @@ def _inverse3(m):
     c00 = m[1, 1] * m[2, 2] - m[1, 2] * m[2, 1]
     c10 = m[1, 2] * m[2, 0] - m[1, 0] * m[2, 2]
     c20 = m[1, 0] * m[2, 1] - m[1, 1] * m[2, 0]
-    det = c00 * m[0, 0] + (c10 * m[0, 1] + c20 * m[0, 2])
+    # expansion along column 0, as Eigen's 3x3 inverse computes it
+    d10 = m[2, 1] * m[0, 2] - m[2, 2] * m[0, 1]
+    d20 = m[0, 1] * m[1, 2] - m[0, 2] * m[1, 1]
+    det = c00 * m[0, 0] + (d10 * m[1, 0] + d20 * m[2, 0])
     inv = np.empty((3, 3))
     invdet = 1.0 / det
     inv[0, 0], inv[0, 1], inv[0, 2] = c00 * invdet, (m[0, 2] * m[2, 1] - m[0, 1] * m[2, 2]) * invdet, (m[0, 1] * m[1, 2] - m[0, 2] * m[1, 1]) * invdet
@@ -356,7 +360,7 @@ def _polar_rotation(m):
     by Newton's iteration X <- (X + X^-T) / 2; exact for an orthonormal
     input such as the identity."""
     x = m.copy()
-    for _ in range(8):
+    for _ in range(32):
         nx = 0.5 * (x + _inverse3(x).T)
         if np.array_equal(nx, x):
             break
@@ -376,7 +380,8 @@ def camera_desc(width: int, height: int, fx: float, fy: float, cx: float, cy: fl
     R = np.asarray(c2w, dtype=np.float64)[:3, :3]
     t = np.asarray(c2w, dtype=np.float64)[:3, 3]
     Ri = _inverse3(R)
-    ti = -(Ri @ t)
+    # -(L^-1 t), each row summed a0 + (a1 + a2) like Eigen's matrix product
+    ti = np.array([-(Ri[i, 0] * t[0] + (Ri[i, 1] * t[1] + Ri[i, 2] * t[2])) for i in range(3)])
     if np.array_equal(R, np.eye(3)):
         rot = np.eye(3)
     else:
@@ -385,7 +390,8 @@ def camera_desc(width: int, height: int, fx: float, fy: float, cx: float, cy: fl
                   float(F32(cx)), float(F32(cy)),
                   np.ascontiguousarray(rot.astype(F32)),
                   np.ascontiguousarray(ti.astype(F32)),
-                  np.ascontiguousarray(R.astype(F32)))
+                  np.ascontiguousarray(R.astype(F32)),
+                  np.array(c2w, dtype=np.float64))
 
 
 def ring_cameras(n: int, radius: float, sizes, focal_scale: float = 0.8,
