@@ -139,11 +139,18 @@ enum {
 
 /* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
 typedef struct {
-  int32_t tile_log2;        /* large-face tile edge = 1 << tile_log2 pixels */
-  int32_t small_bbox_max;   /* faces whose bbox has more pixels go to the tile path */
-  int32_t group_pixels;     /* pixels of z-buffer kept live per view group */
-  int32_t raster_ctas_per_sm;
+  int32_t path;             /* UGU_GPU_PATH_TILED (default) or UGU_GPU_PATH_GLOBAL */
+  int32_t tile_log2;        /* screen tile edge = 1 << tile_log2 pixels (4 or 5) */
+  int32_t bin_capacity;     /* tiled: face slots per tile before the overflow list */
+  int32_t small_bbox_max;   /* global: faces with larger bboxes are split by tile */
+  int32_t group_pixels;     /* global: pixels of z-buffer kept live per view group */
+  int32_t ctas_per_sm;      /* persistent-kernel blocks per SM (0 = occupancy limit) */
 } ugu_gpu_tuning;
+
+enum {
+  UGU_GPU_PATH_TILED = 0,  /* bin faces to tiles, rasterise + resolve each tile on chip */
+  UGU_GPU_PATH_GLOBAL = 1  /* global 64-bit z-buffer per view group, then resolve */
+};
 
 typedef struct {
   uint64_t launches;            /* kernels launched by this context so far */

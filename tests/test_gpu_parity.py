@@ -77,21 +77,37 @@ def test_icosphere7_textured_1080p(ctx, oracle_lib):
     compare(ref, got, "icosphere7")
 
 
-@pytest.mark.parametrize("tile_log2,small", [(3, 0), (4, 0), (5, 16), (6, 1 << 20)])
-def test_tuning_does_not_change_results(ctx, oracle_lib, tile_log2, small):
+TUNINGS = [  # (path, tile_log2, bin_capacity, small_bbox_max, group_pixels)
+    (capi.PATH_TILED, 5, 2048, 256, 1 << 22),
+    (capi.PATH_TILED, 4, 512, 256, 1 << 22),
+    (capi.PATH_TILED, 5, 16, 256, 1 << 22),   # most faces go through the overflow list
+    (capi.PATH_TILED, 4, 1, 256, 1 << 22),
+    (capi.PATH_GLOBAL, 3, 2048, 0, 1 << 22),  # every face split into tile items
+    (capi.PATH_GLOBAL, 4, 2048, 0, 1 << 22),
+    (capi.PATH_GLOBAL, 5, 2048, 16, 1 << 22),
+    (capi.PATH_GLOBAL, 6, 2048, 1 << 20, 1 << 22),
+]
+
+
+def with_tuning(ctx, tup):
+    path, tl, cap, small, gp = tup
+    return capi.Tuning(path, tl, cap, small, gp, 0)
+
+
+@pytest.mark.parametrize("tup", TUNINGS, ids=[f"p{t[0]}_t{t[1]}_c{t[2]}_s{t[3]}" for t in TUNINGS])
+def test_tuning_does_not_change_results(ctx, oracle_lib, tup):
     cam = adv.identity_camera(W=200, H=150, f=120.0)
     m = adv.triangle_soup(cam, n_faces=800, seed=9)
-    opt = adv.option(2, 1, 1, 0, False)
-    ref, _ = oracle_render(oracle_lib, m, cam, opt)
     t0 = ctx.tuning()
-    t = capi.Tuning(tile_log2, small, t0.group_pixels, t0.raster_ctas_per_sm)
-    ctx.check(ctx.set_tuning(t))
-    try:
-        rc, got = gpu_render(ctx, m, cam, opt)
-    finally:
-        ctx.check(ctx.set_tuning(t0))
-    assert rc == 0, ctx.last_error()
-    compare(ref, got, f"tile{tile_log2}/small{small}")
+    for opt in (adv.option(2, 1, 1, 0, False), adv.option(1, 1, 0, 1, True)):
+        ref, _ = oracle_render(oracle_lib, m, cam, opt)
+        ctx.check(ctx.set_tuning(with_tuning(ctx, tup)))
+        try:
+            rc, got = gpu_render(ctx, m, cam, opt)
+        finally:
+            ctx.check(ctx.set_tuning(t0))
+        assert rc == 0, ctx.last_error()
+        compare(ref, got, f"tuning {tup}")
 
 
 def _ring(subdiv, n, seed=4):
@@ -101,8 +117,9 @@ def _ring(subdiv, n, seed=4):
     return m, cams
 
 
+@pytest.mark.parametrize("path", [capi.PATH_TILED, capi.PATH_GLOBAL])
 @pytest.mark.parametrize("flags", [0, capi.PER_VIEW])
-def test_batched_views_two_meshes(ctx, oracle_lib, torch_cuda, flags):
+def test_batched_views_two_meshes(ctx, oracle_lib, torch_cuda, flags, path):
     torch = torch_cuda
     m0, cams = _ring(5, 8)
     m1, cam1 = scenes.scene_uv_sphere_vertex_color()
@@ -120,8 +137,8 @@ def test_batched_views_two_meshes(ctx, oracle_lib, torch_cuda, flags):
     slots = [0] * len(cams) + [1]
     meshes = [m0] * len(cams) + [m1]
     t = ctx.tuning()
-    small_groups = capi.Tuning(t.tile_log2, t.small_bbox_max, 100_000, t.raster_ctas_per_sm)
-    ctx.check(ctx.set_tuning(small_groups))  # several view groups
+    # several view groups on the global path; 16x16 tiles on the tiled one
+    ctx.check(ctx.set_tuning(capi.Tuning(path, 4, 1024, 256, 100_000, 0)))
     try:
         tensors, views = device_views(torch, all_cams, slots)
         rc = ctx.render_views(views, capi.DEVICE_POINTERS | flags)

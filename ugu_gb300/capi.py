@@ -71,9 +71,14 @@ class View(C.Structure):
     _fields_ = [("mesh", C.c_int32), ("camera", CameraDesc), ("images", Images)]
 
 
+PATH_TILED = 0
+PATH_GLOBAL = 1
+
+
 class Tuning(C.Structure):
-    _fields_ = [("tile_log2", C.c_int32), ("small_bbox_max", C.c_int32),
-                ("group_pixels", C.c_int32), ("raster_ctas_per_sm", C.c_int32)]
+    _fields_ = [("path", C.c_int32), ("tile_log2", C.c_int32), ("bin_capacity", C.c_int32),
+                ("small_bbox_max", C.c_int32), ("group_pixels", C.c_int32),
+                ("ctas_per_sm", C.c_int32)]
 
 
 class Stats(C.Structure):

@@ -53,12 +53,26 @@ struct Scratch {
   uint8_t* d_out = nullptr;  // device outputs of host-pointer renders
   size_t d_out_cap = 0;
   bool keys_dirty = false;
+  // tiled path
+  int32_t* tile_count = nullptr;
+  size_t tiles_cap = 0;
+  int32_t* bins = nullptr;
+  size_t bins_cap = 0;  // entries
+  int2* overflow = nullptr;
+  size_t overflow_cap = 0;
+  TileCounters* tcounters = nullptr;
+  TileCounters* h_tcounters = nullptr;  // pinned
+  size_t tcounters_cap = 0;
+  bool tiles_dirty = false;
+  size_t list_min = size_t(1) << 22;  // capacity of the item / overflow lists
 };
 
 struct Group {
   int first, count;
   int max_faces;
   int64_t max_pixels;
+  int64_t tiles;    // tiled path: screen tiles of the group's views
+  int64_t batches;  // tiled path: 32-face batches of the group's views
 };
 
 }  // namespace
@@ -129,6 +143,11 @@ void free_scratch(Scratch& s) {
   cudaFree(s.d_views);
   cudaFreeHost(s.h_views);
   cudaFree(s.d_out);
+  cudaFree(s.tile_count);
+  cudaFree(s.bins);
+  cudaFree(s.overflow);
+  cudaFree(s.tcounters);
+  cudaFreeHost(s.h_tcounters);
   s = Scratch();
 }
 
@@ -231,23 +250,35 @@ size_t host_bytes_of_view(const ugu_gpu_images& im, int64_t px) {
   return b;
 }
 
+int64_t tiles_of(const ugu_gpu_camera& c, int tlog) {
+  const int64_t T = int64_t(1) << tlog;
+  return ((c.width + T - 1) / T) * ((c.height + T - 1) / T);
+}
+
+// Views split into launch groups: per view (the baseline), by z-buffer
+// pixels (global path) or all together (tiled path).
 std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views,
-                               bool per_view, int64_t group_pixels) {
+                               bool per_view) {
+  const ugu_gpu_tuning& t = ctx->tuning;
+  const int64_t limit = t.path == UGU_GPU_PATH_GLOBAL ? (int64_t)t.group_pixels : INT64_MAX;
   std::vector<Group> g;
-  Group cur{0, 0, 0, 0};
+  Group cur{0, 0, 0, 0, 0, 0};
   int64_t acc = 0;
   for (int i = 0; i < n; ++i) {
     int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
-    bool full = cur.count > 0 && (per_view || acc + px > group_pixels);
+    bool full = cur.count > 0 && (per_view || acc + px > limit);
     if (full) {
       g.push_back(cur);
-      cur = Group{i, 0, 0, 0};
+      cur = Group{i, 0, 0, 0, 0, 0};
       acc = 0;
     }
+    const int F = ctx->meshes[views[i].mesh].dev.num_faces;
     cur.count++;
     acc += px;
-    cur.max_faces = std::max(cur.max_faces, ctx->meshes[views[i].mesh].dev.num_faces);
+    cur.max_faces = std::max(cur.max_faces, F);
     cur.max_pixels = std::max(cur.max_pixels, px);
+    cur.tiles += tiles_of(views[i].camera, t.tile_log2);
+    cur.batches += (F + 31) / 32;
   }
   if (cur.count) g.push_back(cur);
   return g;
@@ -264,8 +295,56 @@ int64_t group_key_count(const std::vector<Group>& groups, const ugu_gpu_view* vi
   return mx;
 }
 
+int ensure_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups) {
+  size_t tiles = 0;
+  for (const Group& g : groups) tiles = std::max(tiles, (size_t)g.tiles);
+  const size_t cap = (size_t)ctx->tuning.bin_capacity;
+  if (tiles > s.tiles_cap) {
+    cudaFree(s.tile_count);
+    s.tile_count = nullptr;
+    s.tiles_cap = 0;
+    CK(ctx, cudaMalloc(&s.tile_count, tiles * sizeof(int32_t)), "cudaMalloc(tile counts)");
+    s.tiles_cap = tiles;
+    s.tiles_dirty = true;
+  }
+  if (tiles * cap > s.bins_cap) {
+    cudaFree(s.bins);
+    s.bins = nullptr;
+    s.bins_cap = 0;
+    CK(ctx, cudaMalloc(&s.bins, tiles * cap * sizeof(int32_t)), "cudaMalloc(tile bins)");
+    s.bins_cap = tiles * cap;
+  }
+  if (s.overflow_cap < s.list_min) {
+    cudaFree(s.overflow);
+    s.overflow = nullptr;
+    s.overflow_cap = 0;
+    const size_t oc = s.list_min;
+    CK(ctx, cudaMalloc(&s.overflow, oc * sizeof(int2)), "cudaMalloc(bin overflow)");
+    s.overflow_cap = oc;
+  }
+  if (groups.size() > s.tcounters_cap) {
+    cudaFree(s.tcounters);
+    cudaFreeHost(s.h_tcounters);
+    s.tcounters = nullptr;
+    s.h_tcounters = nullptr;
+    s.tcounters_cap = 0;
+    CK(ctx, cudaMalloc(&s.tcounters, groups.size() * sizeof(TileCounters)),
+       "cudaMalloc(tile counters)");
+    CK(ctx, cudaMallocHost(&s.h_tcounters, groups.size() * sizeof(TileCounters)),
+       "cudaMallocHost(tile counters)");
+    s.tcounters_cap = groups.size();
+  }
+  if (s.tiles_dirty) {
+    CK(ctx, cudaMemsetAsync(s.tile_count, 0, s.tiles_cap * sizeof(int32_t), ctx->stream),
+       "cudaMemsetAsync(tile counts)");
+    s.tiles_dirty = false;
+  }
+  return UGU_GPU_OK;
+}
+
 int ensure_scratch(ugu_gpu_context* ctx, Scratch& s, size_t nkeys, size_t nviews,
                    size_t ngroups, size_t out_bytes) {
+  if (ctx->tuning.path != UGU_GPU_PATH_GLOBAL) nkeys = 0;
   if (nkeys > s.keys_cap) {
     cudaFree(s.keys);
     s.keys = nullptr;
@@ -279,8 +358,11 @@ int ensure_scratch(ugu_gpu_context* ctx, Scratch& s, size_t nkeys, size_t nviews
        "cudaMemsetAsync(z-buffer)");
     s.keys_dirty = false;
   }
-  if (s.items_cap == 0) {
-    size_t cap = size_t(1) << 22;
+  if (s.items_cap < s.list_min && ctx->tuning.path == UGU_GPU_PATH_GLOBAL) {
+    cudaFree(s.items);
+    s.items = nullptr;
+    s.items_cap = 0;
+    size_t cap = s.list_min;
     CK(ctx, cudaMalloc(&s.items, cap * sizeof(TileItem)), "cudaMalloc(tile items)");
     s.items_cap = cap;
   }
@@ -315,19 +397,25 @@ int ensure_scratch(ugu_gpu_context* ctx, Scratch& s, size_t nkeys, size_t nviews
   return UGU_GPU_OK;
 }
 
-RenderParams base_params(ugu_gpu_context* ctx, const Scratch& s) {
-  RenderParams p{};
-  const ugu_gpu_option& o = ctx->opt;
-  p.meshes = ctx->d_meshes;
+ShadeOpts shade_opts(const ugu_gpu_option& o) {
+  ShadeOpts p;
   p.diffuse_color = o.diffuse_color;
   p.interp = o.interp;
   p.shading_normal = o.shading_normal;
   p.diffuse_shading = o.diffuse_shading;
-  p.backface_culling = o.backface_culling ? 1 : 0;
-  // OrenNayarParam (pixel_shader.h:143-148)
+  // OrenNayarParam (pixel_shader.h:143-148), in float like the reference
   float sigma_2 = o.oren_nayar_sigma * o.oren_nayar_sigma;
   p.on_A = 1.0f - (0.5f * sigma_2 / (sigma_2 + 0.33f));
   p.on_B = 0.45f * sigma_2 / (sigma_2 + 0.09f);
+  return p;
+}
+
+RenderParams base_params(ugu_gpu_context* ctx, const Scratch& s) {
+  RenderParams p{};
+  const ugu_gpu_option& o = ctx->opt;
+  p.meshes = ctx->d_meshes;
+  p.shade = shade_opts(o);
+  p.backface_culling = o.backface_culling ? 1 : 0;
   p.keys = s.keys;
   p.items = s.items;
   p.item_capacity = (int64_t)s.items_cap;
@@ -336,9 +424,48 @@ RenderParams base_params(ugu_gpu_context* ctx, const Scratch& s) {
   return p;
 }
 
+int persistent_grid(ugu_gpu_context* ctx, int blocks_per_sm) {
+  const int per_sm = ctx->tuning.ctas_per_sm > 0 ? std::min(ctx->tuning.ctas_per_sm, blocks_per_sm)
+                                                 : blocks_per_sm;
+  return ctx->num_sms * std::max(per_sm, 1);
+}
+
+int enqueue_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
+                  int* kernels) {
+  const ugu_gpu_option& o = ctx->opt;
+  int nk = 0;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const Group& gr = groups[gi];
+    TileParams p{};
+    p.meshes = ctx->d_meshes;
+    p.views = s.d_views + gr.first;
+    p.num_views = gr.count;
+    p.shade = shade_opts(o);
+    p.backface_culling = o.backface_culling ? 1 : 0;
+    p.tile_log2 = ctx->tuning.tile_log2;
+    p.total_tiles = (int32_t)gr.tiles;
+    p.bin_cap = ctx->tuning.bin_capacity;
+    p.total_batches = gr.batches;
+    p.tile_count = s.tile_count;
+    p.bins = s.bins;
+    p.overflow = s.overflow;
+    p.overflow_cap = (int32_t)s.overflow_cap;
+    p.counters = s.tcounters + gi;
+    CK(ctx, cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream),
+       "cudaMemsetAsync(tile counters)");
+    launch_bin(p, persistent_grid(ctx, bin_kernel_blocks_per_sm()), ctx->stream);
+    launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
+    nk += 2;
+  }
+  CK(ctx, cudaGetLastError(), "kernel launch");
+  *kernels = nk;
+  return UGU_GPU_OK;
+}
+
 // Enqueue the kernels of every group (no synchronisation).
 int enqueue_groups(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
                    const ugu_gpu_view* views, int* kernels) {
+  if (ctx->tuning.path != UGU_GPU_PATH_GLOBAL) return enqueue_tiled(ctx, s, groups, kernels);
   RenderParams base = base_params(ctx, s);
   int nk = 0;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
@@ -361,10 +488,10 @@ int enqueue_groups(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& g
 // Fill s.h_views for the views; host-pointer outputs get device staging.
 void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
                 const ugu_gpu_view* views, bool device_ptrs) {
-  (void)ctx;
   size_t off = 0;
+  const int tlog = ctx->tuning.tile_log2;
   for (const Group& gr : groups) {
-    int64_t key_off = 0;
+    int64_t key_off = 0, tile_base = 0, batch_begin = 0;
     for (int i = gr.first; i < gr.first + gr.count; ++i) {
       const ugu_gpu_view& v = views[i];
       DevView& d = s.h_views[i];
@@ -374,6 +501,12 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
       d.key_offset = key_off;
       int64_t px = (int64_t)v.camera.width * v.camera.height;
       key_off += px;
+      const int T = 1 << tlog;
+      d.tiles_x = (v.camera.width + T - 1) / T;
+      d.tile_base = (int32_t)tile_base;
+      tile_base += tiles_of(v.camera, tlog);
+      d.batch_begin = batch_begin;
+      batch_begin += (ctx->meshes[v.mesh].dev.num_faces + 31) / 32;
       if (device_ptrs) {
         d.color = v.images.color;
         d.depth = v.images.depth;
@@ -423,9 +556,15 @@ int copy_back(ugu_gpu_context* ctx, const Scratch& s, int n, const ugu_gpu_view*
 int check_counters(ugu_gpu_context* ctx, const Scratch& s, size_t ngroups) {
   uint64_t special = 0, overflow = 0, items = 0;
   for (size_t g = 0; g < ngroups; ++g) {
-    special += s.h_counters[g].special;
-    overflow += s.h_counters[g].overflow;
-    items += s.h_counters[g].tile_items;
+    if (ctx->tuning.path == UGU_GPU_PATH_GLOBAL) {
+      special += s.h_counters[g].special;
+      overflow += s.h_counters[g].overflow;
+      items += s.h_counters[g].tile_items;
+    } else {
+      special += s.h_tcounters[g].special;
+      overflow += s.h_tcounters[g].dropped;
+      items += s.h_tcounters[g].overflow_count;
+    }
   }
   ctx->special += special;
   ctx->large_items = items;
@@ -449,6 +588,35 @@ int validate_views(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views) {
   return UGU_GPU_OK;
 }
 
+int prepare_scratch(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
+                    const ugu_gpu_view* views, int n, size_t out_bytes) {
+  int rc = ensure_scratch(ctx, s, (size_t)group_key_count(groups, views), (size_t)n,
+                          groups.size(), out_bytes);
+  if (rc || ctx->tuning.path == UGU_GPU_PATH_GLOBAL) return rc;
+  return ensure_tiled(ctx, s, groups);
+}
+
+// Everything one render enqueues once its view table is on the device.
+int enqueue_render(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
+                   const ugu_gpu_view* views, int n, bool dev, int* kernels) {
+  const bool global = ctx->tuning.path == UGU_GPU_PATH_GLOBAL;
+  if (global)
+    CK(ctx, cudaMemsetAsync(s.counters, 0, groups.size() * sizeof(DevCounters), ctx->stream),
+       "cudaMemsetAsync(counters)");
+  int rc = enqueue_groups(ctx, s, groups, views, kernels);
+  if (rc) return rc;
+  if (!dev && (rc = copy_back(ctx, s, n, views))) return rc;
+  if (global)
+    CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, groups.size() * sizeof(DevCounters),
+                            cudaMemcpyDeviceToHost, ctx->stream),
+       "cudaMemcpyAsync(counters)");
+  else
+    CK(ctx, cudaMemcpyAsync(s.h_tcounters, s.tcounters, groups.size() * sizeof(TileCounters),
+                            cudaMemcpyDeviceToHost, ctx->stream),
+       "cudaMemcpyAsync(tile counters)");
+  return UGU_GPU_OK;
+}
+
 int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t flags) {
   if (n < 0 || (n > 0 && !views))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view list");
@@ -458,44 +626,39 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
   const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
   if ((flags & UGU_GPU_ASYNC) && !dev)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "UGU_GPU_ASYNC needs device pointers");
-  std::vector<Group> groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0,
-                                          ctx->tuning.group_pixels);
+  std::vector<Group> groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0);
   size_t out_bytes = 0;
   if (!dev)
     for (int i = 0; i < n; ++i)
       out_bytes += host_bytes_of_view(views[i].images,
                                       (int64_t)views[i].camera.width * views[i].camera.height);
   Scratch& s = ctx->scratch;
-  rc = ensure_scratch(ctx, s, (size_t)group_key_count(groups, views), (size_t)n, groups.size(),
-                      out_bytes);
-  if (rc) return rc;
-  // The pinned view table may still be read by a previous asynchronous copy.
-  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-  fill_views(ctx, s, groups, views, dev);
-  CK(ctx, cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView), cudaMemcpyHostToDevice,
-                          ctx->stream),
-     "cudaMemcpyAsync(views)");
-  CK(ctx, cudaMemsetAsync(s.counters, 0, groups.size() * sizeof(DevCounters), ctx->stream),
-     "cudaMemsetAsync(counters)");
-  int kernels = 0;
-  rc = enqueue_groups(ctx, s, groups, views, &kernels);
-  if (rc) {
-    s.keys_dirty = true;
+  for (int attempt = 0;; ++attempt) {
+    rc = prepare_scratch(ctx, s, groups, views, n, out_bytes);
+    if (rc) return rc;
+    // The pinned view table may still be read by a previous asynchronous copy.
+    CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    fill_views(ctx, s, groups, views, dev);
+    CK(ctx, cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView), cudaMemcpyHostToDevice,
+                            ctx->stream),
+       "cudaMemcpyAsync(views)");
+    int kernels = 0;
+    rc = enqueue_render(ctx, s, groups, views, n, dev, &kernels);
+    if (rc) {
+      s.keys_dirty = s.tiles_dirty = true;
+      return rc;
+    }
+    ctx->launches += kernels;
+    if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
+    CK(ctx, cudaStreamSynchronize(ctx->stream), "render");
+    rc = check_counters(ctx, s, groups.size());
+    if (rc == UGU_GPU_ERR_CAPACITY && attempt == 0) {
+      s.list_min *= 8;  // a list overflowed: grow it and render again
+      s.keys_dirty = s.tiles_dirty = true;
+      continue;
+    }
     return rc;
   }
-  ctx->launches += kernels;
-  if (!dev) {
-    rc = copy_back(ctx, s, n, views);
-    if (rc) return rc;
-  }
-  CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, groups.size() * sizeof(DevCounters),
-                          cudaMemcpyDeviceToHost, ctx->stream),
-     "cudaMemcpyAsync(counters)");
-  if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
-  CK(ctx, cudaStreamSynchronize(ctx->stream), "render");
-  rc = check_counters(ctx, s, groups.size());
-  if (rc == UGU_GPU_ERR_CAPACITY) s.keys_dirty = true;
-  return rc;
 }
 
 }  // namespace
@@ -535,6 +698,9 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
     return UGU_GPU_ERR_CUDA;
   }
   ctx->stream = ctx->own_stream;
+  // occupancy queries happen here, never inside a stream capture
+  tile_kernel_blocks_per_sm();
+  bin_kernel_blocks_per_sm();
   ctx->opt.diffuse_color = 0;
   ctx->opt.interp = 1;
   ctx->opt.shading_normal = 1;
@@ -542,10 +708,12 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->opt.depth_scale = 1.0f;
   ctx->opt.backface_culling = 1;
   ctx->opt.oren_nayar_sigma = 0.3f;
-  ctx->tuning.tile_log2 = 4;
+  ctx->tuning.path = UGU_GPU_PATH_TILED;
+  ctx->tuning.tile_log2 = 5;
+  ctx->tuning.bin_capacity = 2048;
   ctx->tuning.small_bbox_max = 256;
   ctx->tuning.group_pixels = 4 << 20;
-  ctx->tuning.raster_ctas_per_sm = 8;
+  ctx->tuning.ctas_per_sm = 0;
   *out = ctx;
   return UGU_GPU_OK;
 }
@@ -724,11 +892,9 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
   if (rc) return rc;
   ugu_gpu_plan* plan = new ugu_gpu_plan();
   plan->ctx = ctx;
-  plan->groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0,
-                             ctx->tuning.group_pixels);
+  plan->groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0);
   Scratch& s = plan->scratch;
-  rc = ensure_scratch(ctx, s, (size_t)group_key_count(plan->groups, views), (size_t)n,
-                      plan->groups.size(), 0);
+  rc = prepare_scratch(ctx, s, plan->groups, views, n, 0);
   if (!rc) {
     fill_views(ctx, s, plan->groups, views, true);
     cudaError_t e = cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView),
@@ -741,12 +907,9 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaStreamBeginCapture");
   }
   if (!rc) {
-    cudaMemsetAsync(s.counters, 0, plan->groups.size() * sizeof(DevCounters), ctx->stream);
     int k = 0;
-    rc = enqueue_groups(ctx, s, plan->groups, views, &k);
+    rc = enqueue_render(ctx, s, plan->groups, views, n, true, &k);
     plan->kernels = k;
-    cudaMemcpyAsync(s.h_counters, s.counters, plan->groups.size() * sizeof(DevCounters),
-                    cudaMemcpyDeviceToHost, ctx->stream);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &plan->graph);
     if (!rc && e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaStreamEndCapture");
   }
@@ -807,9 +970,21 @@ int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream) {
 
 int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
   if (!ctx || !t) return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL argument");
-  if (t->tile_log2 < 3 || t->tile_log2 > 6 || t->small_bbox_max < 0 || t->group_pixels < 1 ||
-      t->raster_ctas_per_sm < 1)
+  const bool tiled = t->path == UGU_GPU_PATH_TILED;
+  if ((t->path != UGU_GPU_PATH_TILED && t->path != UGU_GPU_PATH_GLOBAL) ||
+      (tiled && (t->tile_log2 < 4 || t->tile_log2 > 5)) ||
+      (!tiled && (t->tile_log2 < 3 || t->tile_log2 > 6)) || t->bin_capacity < 1 ||
+      t->small_bbox_max < 0 || t->group_pixels < 1 || t->ctas_per_sm < 0)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "tuning out of range");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (t->tile_log2 != ctx->tuning.tile_log2 || t->bin_capacity != ctx->tuning.bin_capacity) {
+    // bins are laid out per tile size and capacity: start them afresh
+    cudaFree(ctx->scratch.tile_count);
+    cudaFree(ctx->scratch.bins);
+    ctx->scratch.tile_count = nullptr;
+    ctx->scratch.bins = nullptr;
+    ctx->scratch.tiles_cap = ctx->scratch.bins_cap = 0;
+  }
   ctx->tuning = *t;
   return UGU_GPU_OK;
 }

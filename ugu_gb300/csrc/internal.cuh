@@ -42,8 +42,11 @@ struct DevMesh {
 struct DevView {
   Cam cam;
   int32_t mesh;
+  int32_t tiles_x;     // tiled path: tiles per row
+  int64_t key_offset;  // global path: first z-buffer key of this view within its group
+  int64_t batch_begin; // tiled path: first 32-face batch of this view
+  int32_t tile_base;   // tiled path: first global tile of this view
   int32_t pad_;
-  int64_t key_offset;  // first z-buffer key of this view within its group
   uint8_t* color;
   float* depth;
   float* normal;
@@ -60,6 +63,19 @@ struct DevCounters {
   unsigned long long pad;
 };
 
+// The option fields the pixel shaders read (RendererCpuOption,
+// renderer.h:17-38) and the Oren-Nayar constants (pixel_shader.h:143-148).
+struct ShadeOpts {
+  int32_t diffuse_color, interp, shading_normal, diffuse_shading;
+  float on_A, on_B;
+};
+
+struct Shaded {
+  uint8_t c[3];
+  float cf[3];
+  float n[3];
+};
+
 struct TileItem {
   int32_t view;  // view index within the group
   int32_t face;
@@ -70,8 +86,8 @@ struct RenderParams {
   const DevMesh* meshes;
   const DevView* views;  // views of this group
   int32_t num_views;
-  int32_t diffuse_color, interp, shading_normal, diffuse_shading, backface_culling;
-  float on_A, on_B;
+  ShadeOpts shade;
+  int32_t backface_culling;
   unsigned long long* keys;
   DevCounters* counters;
   TileItem* items;
@@ -79,6 +95,38 @@ struct RenderParams {
   int32_t tile_log2;
   int32_t small_bbox_max;
 };
+
+// Counters of one tiled render (memset before every launch).
+struct TileCounters {
+  unsigned int next_tile;       // work-queue head of k_tile
+  unsigned int overflow_count;  // entries appended to the overflow list
+  unsigned long long special;   // covered samples with unorderable depth
+  unsigned long long dropped;   // overflow entries beyond the list's capacity
+  unsigned long long pad;
+};
+
+struct TileParams {
+  const DevMesh* meshes;
+  const DevView* views;
+  int32_t num_views;
+  ShadeOpts shade;
+  int32_t backface_culling;
+  int32_t tile_log2;
+  int32_t total_tiles;
+  int32_t bin_cap;
+  int64_t total_batches;
+  int32_t* tile_count;  // faces binned per global tile (k_tile resets it to 0)
+  int32_t* bins;        // total_tiles x bin_cap face ids
+  int2* overflow;       // (global tile, face) beyond bin_cap
+  int32_t overflow_cap;
+  TileCounters* counters;
+};
+
+// Host-side launchers (tile.cu).
+void launch_bin(const TileParams& p, int grid, cudaStream_t s);
+void launch_tile(const TileParams& p, int grid, cudaStream_t s);
+int tile_kernel_blocks_per_sm();
+int bin_kernel_blocks_per_sm();
 
 // Host-side launchers (raster.cu).
 void launch_raster(const RenderParams& p, int max_faces, int num_sms, cudaStream_t s);

@@ -1,0 +1,437 @@
+// tile.cu -- the tiled forward path: bin faces to (view, tile) lists, then one
+// persistent kernel that rasterises and resolves each tile in shared memory.
+//
+//   k_bin   one pass over every (view, face): Loop A + the per-face culls of
+//           Loop B (rasterizer.cc:131-193) and, for each surviving face, an
+//           append of its id to the list of every screen tile its bbox
+//           touches (atomic slot per tile; past bin_cap to an overflow list).
+//   k_tile  persistent blocks pull (view, tile) items from a work queue.
+//           For one tile: set the listed faces up in shared memory, split
+//           each warp's 32 faces into (face, pixel) pairs with a warp prefix
+//           scan of their bbox-in-tile pixel counts, run Loop B's pixel test
+//           on every pair into a shared-memory z-buffer of 64-bit
+//           (depth bits << 32 | face id << 1 | back-face bit) keys with
+//           atomicMin, then run Loop C (rasterizer.cc:244-301) for the
+//           tile's pixels and write the outputs.
+//
+// Faces whose normal points away from the tile's centre ray are drawn after
+// the others and skipped when a proven lower bound of their depth lies
+// behind the deepest key of a fully covered tile: such a face can never win
+// the z-test there, so the result is unchanged.
+#include <cuda_runtime.h>
+
+#include "internal.cuh"
+#include "shade.cuh"
+
+namespace ugu_gpu {
+
+namespace {
+
+constexpr int kBinThreads = 256;
+constexpr int kTileThreads = 256;
+constexpr int kWarps = kTileThreads / 32;
+constexpr int kChunk = 256;      // faces set up in shared memory at a time
+constexpr int kHash = 512;       // fid -> chunk slot table (power of two)
+constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
+constexpr float kU64 = 3.814697265625e-06f;  // 2^-18 = 64 ulp(1)
+
+__device__ __forceinline__ int find_view_by_batch(const TileParams& p, int64_t b) {
+  int lo = 0, hi = p.num_views - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (p.views[mid].batch_begin <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int find_view_by_tile(const TileParams& p, int t) {
+  int lo = 0, hi = p.num_views - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (p.views[mid].tile_base <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ bool setup_face_g(const DevMesh& m, const Cam& c, int f,
+                                             FaceSetup& s) {
+  int4 vi = __ldg(&m.vidx[f]);
+  float4 a = __ldg(&m.vertices[vi.x]);
+  float4 b = __ldg(&m.vertices[vi.y]);
+  float4 d = __ldg(&m.vertices[vi.z]);
+  return face_setup(c, project(c, a.x, a.y, a.z), project(c, b.x, b.y, b.z),
+                    project(c, d.x, d.y, d.z), s);
+}
+
+__global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < p.total_batches;
+       b += nwarps) {
+    const int v = find_view_by_batch(p, b);
+    const DevView* V = &p.views[v];
+    const DevMesh* M = &p.meshes[V->mesh];
+    const int f = (int)((b - V->batch_begin) * 32) + lane;
+    if (f >= M->num_faces) continue;
+    const Cam c = V->cam;
+    FaceSetup s;
+    if (!setup_face_g(*M, c, f, s)) continue;
+    if (s.x1 < s.x0 || s.y1 < s.y0) continue;
+    const int ts = p.tile_log2;
+    const int tx0 = s.x0 >> ts, tx1 = s.x1 >> ts, ty0 = s.y0 >> ts, ty1 = s.y1 >> ts;
+    for (int ty = ty0; ty <= ty1; ++ty)
+      for (int tx = tx0; tx <= tx1; ++tx) {
+        const int t = V->tile_base + ty * V->tiles_x + tx;
+        const int slot = atomicAdd(&p.tile_count[t], 1);
+        if (slot < p.bin_cap) {
+          p.bins[(int64_t)t * p.bin_cap + slot] = f;
+        } else {
+          const unsigned o = atomicAdd(&p.counters->overflow_count, 1u);
+          if (o < (unsigned)p.overflow_cap)
+            p.overflow[o] = make_int2(t, f);
+          else
+            atomicAdd(&p.counters->dropped, 1ull);
+        }
+      }
+  }
+}
+
+struct TileSmem {
+  unsigned long long keys[kMaxTile * kMaxTile];
+  float4 r0[kChunk];  // v0.x v0.y v1.x v1.y
+  float4 r1[kChunk];  // v2.x v2.y area fid-bits
+  float4 r2[kChunk];  // v0.z v1.z v2.z depth lower bound
+  float4 r3[kChunk];  // back-face sign: sa sb sc tolerance
+  int4 r4[kChunk];    // bbox-in-tile x0 y0 width magic
+  int cnt[kChunk];    // pixels of bbox-in-tile, 0 when culled
+  unsigned char back[kChunk];
+  int hkey[kHash];
+  short hval[kHash];
+  int pre[kWarps][33];
+  DevView view;
+  DevMesh mesh;
+  int item;
+  int any_back;
+  float zmax_bits;
+};
+
+__device__ __forceinline__ unsigned hash_fid(int f) { return ((unsigned)f * 2654435761u) >> 23; }
+
+// Loop B's per-pixel body (rasterizer.cc:196-237) for chunk face j at (x, y),
+// into the tile's shared z-buffer.
+__device__ __forceinline__ void test_pair(TileSmem& sm, const TileParams& p, const Cam& c, int j,
+                                          int x, int y, int tx0, int ty0, int tlog) {
+  const float4 r0 = sm.r0[j];
+  const float4 r1 = sm.r1[j];
+  const float4 r3 = sm.r3[j];
+  const int fid = __float_as_int(r1.w);
+  // sign of face_normal . ray_w: the affine surrogate decides unless it is
+  // within its error bound of zero; then the reference's ray is computed.
+  const float sv = fmaf(r3.x, (float)x, fmaf(r3.y, (float)y, r3.z));
+  bool bf;
+  if (sv > r3.w) {
+    bf = true;
+  } else if (sv < -r3.w) {
+    bf = false;
+  } else {
+    const float4 fn = __ldg(&sm.mesh.fnormals[fid]);
+    const float3 r = ray_w(c, x, y);
+    bf = dot3(fn.x, fn.y, fn.z, r.x, r.y, r.z) > 0.0f;
+  }
+  FaceSetup s;
+  s.v0 = make_float3(r0.x, r0.y, 0.0f);
+  s.v1 = make_float3(r0.z, r0.w, 0.0f);
+  s.v2 = make_float3(r1.x, r1.y, 0.0f);
+  Bary b = edges_at(s, x, y);
+  if (!covered(b, bf)) return;
+  const float4 r2 = sm.r2[j];
+  s.v0.z = r2.x;
+  s.v1.z = r2.y;
+  s.v2.z = r2.z;
+  s.area = r1.z;
+  const float z = perspective(s, b);
+  if (!orderable_depth(z)) {
+    atomicAdd(&p.counters->special, 1ull);
+    return;
+  }
+  const unsigned long long key = make_key(z, fid, bf);
+  unsigned long long* kp = &sm.keys[((y - ty0) << tlog) + (x - tx0)];
+  if (key < *(volatile unsigned long long*)kp) atomicMin(kp, key);
+}
+
+// Warp-cooperative pass over the chunk's faces with back == want_back.
+__device__ __forceinline__ void raster_pass(TileSmem& sm, const TileParams& p, const Cam& c,
+                                            int m, unsigned char want_back, int tx0, int ty0,
+                                            int tlog) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int base = warp * 32; base < m; base += kTileThreads) {
+    const int j = base + lane;
+    const int cnt = (j < m && sm.back[j] == want_back) ? sm.cnt[j] : 0;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int* pre = sm.pre[warp];
+    pre[lane] = incl - cnt;
+    __syncwarp();
+    for (int k = lane; k < total; k += 32) {
+      int q = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (pre[q + step] <= k) q += step;
+      const int jj = base + q;
+      const int local = k - pre[q];
+      const int4 r4 = sm.r4[jj];
+      const int yy = (local * r4.w) >> 20;
+      const int xx = local - yy * r4.z;
+      test_pair(sm, p, c, jj, r4.x + xx, r4.y + yy, tx0, ty0, tlog);
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int tlog = p.tile_log2;
+  const int T = 1 << tlog;
+  int cur_view = -1;
+  for (;;) {
+    if (tid == 0) sm.item = (int)atomicAdd(&p.counters->next_tile, 1u);
+    __syncthreads();
+    const int item = sm.item;
+    if (item >= p.total_tiles) break;
+    const int v = find_view_by_tile(p, item);
+    if (v != cur_view) {
+      const int* src = reinterpret_cast<const int*>(&p.views[v]);
+      int* dst = reinterpret_cast<int*>(&sm.view);
+      for (int i = tid; i < (int)(sizeof(DevView) / 4); i += kTileThreads) dst[i] = src[i];
+      __syncthreads();
+      const int* msrc = reinterpret_cast<const int*>(&p.meshes[sm.view.mesh]);
+      int* mdst = reinterpret_cast<int*>(&sm.mesh);
+      for (int i = tid; i < (int)(sizeof(DevMesh) / 4); i += kTileThreads) mdst[i] = msrc[i];
+      cur_view = v;
+    }
+    const Cam& c = sm.view.cam;
+    const int local = item - sm.view.tile_base;
+    const int tyi = local / sm.view.tiles_x;
+    const int txi = local - tyi * sm.view.tiles_x;
+    const int tx0 = txi << tlog, ty0 = tyi << tlog;
+    const int tw = min(T, c.width - tx0), th = min(T, c.height - ty0);
+    for (int i = tid; i < T * T; i += kTileThreads) sm.keys[i] = kEmptyKey;
+    const int n_total = p.tile_count[item];
+    const int n_bin = min(n_total, p.bin_cap);
+    __syncthreads();
+
+    // Per-view constants of the back-face surrogate's error bound.
+    const float Dx = (c.width + fabsf(c.cx)) / c.fx;
+    const float Dy = (c.height + fabsf(c.cy)) / c.fy;
+    const float Dmax = 1.0f + fmaxf(fabsf(c.cx), fabsf(c.width - 1 - c.cx)) / c.fx +
+                       fmaxf(fabsf(c.cy), fabsf(c.height - 1 - c.cy)) / c.fy;
+    const float xc = tx0 + 0.5f * (tw - 1), yc = ty0 + 0.5f * (th - 1);
+
+    for (int cs = 0; cs < n_bin; cs += kChunk) {
+      const int m = min(kChunk, n_bin - cs);
+      for (int i = tid; i < kHash; i += kTileThreads) sm.hkey[i] = -1;
+      if (tid == 0) sm.any_back = 0;
+      __syncthreads();
+      for (int j = tid; j < m; j += kTileThreads) {
+        const int f = p.bins[(int64_t)item * p.bin_cap + cs + j];
+        FaceSetup s;
+        setup_face_g(sm.mesh, c, f, s);  // succeeded in k_bin: same arithmetic
+        const int bx0 = max(s.x0, tx0), bx1 = min(s.x1, tx0 + tw - 1);
+        const int by0 = max(s.y0, ty0), by1 = min(s.y1, ty0 + th - 1);
+        const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;
+        const int n = (bw > 0 && bh > 0) ? bw * bh : 0;
+        // back-face surrogate: s(x, y) = (C^T n) . ((x-cx)/fx, (y-cy)/fy, 1)
+        const float4 fn = __ldg(&sm.mesh.fnormals[f]);
+        const float* C = c.C;
+        const float g0 = C[0] * fn.x + C[3] * fn.y + C[6] * fn.z;
+        const float g1 = C[1] * fn.x + C[4] * fn.y + C[7] * fn.z;
+        const float g2 = C[2] * fn.x + C[5] * fn.y + C[8] * fn.z;
+        const float G = (fabsf(C[0]) + fabsf(C[1]) + fabsf(C[2])) * fabsf(fn.x) +
+                        (fabsf(C[3]) + fabsf(C[4]) + fabsf(C[5])) * fabsf(fn.y) +
+                        (fabsf(C[6]) + fabsf(C[7]) + fabsf(C[8])) * fabsf(fn.z);
+        const float sa = g0 / c.fx, sb = g1 / c.fy;
+        const float sc = g2 - sa * c.cx - sb * c.cy;
+        const float tol = kU64 * (G * (1.0f + Dx + Dy) + fabsf(sa) * (c.width + fabsf(c.cx)) +
+                                  fabsf(sb) * (c.height + fabsf(c.cy)) + fabsf(g2)) +
+                          2.0f * kU64 * G * Dmax;
+        // lower bound of any depth the face can produce (see file comment)
+        const float zmin = fminf(fminf(s.v0.z, s.v1.z), s.v2.z);
+        const float BW = fmaxf(fmaxf(s.v0.x, s.v1.x), s.v2.x) - fminf(fminf(s.v0.x, s.v1.x), s.v2.x) + 1.0f;
+        const float BH = fmaxf(fmaxf(s.v0.y, s.v1.y), s.v2.y) - fminf(fminf(s.v0.y, s.v1.y), s.v2.y) + 1.0f;
+        const float delta = kU64 * BW * BH;
+        const float aa = fabsf(s.area);
+        float zlb = -1.0f;
+        if (aa > 2.0f * delta && zmin > 0.0f) zlb = zmin * (aa / (aa + delta)) * 0.99998474f;
+        sm.r0[j] = make_float4(s.v0.x, s.v0.y, s.v1.x, s.v1.y);
+        sm.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, __int_as_float(f));
+        sm.r2[j] = make_float4(s.v0.z, s.v1.z, s.v2.z, zlb);
+        sm.r3[j] = make_float4(sa, sb, sc, tol);
+        sm.r4[j] = make_int4(bx0, by0, bw, (1 << 20) / max(bw, 1) + ((1 << 20) % max(bw, 1) ? 1 : 0));
+        sm.cnt[j] = n;
+        const bool back = fmaf(sa, xc, fmaf(sb, yc, sc)) > 0.0f;
+        sm.back[j] = back ? 1 : 0;
+        if (back && n) sm.any_back = 1;
+        unsigned h = hash_fid(f) & (kHash - 1);
+        while (atomicCAS(&sm.hkey[h], -1, f) != -1) h = (h + 1) & (kHash - 1);
+        sm.hval[h] = (short)j;
+      }
+      __syncthreads();
+      raster_pass(sm, p, c, m, 0, tx0, ty0, tlog);
+      __syncthreads();
+      if (sm.any_back) {
+        // deepest key of the tile (+inf while any pixel is still empty)
+        if (tid == 0) sm.zmax_bits = 0.0f;
+        __syncthreads();
+        float zm = 0.0f;
+        for (int i = tid; i < T * T; i += kTileThreads) {
+          const int ly = i >> tlog, lx = i & (T - 1);
+          if (lx >= tw || ly >= th) continue;
+          const unsigned long long k = sm.keys[i];
+          zm = fmaxf(zm, k == kEmptyKey ? __int_as_float(0x7f800000) : key_depth(k));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) zm = fmaxf(zm, __shfl_xor_sync(0xffffffffu, zm, o));
+        if ((tid & 31) == 0) atomicMax((int*)&sm.zmax_bits, __float_as_int(zm));
+        __syncthreads();
+        const float zmax = sm.zmax_bits;
+        for (int j = tid; j < m; j += kTileThreads)
+          if (sm.back[j] && sm.r2[j].w > zmax) sm.cnt[j] = 0;
+        __syncthreads();
+        raster_pass(sm, p, c, m, 1, tx0, ty0, tlog);
+        __syncthreads();
+      }
+    }
+    if (n_total > p.bin_cap) {
+      // Faces past the bin's capacity: one thread per overflow entry.
+      const unsigned no = min(p.counters->overflow_count, (unsigned)p.overflow_cap);
+      for (unsigned o = tid; o < no; o += kTileThreads) {
+        const int2 e = p.overflow[o];
+        if (e.x != item) continue;
+        FaceSetup s;
+        setup_face_g(sm.mesh, c, e.y, s);
+        const float4 fn = __ldg(&sm.mesh.fnormals[e.y]);
+        for (int y = max(s.y0, ty0); y <= min(s.y1, ty0 + th - 1); ++y)
+          for (int x = max(s.x0, tx0); x <= min(s.x1, tx0 + tw - 1); ++x) {
+            const float3 r = ray_w(c, x, y);
+            const bool bf = dot3(fn.x, fn.y, fn.z, r.x, r.y, r.z) > 0.0f;
+            Bary b = edges_at(s, x, y);
+            if (!covered(b, bf)) continue;
+            const float z = perspective(s, b);
+            if (!orderable_depth(z)) {
+              atomicAdd(&p.counters->special, 1ull);
+              continue;
+            }
+            atomicMin(&sm.keys[((y - ty0) << tlog) + (x - tx0)], make_key(z, e.y, bf));
+          }
+      }
+      __syncthreads();
+    }
+
+    // Loop C for the tile's pixels.
+    const DevView& V = sm.view;
+    const int W = c.width;
+    for (int i = tid; i < T * T; i += kTileThreads) {
+      const int ly = i >> tlog, lx = i & (T - 1);
+      if (lx >= tw || ly >= th) continue;
+      const int x = tx0 + lx, y = ty0 + ly;
+      const int64_t pix = (int64_t)y * W + x;
+      const unsigned long long key = sm.keys[i];
+      float depth = 0.0f;
+      int32_t fid = -1;
+      uint8_t mask = 0;
+      Shaded sh;
+      sh.c[0] = sh.c[1] = sh.c[2] = 0;
+      sh.cf[0] = sh.cf[1] = sh.cf[2] = 0.0f;
+      sh.n[0] = sh.n[1] = sh.n[2] = 0.0f;
+      if (key != kEmptyKey && !(p.backface_culling && key_backface(key))) {
+        depth = key_depth(key);
+        fid = key_face(key);
+        if (fid > 0) {  // rasterizer.cc:254: face 0 is never shaded
+          mask = 255;
+          int slot = -1;
+          unsigned h = hash_fid(fid) & (kHash - 1);
+          for (int probe = 0; probe < kHash; ++probe) {
+            const int k = sm.hkey[h];
+            if (k == fid) {
+              slot = sm.hval[h];
+              break;
+            }
+            if (k == -1) break;
+            h = (h + 1) & (kHash - 1);
+          }
+          FaceSetup s;
+          if (slot >= 0) {
+            const float4 r0 = sm.r0[slot], r1 = sm.r1[slot], r2 = sm.r2[slot];
+            s.v0 = make_float3(r0.x, r0.y, r2.x);
+            s.v1 = make_float3(r0.z, r0.w, r2.y);
+            s.v2 = make_float3(r1.x, r1.y, r2.z);
+            s.area = r1.z;
+          } else {
+            s = project_face(sm.mesh, c, fid);
+          }
+          shade_face_pixel(p.shade, sm.mesh, c, fid, s, x, y, sh);
+        }
+      }
+      if (V.depth) V.depth[pix] = depth;
+      if (V.face_id) V.face_id[pix] = fid;
+      if (V.mask) V.mask[pix] = mask;
+      if (V.color) {
+        V.color[3 * pix + 0] = sh.c[0];
+        V.color[3 * pix + 1] = sh.c[1];
+        V.color[3 * pix + 2] = sh.c[2];
+      }
+      if (V.normal) {
+        V.normal[3 * pix + 0] = sh.n[0];
+        V.normal[3 * pix + 1] = sh.n[1];
+        V.normal[3 * pix + 2] = sh.n[2];
+      }
+      if (V.color_f32) {
+        V.color_f32[3 * pix + 0] = sh.cf[0];
+        V.color_f32[3 * pix + 1] = sh.cf[1];
+        V.color_f32[3 * pix + 2] = sh.cf[2];
+      }
+    }
+    if (tid == 0) p.tile_count[item] = 0;  // leave the bins empty for the next launch
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+void launch_bin(const TileParams& p, int grid, cudaStream_t s) {
+  k_bin<<<grid, kBinThreads, 0, s>>>(p);
+}
+
+void launch_tile(const TileParams& p, int grid, cudaStream_t s) {
+  k_tile<<<grid, kTileThreads, sizeof(TileSmem), s>>>(p);
+}
+
+int tile_kernel_blocks_per_sm() {
+  static int blocks = 0;
+  if (!blocks) {
+    cudaFuncSetAttribute(k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(TileSmem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_tile, kTileThreads,
+                                                  sizeof(TileSmem));
+    if (blocks < 1) blocks = 1;
+  }
+  return blocks;
+}
+
+int bin_kernel_blocks_per_sm() {
+  static int blocks = 0;
+  if (!blocks) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_bin, kBinThreads, 0);
+    if (blocks < 1) blocks = 1;
+  }
+  return blocks;
+}
+
+}  // namespace ugu_gpu
