@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-per-view", action="store_true")
     ap.add_argument("--views", type=int, default=N_VIEWS)
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
@@ -264,6 +265,9 @@ def main():
             setattr(v.images, k, x.data_ptr())
         outs.append(t)
         views.append(v)
+    tuned = ctx.autotune(views) if not args.no_autotune else ctx.tuning()
+    tuning = {"path": ["tiled", "global"][tuned.path], "tile": 1 << tuned.tile_log2,
+              "bin_capacity": tuned.bin_capacity}
     plan = ctx.plan_create(views, capi.DEVICE_POINTERS)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
@@ -370,7 +374,8 @@ def main():
                    "pixels": total_px, "mesh_faces": m.num_faces, "mesh_vertices": m.num_vertices,
                    "texture": "2048x2048 RGB8", "outputs": "color,depth,normal,mask,face_id",
                    "l2": "flushed (256 MB write) between timed steps",
-                   "launch": "one CUDA-graph replay of the batched render per step"},
+                   "launch": "one CUDA-graph replay of the batched render per step",
+                   "tuning": tuning},
         "gpix_per_s": world * total_px / (ms_step / 1e3) / 1e9,
         "per_view_views_per_s": per_view,
         "batched_over_per_view": (views_per_s / world / per_view) if per_view else None,

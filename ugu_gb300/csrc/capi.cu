@@ -453,7 +453,7 @@ int enqueue_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& gr
     p.counters = s.tcounters + gi;
     CK(ctx, cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream),
        "cudaMemsetAsync(tile counters)");
-    launch_bin(p, persistent_grid(ctx, bin_kernel_blocks_per_sm()), ctx->stream);
+    launch_bin(p, gr.max_faces, ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
     nk += 2;
   }
@@ -710,7 +710,7 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->opt.oren_nayar_sigma = 0.3f;
   ctx->tuning.path = UGU_GPU_PATH_TILED;
   ctx->tuning.tile_log2 = 5;
-  ctx->tuning.bin_capacity = 2048;
+  ctx->tuning.bin_capacity = 8192;  // 8 faces per pixel of a 32x32 tile
   ctx->tuning.small_bbox_max = 256;
   ctx->tuning.group_pixels = 4 << 20;
   ctx->tuning.ctas_per_sm = 0;
@@ -997,11 +997,65 @@ int ugu_gpu_get_tuning(const ugu_gpu_context* ctx, ugu_gpu_tuning* t) {
 
 int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                      ugu_gpu_tuning* chosen) {
-  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
-  (void)n;
-  (void)views;
-  if (chosen) *chosen = ctx->tuning;
-  return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "autotune is not built yet");
+  if (!ctx || n <= 0 || !views)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad autotune arguments");
+  cudaSetDevice(ctx->device);
+  const ugu_gpu_tuning start = ctx->tuning;
+  // Candidates: the tiled path at both tile sizes with two bin capacities,
+  // and the global path at its default grouping.
+  std::vector<ugu_gpu_tuning> cands;
+  for (int tl : {4, 5})
+    for (int per_px : {4, 8}) {
+      ugu_gpu_tuning t = start;
+      t.path = UGU_GPU_PATH_TILED;
+      t.tile_log2 = tl;
+      t.bin_capacity = per_px << (2 * tl);
+      t.ctas_per_sm = 0;
+      cands.push_back(t);
+    }
+  {
+    ugu_gpu_tuning t = start;
+    t.path = UGU_GPU_PATH_GLOBAL;
+    t.tile_log2 = 4;
+    t.small_bbox_max = 256;
+    t.group_pixels = 8 << 20;
+    cands.push_back(t);
+  }
+  cudaEvent_t e0, e1;
+  CK(ctx, cudaEventCreate(&e0), "cudaEventCreate");
+  CK(ctx, cudaEventCreate(&e1), "cudaEventCreate");
+  float best = 1e30f;
+  ugu_gpu_tuning best_t = start;
+  int rc = UGU_GPU_OK;
+  for (const ugu_gpu_tuning& t : cands) {
+    if ((rc = ugu_gpu_set_tuning(ctx, &t))) break;
+    // warm up (allocates the candidate's scratch), then time three renders
+    if ((rc = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS))) break;
+    float ms = 0.0f;
+    for (int r = 0; r < 3 && !rc; ++r) {
+      cudaEventRecord(e0, ctx->stream);
+      rc = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS | UGU_GPU_ASYNC);
+      cudaEventRecord(e1, ctx->stream);
+      cudaEventSynchronize(e1);
+      float m = 0.0f;
+      cudaEventElapsedTime(&m, e0, e1);
+      ms += m;
+    }
+    if (rc) break;
+    if (ms < best) {
+      best = ms;
+      best_t = t;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) {
+    ugu_gpu_set_tuning(ctx, &start);
+    return rc;
+  }
+  rc = ugu_gpu_set_tuning(ctx, &best_t);
+  if (chosen) *chosen = best_t;
+  return rc;
 }
 
 int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,

@@ -123,7 +123,7 @@ struct TileParams {
 };
 
 // Host-side launchers (tile.cu).
-void launch_bin(const TileParams& p, int grid, cudaStream_t s);
+void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
 int tile_kernel_blocks_per_sm();
 int bin_kernel_blocks_per_sm();

@@ -35,15 +35,6 @@ constexpr int kHash = 512;       // fid -> chunk slot table (power of two)
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr float kU64 = 3.814697265625e-06f;  // 2^-18 = 64 ulp(1)
 
-__device__ __forceinline__ int find_view_by_batch(const TileParams& p, int64_t b) {
-  int lo = 0, hi = p.num_views - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (p.views[mid].batch_begin <= b) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 __device__ __forceinline__ int find_view_by_tile(const TileParams& p, int t) {
   int lo = 0, hi = p.num_views - 1;
   while (lo < hi) {
@@ -63,37 +54,43 @@ __device__ __forceinline__ bool setup_face_g(const DevMesh& m, const Cam& c, int
                     project(c, d.x, d.y, d.z), s);
 }
 
+// One block per (256 faces, view): the view's camera and mesh descriptor are
+// staged in shared memory once per block.
 __global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < p.total_batches;
-       b += nwarps) {
-    const int v = find_view_by_batch(p, b);
-    const DevView* V = &p.views[v];
-    const DevMesh* M = &p.meshes[V->mesh];
-    const int f = (int)((b - V->batch_begin) * 32) + lane;
-    if (f >= M->num_faces) continue;
-    const Cam c = V->cam;
-    FaceSetup s;
-    if (!setup_face_g(*M, c, f, s)) continue;
-    if (s.x1 < s.x0 || s.y1 < s.y0) continue;
-    const int ts = p.tile_log2;
-    const int tx0 = s.x0 >> ts, tx1 = s.x1 >> ts, ty0 = s.y0 >> ts, ty1 = s.y1 >> ts;
-    for (int ty = ty0; ty <= ty1; ++ty)
-      for (int tx = tx0; tx <= tx1; ++tx) {
-        const int t = V->tile_base + ty * V->tiles_x + tx;
-        const int slot = atomicAdd(&p.tile_count[t], 1);
-        if (slot < p.bin_cap) {
-          p.bins[(int64_t)t * p.bin_cap + slot] = f;
-        } else {
-          const unsigned o = atomicAdd(&p.counters->overflow_count, 1u);
-          if (o < (unsigned)p.overflow_cap)
-            p.overflow[o] = make_int2(t, f);
-          else
-            atomicAdd(&p.counters->dropped, 1ull);
-        }
-      }
+  __shared__ DevView sv;
+  __shared__ DevMesh sm;
+  {
+    const int* src = reinterpret_cast<const int*>(&p.views[blockIdx.y]);
+    int* dst = reinterpret_cast<int*>(&sv);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevView) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    const int* msrc = reinterpret_cast<const int*>(&p.meshes[sv.mesh]);
+    int* mdst = reinterpret_cast<int*>(&sm);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevMesh) / 4); i += blockDim.x) mdst[i] = msrc[i];
+    __syncthreads();
   }
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= sm.num_faces) return;
+  const Cam& c = sv.cam;
+  FaceSetup s;
+  if (!setup_face_g(sm, c, f, s)) return;
+  if (s.x1 < s.x0 || s.y1 < s.y0) return;
+  const int ts = p.tile_log2;
+  const int tx0 = s.x0 >> ts, tx1 = s.x1 >> ts, ty0 = s.y0 >> ts, ty1 = s.y1 >> ts;
+  for (int ty = ty0; ty <= ty1; ++ty)
+    for (int tx = tx0; tx <= tx1; ++tx) {
+      const int t = sv.tile_base + ty * sv.tiles_x + tx;
+      const int slot = atomicAdd(&p.tile_count[t], 1);
+      if (slot < p.bin_cap) {
+        p.bins[(int64_t)t * p.bin_cap + slot] = f;
+      } else {
+        const unsigned o = atomicAdd(&p.counters->overflow_count, 1u);
+        if (o < (unsigned)p.overflow_cap)
+          p.overflow[o] = make_int2(t, f);
+        else
+          atomicAdd(&p.counters->dropped, 1ull);
+      }
+    }
 }
 
 struct TileSmem {
@@ -405,7 +402,8 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
 
 }  // namespace
 
-void launch_bin(const TileParams& p, int grid, cudaStream_t s) {
+void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {
+  dim3 grid((max_faces + kBinThreads - 1) / kBinThreads, p.num_views);
   k_bin<<<grid, kBinThreads, 0, s>>>(p);
 }
 

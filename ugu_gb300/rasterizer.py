@@ -144,6 +144,14 @@ class Context:
     def set_tuning(self, t: capi.Tuning) -> int:
         return self.lib.ugu_gpu_set_tuning(self.h, C.byref(t))
 
+    def autotune(self, views) -> capi.Tuning:
+        """Times candidate tunings on these views (device pointers) and keeps
+        the fastest; returns it."""
+        arr = (capi.View * len(views))(*views)
+        t = capi.Tuning()
+        self.check(self.lib.ugu_gpu_autotune(self.h, len(views), C.addressof(arr), C.byref(t)))
+        return t
+
     def stats(self) -> capi.Stats:
         s = capi.Stats()
         self.check(self.lib.ugu_gpu_get_stats(self.h, C.byref(s)))
