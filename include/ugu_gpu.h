@@ -214,6 +214,60 @@ UGU_GPU_API int ugu_gpu_synchronize(ugu_gpu_context* ctx);
 /* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
 UGU_GPU_API int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream);
 
+/* --- rendering without allocating ---------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: a plug-in whose host application owns all device memory and hands
+ * out only finished buffers; code held to a fixed device-memory budget by
+ * another allocator, where one more cudaMalloc would fail or fragment its
+ * pool; a frame loop that cannot take the device synchronisation cudaMalloc
+ * and cudaFree may cause.  ugu_gpu_render_noalloc renders one view with the
+ * global-z-buffer kernels, allocates nothing (no cudaMalloc, no cudaFree, no
+ * allocating library call) and needs no context: the mesh and the output
+ * images are the caller's device buffers, and the scratch (z-buffer,
+ * descriptors, counters, large-face tile list) is a static device array of
+ * about 20 MB that every GPU loading this library keeps until the process
+ * exits.
+ *
+ * Limits: width * height <= UGU_GPU_NOALLOC_MAX_PIXELS, at most
+ * UGU_GPU_NOALLOC_MAX_MATERIALS materials; larger requests return
+ * UGU_GPU_ERR_CAPACITY.  The mesh arrays must be in the 4-wide layout below
+ * (16-byte aligned) with in-range indices: device-resident indices are not
+ * checked.  The first call on a device looks up the array's device address
+ * for that device; make that first call before any stream capture.  All
+ * calls share the array and it keeps the last call's contents (each call
+ * clears what it needs first), so calls whose GPU work overlaps -- on
+ * different streams or from different host threads -- race and must be
+ * serialised by the caller.  Runs on the current device and on `stream`
+ * (NULL = default stream) and returns when the images are written; errors
+ * are reported in ugu_gpu_last_error(NULL). */
+#define UGU_GPU_NOALLOC_MAX_PIXELS 2097152 /* e.g. 1920 x 1080 */
+#define UGU_GPU_NOALLOC_MAX_MATERIALS 16
+
+typedef struct {
+  int32_t width, height;
+  const uint32_t* rgba8; /* device, H*W texels r | g << 8 | b << 16, or NULL */
+  const float* rgb_f32;  /* device, H*W*3, or NULL */
+} ugu_gpu_device_texture;
+
+typedef struct {
+  int32_t num_vertices, num_faces, num_normals, num_uv, num_materials;
+  const float* vertices4;          /* device, V*4: x, y, z, unused */
+  const int32_t* vertex_indices4;  /* device, F*4: i0, i1, i2, unused */
+  const float* face_normals4;      /* device, F*4 */
+  const float* normals4;           /* device, N*4, or NULL */
+  const int32_t* normal_indices4;  /* device, F*4, or NULL */
+  const float* vertex_colors4;     /* device, V*4, or NULL */
+  const float* uv2;                /* device, T*2, or NULL */
+  const int32_t* uv_indices4;      /* device, F*4, or NULL */
+  const int32_t* material_ids;     /* device, F, or NULL */
+  const ugu_gpu_device_texture* materials; /* host array of num_materials */
+} ugu_gpu_device_mesh;
+
+UGU_GPU_API int ugu_gpu_render_noalloc(const ugu_gpu_device_mesh* mesh,
+                                       const ugu_gpu_option* opt,
+                                       const ugu_gpu_camera* cam,
+                                       const ugu_gpu_images* images, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,8 +91,24 @@ EXPORTS = [
     "ugu_gpu_set_option", "ugu_gpu_set_mesh", "ugu_gpu_render", "ugu_gpu_render_views",
     "ugu_gpu_plan_create", "ugu_gpu_plan_launch", "ugu_gpu_plan_destroy", "ugu_gpu_backward",
     "ugu_gpu_set_tuning", "ugu_gpu_get_tuning", "ugu_gpu_autotune", "ugu_gpu_get_stats",
-    "ugu_gpu_synchronize", "ugu_gpu_set_stream",
+    "ugu_gpu_synchronize", "ugu_gpu_set_stream", "ugu_gpu_render_noalloc",
 ]
+
+NOALLOC_MAX_PIXELS = 2097152
+NOALLOC_MAX_MATERIALS = 16
+
+
+class DeviceTexture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgba8", P), ("rgb_f32", P)]
+
+
+class DeviceMesh(C.Structure):
+    _fields_ = [("num_vertices", C.c_int32), ("num_faces", C.c_int32),
+                ("num_normals", C.c_int32), ("num_uv", C.c_int32),
+                ("num_materials", C.c_int32), ("vertices4", P), ("vertex_indices4", P),
+                ("face_normals4", P), ("normals4", P), ("normal_indices4", P),
+                ("vertex_colors4", P), ("uv2", P), ("uv_indices4", P), ("material_ids", P),
+                ("materials", P)]
 
 _lib = None
 
@@ -125,6 +141,8 @@ def load(path: str | None = None):
     lib.ugu_gpu_get_stats.argtypes = [P, C.POINTER(Stats)]
     lib.ugu_gpu_synchronize.argtypes = [P]
     lib.ugu_gpu_set_stream.argtypes = [P, P]
+    lib.ugu_gpu_render_noalloc.argtypes = [C.POINTER(DeviceMesh), C.POINTER(Option),
+                                           C.POINTER(CameraDesc), C.POINTER(Images), P]
     for name in EXPORTS:
         if name != "ugu_gpu_last_error":
             getattr(lib, name).restype = C.c_int

@@ -77,6 +77,11 @@ struct Group {
 
 }  // namespace
 
+namespace ugu_gpu {
+// Error message for ugu_gpu_last_error(NULL) from entry points without a context.
+void set_thread_error(const char* msg) { g_create_error = msg; }
+}  // namespace ugu_gpu
+
 struct ugu_gpu_context {
   int device = 0;
   int num_sms = 0;
