@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--no-per-view", action="store_true")
     ap.add_argument("--views", type=int, default=N_VIEWS)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-backward", action="store_true")
+    ap.add_argument("--workload", default="ring64",
+                    choices=["ring64", "uvsphere", "single1080", "texdescent256"],
+                    help="ring64 (default): the batched-forward workload; the others "
+                         "measure the single-view and large fwd+bwd configurations")
     return ap.parse_args()
 
 
@@ -104,6 +109,23 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    """The slowest rank's per-step time (the contract's max over ranks)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_views_per_s(n_views: int, ms_step_max: float, world: int) -> float:
+    """Replicas only: every rank renders the whole batch of views, so the
+    job renders world * n_views views per (slowest) step."""
+    return world * n_views / (ms_step_max / 1e3)
 
 
 def measured_peak_hbm():
@@ -170,6 +192,62 @@ def cpu_oracle_views_per_s(m, cams, threads, max_views=None):
     return len(views) / dt, px / dt / 1e9, dt, len(views)
 
 
+def measure_fwd_bwd(ctx, torch, dev, stream, flush, timed, args, n_views=16, size=(640, 480)):
+    import numpy as np
+
+    from ugu_gb300 import capi, scenes
+    m = scenes.icosphere_textured(7, 2048, f32=True)
+    t = m.copy()
+    t.textures = [scenes.random_u8(5, m.textures[0].shape)]
+    t.textures_f32 = [t.textures[0].astype(np.float32)]
+    r = np.sqrt((t.vertices.astype(np.float64) ** 2).sum(axis=1))
+    t.vertices = (t.vertices * (1.0 + 0.005 * scenes.normal(6, t.num_vertices) / r)[:, None]
+                  ).astype(np.float32)
+    cams = scenes.ring_cameras(n_views, 3.0, [size] * n_views)
+    ctx.check(ctx.set_mesh(1, m))
+    ctx.check(ctx.set_mesh(2, t))
+
+    def views_for(slot, outs):
+        tensors, views = [], []
+        for c in cams:
+            tt = {k: torch.empty((c.height, c.width) + ((3,) if k == "color_f32" else ()),
+                                 dtype=torch.float32 if k == "color_f32" else torch.int32,
+                                 device=dev) for k in outs}
+            v = capi.View()
+            v.mesh = slot
+            v.camera = capi.camera_struct(c)
+            for k, x in tt.items():
+                setattr(v.images, k, x.data_ptr())
+            tensors.append(tt)
+            views.append(v)
+        return tensors, views
+
+    tgt, tviews = views_for(2, ("color_f32",))
+    ctx.check(ctx.render_views(tviews, capi.DEVICE_POINTERS))
+    fw, fviews = views_for(1, ("face_id", "color_f32"))
+    plan = ctx.plan_create(fviews, capi.DEVICE_POINTERS)
+    gtex = torch.zeros(m.textures_f32[0].size, dtype=torch.float32, device=dev)
+    gpos = torch.zeros(3 * m.num_vertices, dtype=torch.float32, device=dev)
+    loss = torch.zeros(n_views, dtype=torch.float32, device=dev)
+    tptr = [x["color_f32"].data_ptr() for x in tgt]
+
+    def step():
+        ctx.check(plan.launch())
+        ctx.check(ctx.backward(fviews, tptr, gtex.data_ptr(), None, gpos.data_ptr(),
+                               loss.data_ptr(), capi.DEVICE_POINTERS | capi.ASYNC))
+
+    for _ in range(3):
+        step()
+    ctx.check(ctx.synchronize())
+    ms = timed(step, max(3, args.steps))
+    ctx.check(ctx.synchronize())
+    plan.close()
+    ms_step = sum(ms) / len(ms)
+    return {"views_per_s": n_views / (ms_step / 1e3), "ms_per_step": ms_step,
+            "workload": f"icosphere7_tex2048_f32_{n_views}x{size[0]}x{size[1]}",
+            "grads": "texels + vertex positions"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -221,10 +299,173 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_single(args, which):
+    """One view per step through the C ABI (device outputs, graph replay):
+    the UV-sphere vertex-colour view at 640x480 or the textured icosphere-7
+    view at 1920x1080; the oracle on one host core beside it."""
+    import torch
+
+    from ugu_gb300 import capi, scenes
+    from ugu_gb300.rasterizer import Context, RendererCpuOption
+    if which == "uvsphere":
+        m, cam = scenes.scene_uv_sphere_vertex_color()
+        opt = RendererCpuOption(diffuse_color=2, interp=1, shading_normal=1, backface_culling=True)
+    else:
+        m, cam = scenes.scene_icosphere_single_view()
+        opt = option()
+    ctx = Context(0)
+    ctx.check(ctx.set_mesh(0, m))
+    ctx.check(ctx.set_option(opt))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.check(ctx.set_stream(stream.cuda_stream))
+    H, W = cam.height, cam.width
+    t = {"color": torch.empty((H, W, 3), dtype=torch.uint8, device="cuda"),
+         "depth": torch.empty((H, W), dtype=torch.float32, device="cuda"),
+         "normal": torch.empty((H, W, 3), dtype=torch.float32, device="cuda"),
+         "mask": torch.empty((H, W), dtype=torch.uint8, device="cuda"),
+         "face_id": torch.empty((H, W), dtype=torch.int32, device="cuda")}
+    v = capi.View()
+    v.mesh = 0
+    v.camera = capi.camera_struct(cam)
+    for k, x in t.items():
+        setattr(v.images, k, x.data_ptr())
+    tuned = ctx.autotune([v])
+    plan = ctx.plan_create([v], capi.DEVICE_POINTERS)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        ctx.check(plan.launch())
+    ctx.check(ctx.synchronize())
+    ev = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.check(plan.launch())
+        b.record(stream)
+        ev.append((a, b))
+    ctx.check(ctx.synchronize())
+    ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+    import oracle
+    oracle.build()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        rc, _, _ = oracle.render(m, cam, opt)
+    cpu = reps / (time.perf_counter() - t0)
+    print(json.dumps({"metric": "views/s", "value": 1e3 / ms, "unit": "views/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                      "gpix_per_s": W * H / (ms / 1e3) / 1e9,
+                      "config": {"workload": which, "pixels": W * H, "faces": m.num_faces,
+                                 "tuning": {"path": ["tiled", "global"][tuned.path],
+                                            "tile": 1 << tuned.tile_log2}},
+                      "cpu_baseline": {"value": cpu, "unit": "views/s", "cores": 1,
+                                       "kind": "port"}}), flush=True)
+
+
+class _DeviceArray:
+    """A device buffer as __cuda_array_interface__ (zero-copy for torch)."""
+
+    def __init__(self, ptr, shape, typestr="<f4"):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr,
+                                         "data": (int(ptr), False), "version": 3}
+
+
+def run_texdescent(args, n_views=256, iters=20, lr=0.1):
+    """The large forward+backward: icosphere-8 (1,310,720 faces, radial noise
+    0.01), a 4096^2 float texture, 256 Fibonacci-sphere cameras at distance
+    3, 1280x720, fx = 1000; 20 iterations of texture gradient descent
+    (texel -= 0.1 * dL/dtexel), each a batched forward (face_id + float
+    colour) and a backward against fixed target images (a second seeded
+    texture).  The texels are updated in place in the mesh slot's device
+    copy (ugu_gpu_get_device_mesh)."""
+    import numpy as np
+    import torch
+
+    from ugu_gb300 import capi, scenes
+    from ugu_gb300.rasterizer import Context, RendererCpuOption
+    t_setup = time.perf_counter()
+    m = scenes.icosphere(8, 1.0, 0.01, seed=1)
+    scenes.calc_normals(m)
+    scenes.with_texture(m, 4096, seed=3, f32=True)
+    tm = m.copy()
+    tm.textures = [scenes.random_u8(5, m.textures[0].shape)]
+    tm.textures_f32 = [tm.textures[0].astype(np.float32)]
+    cams = scenes.fibonacci_cameras(n_views, 3.0, 1280, 720, 1000.0)
+    ctx = Context(0)
+    ctx.check(ctx.set_option(RendererCpuOption(diffuse_color=1, interp=1, shading_normal=1,
+                                               backface_culling=True)))
+    ctx.check(ctx.set_mesh(0, m))
+    ctx.check(ctx.set_mesh(1, tm))
+    dev = torch.device("cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.check(ctx.set_stream(stream.cuda_stream))
+
+    def views_for(slot, outs):
+        tensors, views = [], []
+        for c in cams:
+            tt = {k: torch.empty((c.height, c.width) + ((3,) if k == "color_f32" else ()),
+                                 dtype=torch.float32 if k == "color_f32" else torch.int32,
+                                 device=dev) for k in outs}
+            v = capi.View()
+            v.mesh = slot
+            v.camera = capi.camera_struct(c)
+            for k, x in tt.items():
+                setattr(v.images, k, x.data_ptr())
+            tensors.append(tt)
+            views.append(v)
+        return tensors, views
+
+    tgt, tviews = views_for(1, ("color_f32",))
+    ctx.check(ctx.render_views(tviews, capi.DEVICE_POINTERS))
+    dm = ctx.device_mesh(0)
+    tex = torch.as_tensor(_DeviceArray(dm.textures[0].rgb_f32, m.textures_f32[0].shape),
+                          device=dev)
+    grad = torch.zeros_like(tex)
+    loss = torch.zeros(n_views, dtype=torch.float32, device=dev)
+    fw, fviews = views_for(0, ("face_id", "color_f32"))
+    plan = ctx.plan_create(fviews, capi.DEVICE_POINTERS)
+    tptr = [x["color_f32"].data_ptr() for x in tgt]
+    setup_s = time.perf_counter() - t_setup
+    losses = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for it in range(iters):
+        ctx.check(plan.launch())
+        grad.zero_()
+        loss.zero_()
+        ctx.check(ctx.backward(fviews, tptr, grad.data_ptr(), None, None, loss.data_ptr(),
+                               capi.DEVICE_POINTERS | capi.ASYNC))
+        tex.add_(grad, alpha=-lr)
+        losses.append(loss.sum())
+    e1.record(stream)
+    ctx.check(ctx.synchronize())
+    ms = e0.elapsed_time(e1)
+    losses = [float(x) for x in losses]
+    px = sum(c.width * c.height for c in cams)
+    plan.close()
+    ctx.close()
+    print(json.dumps({
+        "metric": "views/s (forward+backward)", "value": iters * n_views / (ms / 1e3),
+        "unit": "views/s", "n_gpus": 1, "steps": iters, "warmup": 0,
+        "ms_per_step": ms / iters, "gpix_per_s": iters * px / (ms / 1e3) / 1e9,
+        "config": {"workload": "texdescent256_icosphere8_tex4096_f32_1280x720",
+                   "views": n_views, "iterations": iters, "lr": lr, "faces": m.num_faces},
+        "loss_first": losses[0], "loss_last": losses[-1], "setup_s": setup_s}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload in ("uvsphere", "single1080"):
+        run_single(args, args.workload)
+        return
+    if args.workload == "texdescent256":
+        run_texdescent(args)
         return
     rank, world, local = dist_env()
     import torch
@@ -303,13 +544,8 @@ def main():
     clk = clocks.stop()
     ctx.check(ctx.synchronize())
     launches = ctx.stats().launches - launches0
-    ms_step = sum(ms) / len(ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    views_per_s = world * len(cams) / (ms_step / 1e3)
+    ms_step = max_over_ranks(sum(ms) / len(ms), world)
+    views_per_s = replica_views_per_s(len(cams), ms_step, world)
 
     # per-view launch sequences (no graph), same outputs
     per_view = None
@@ -355,6 +591,13 @@ def main():
         e2e = {"value": world * len(cams) / dt, "unit": "views/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h + 32 * 64}
 
+    # forward + backward: 16 ring views at 640x480 of the same mesh with float
+    # texels; a step is one graph-replayed forward (face_id + float colour)
+    # and one backward of the per-pixel L2 loss against fixed targets.
+    fwd_bwd = None
+    if not args.no_backward:
+        fwd_bwd = measure_fwd_bwd(ctx, torch, dev, stream, flush, timed, args)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -379,6 +622,7 @@ def main():
         "gpix_per_s": world * total_px / (ms_step / 1e3) / 1e9,
         "per_view_views_per_s": per_view,
         "batched_over_per_view": (views_per_s / world / per_view) if per_view else None,
+        "fwd_bwd": fwd_bwd,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": committed_traffic(),
                      "peak_source": peak_kind,

@@ -263,6 +263,13 @@ typedef struct {
   const ugu_gpu_device_texture* materials; /* host array of num_materials */
 } ugu_gpu_device_mesh;
 
+/* Device arrays of a mesh slot in the layout above (pointers owned by the
+ * context, valid until the slot is set again).  Lets a caller update the
+ * uploaded parameters in place, e.g. a gradient step on the float texels.
+ * No counterpart in the reference. */
+UGU_GPU_API int ugu_gpu_get_device_mesh(ugu_gpu_context* ctx, int32_t slot,
+                                        ugu_gpu_device_mesh* out);
+
 UGU_GPU_API int ugu_gpu_render_noalloc(const ugu_gpu_device_mesh* mesh,
                                        const ugu_gpu_option* opt,
                                        const ugu_gpu_camera* cam,

@@ -62,6 +62,13 @@ class OptionS(C.Structure):
                 ("backface_culling", C.c_int32), ("oren_nayar_sigma", C.c_float)]
 
 
+class PerturbS(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("index", C.c_int64), ("delta", C.c_double)]
+
+
+PERTURB_TEXEL, PERTURB_VCOLOR, PERTURB_VPOS = 1, 2, 3
+
+
 class StatsS(C.Structure):
     _fields_ = [("bbox_pixels", C.c_int64), ("covered", C.c_int64),
                 ("special_candidates", C.c_int64), ("texel_clamps", C.c_int64)]
@@ -89,7 +96,7 @@ def load():
         lib.oracle_render.restype = C.c_int
         lib.oracle_ray_w.argtypes = [P, C.c_int32, C.c_int32, P]
         lib.oracle_interp_f64.argtypes = [P, P, P, P, P, P, P]
-        lib.oracle_backward_f64.argtypes = [P, P, P, P, P, P, P, P]
+        lib.oracle_backward_f64.argtypes = [P, P, P, P, P, P, P, P, P]
         lib.oracle_backward_f64.restype = C.c_double
         lib.oracle_calc_normals.argtypes = [C.c_int32, P, C.c_int32, P, P, P]
         _lib = lib
@@ -235,8 +242,9 @@ def interp_f64(mesh, cam, opt, face_id):
 
 
 def backward_f64(mesh, cam, opt, face_id, target, grad_tex=None, grad_vcolor=None,
-                 grad_vpos=None) -> float:
-    """Accumulates FP64 gradients into the given float64 arrays; returns the loss."""
+                 grad_vpos=None, perturb=None) -> float:
+    """Accumulates FP64 gradients into the given float64 arrays; returns the
+    loss.  perturb = (kind, flat index, delta) moves one parameter in double."""
     lib = load()
     mh = _MeshHandle(mesh)
     cs = camera_struct(cam)
@@ -245,9 +253,11 @@ def backward_f64(mesh, cam, opt, face_id, target, grad_tex=None, grad_vcolor=Non
     tgt = np.ascontiguousarray(target, dtype=np.float32)
     for a in (grad_tex, grad_vcolor, grad_vpos):
         assert a is None or (a.dtype == np.float64 and a.flags.c_contiguous)
+    ps = None if perturb is None else PerturbS(int(perturb[0]), int(perturb[1]), float(perturb[2]))
     return lib.oracle_backward_f64(C.addressof(mh.s), C.addressof(cs), C.addressof(os_),
                                    fid.ctypes.data, tgt.ctypes.data, _ptr(grad_tex),
-                                   _ptr(grad_vcolor), _ptr(grad_vpos))
+                                   _ptr(grad_vcolor), _ptr(grad_vpos),
+                                   None if ps is None else C.addressof(ps))
 
 
 def calc_normals(vertices, faces):

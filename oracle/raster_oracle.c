@@ -459,17 +459,26 @@ static void setup64(const double* P, const int32_t* f, const oracle_camera* cam,
   for (int k = 0; k < 3; k++) r->w[k] = r->q[k] / r->s;
 }
 
+/* The parameter moved for finite differences (NULL = none); set by
+ * oracle_backward_f64 for the duration of one call. */
+static _Thread_local const oracle_perturb* g_pert = NULL;
+
+static double pert(int kind, int64_t index) {
+  return (g_pert && g_pert->kind == kind && g_pert->index == index) ? g_pert->delta : 0.0;
+}
+
 static double* positions64(const oracle_mesh* m) {
   double* P = (double*)malloc(((size_t)m->num_vertices + 1) * 3 * sizeof(double));
   if (!P) return NULL;
-  for (int i = 0; i < 3 * m->num_vertices; i++) P[i] = m->vertices[i];
+  for (int i = 0; i < 3 * m->num_vertices; i++) P[i] = m->vertices[i] + pert(3, i);
   return P;
 }
 
 static double texel64(const oracle_mesh* m, int mid, int64_t idx, int k) {
   const float* tf = m->textures_f32 ? m->textures_f32[mid] : NULL;
-  if (tf) return tf[3 * idx + k];
-  return (double)m->textures[mid].data[3 * idx + k];
+  double d = mid == 0 ? pert(1, 3 * idx + k) : 0.0;
+  if (tf) return tf[3 * idx + k] + d;
+  return (double)m->textures[mid].data[3 * idx + k] + d;
 }
 
 /* Colour of the differentiable path in double, plus its derivatives with
@@ -481,9 +490,9 @@ static void color64(const oracle_mesh* m, const oracle_option* o, int fid,
   if (o->diffuse_color == 2) {
     const int32_t* f = &m->vertex_indices[3 * fid];
     for (int k = 0; k < 3; k++) {
-      double c0 = m->vertex_colors[3 * f[0] + k];
-      double c1 = m->vertex_colors[3 * f[1] + k];
-      double c2 = m->vertex_colors[3 * f[2] + k];
+      double c0 = m->vertex_colors[3 * f[0] + k] + pert(2, 3 * f[0] + k);
+      double c1 = m->vertex_colors[3 * f[1] + k] + pert(2, 3 * f[1] + k);
+      double c2 = m->vertex_colors[3 * f[2] + k] + pert(2, 3 * f[2] + k);
       col[k] = s * c0 + u * c1 + v * c2;
       if (dcdu) dcdu[k] = c1 - c0;
       if (dcdv) dcdv[k] = c2 - c0;
@@ -589,10 +598,15 @@ static void edge_grad(double g, double ax, double ay, double bx, double by,
 double oracle_backward_f64(const oracle_mesh* m, const oracle_camera* cam,
                            const oracle_option* o, const int32_t* face_id,
                            const float* target, double* grad_tex,
-                           double* grad_vcolor, double* grad_vpos) {
+                           double* grad_vcolor, double* grad_vpos,
+                           const oracle_perturb* perturb) {
   const int W = cam->width, H = cam->height;
+  g_pert = perturb;
   double* P = positions64(m);
-  if (!P) return NAN;
+  if (!P) {
+    g_pert = NULL;
+    return NAN;
+  }
   double loss = 0.0;
   for (int y = 0; y < H; y++) {
     for (int x = 0; x < W; x++) {
@@ -660,6 +674,7 @@ double oracle_backward_f64(const oracle_mesh* m, const oracle_camera* cam,
     }
   }
   free(P);
+  g_pert = NULL;
   return loss;
 }
 

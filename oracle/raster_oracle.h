@@ -112,6 +112,15 @@ void oracle_interp_f64(const oracle_mesh* mesh, const oracle_camera* cam,
                        const oracle_option* opt, const int32_t* face_id,
                        double* depth, double* normal, double* color);
 
+/* One parameter moved by `delta` (in double) inside the FP64 path, for
+ * finite differences: kind 1 = texel of material 0 (flat index into
+ * H*W*3), 2 = vertex colour (V*3), 3 = vertex position (V*3). */
+typedef struct {
+  int32_t kind;
+  int64_t index;
+  double delta;
+} oracle_perturb;
+
 /* FP64 analytic gradient of L = sum over pixels with face_id > 0 of
  * |C(p) - T(p)|^2 where C is the float colour of the differentiable path
  * (float RGB texture, bilinear; or float vertex colours), visibility held
@@ -121,7 +130,8 @@ void oracle_interp_f64(const oracle_mesh* mesh, const oracle_camera* cam,
 double oracle_backward_f64(const oracle_mesh* mesh, const oracle_camera* cam,
                            const oracle_option* opt, const int32_t* face_id,
                            const float* target, double* grad_tex,
-                           double* grad_vcolor, double* grad_vpos);
+                           double* grad_vcolor, double* grad_vpos,
+                           const oracle_perturb* perturb);
 
 /* Mesh::CalcFaceNormal / Mesh::CalcNormal (src/mesh.cc:297-349). */
 void oracle_calc_normals(int32_t num_vertices, const float* vertices,

@@ -92,6 +92,7 @@ EXPORTS = [
     "ugu_gpu_plan_create", "ugu_gpu_plan_launch", "ugu_gpu_plan_destroy", "ugu_gpu_backward",
     "ugu_gpu_set_tuning", "ugu_gpu_get_tuning", "ugu_gpu_autotune", "ugu_gpu_get_stats",
     "ugu_gpu_synchronize", "ugu_gpu_set_stream", "ugu_gpu_render_noalloc",
+    "ugu_gpu_get_device_mesh",
 ]
 
 NOALLOC_MAX_PIXELS = 2097152
@@ -143,6 +144,7 @@ def load(path: str | None = None):
     lib.ugu_gpu_set_stream.argtypes = [P, P]
     lib.ugu_gpu_render_noalloc.argtypes = [C.POINTER(DeviceMesh), C.POINTER(Option),
                                            C.POINTER(CameraDesc), C.POINTER(Images), P]
+    lib.ugu_gpu_get_device_mesh.argtypes = [P, C.c_int32, C.POINTER(DeviceMesh)]
     for name in EXPORTS:
         if name != "ugu_gpu_last_error":
             getattr(lib, name).restype = C.c_int

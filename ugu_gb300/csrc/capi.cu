@@ -27,6 +27,7 @@ thread_local std::string g_create_error;
 struct MeshSlot {
   bool present = false;
   DevMesh dev{};
+  std::vector<ugu_gpu_device_texture> dev_tex;  // device texture pointers, host copy
   std::vector<void*> allocs;
   bool has_fnormals = false, has_normals = false, has_vcolors = false;
   bool has_uv = false, has_matids = false;
@@ -65,6 +66,10 @@ struct Scratch {
   size_t tcounters_cap = 0;
   bool tiles_dirty = false;
   size_t list_min = size_t(1) << 22;  // capacity of the item / overflow lists
+  // backward: per-view target pointers
+  const float** d_targets = nullptr;
+  const float** h_targets = nullptr;  // pinned
+  size_t targets_cap = 0;
 };
 
 struct Group {
@@ -153,6 +158,8 @@ void free_scratch(Scratch& s) {
   cudaFree(s.overflow);
   cudaFree(s.tcounters);
   cudaFreeHost(s.h_tcounters);
+  cudaFree(s.d_targets);
+  cudaFreeHost(s.h_targets);
   s = Scratch();
 }
 
@@ -858,6 +865,9 @@ int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) 
       }
     }
     if ((rc = upload(ctx, s, tex, &d.textures))) return rc;
+    s.dev_tex.resize(tex.size());
+    for (size_t i = 0; i < tex.size(); ++i)
+      s.dev_tex[i] = {tex[i].width, tex[i].height, tex[i].rgba8, tex[i].rgbf};
   }
   CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &d, sizeof(DevMesh), cudaMemcpyHostToDevice),
      "cudaMemcpy(mesh table)");
@@ -1067,9 +1077,98 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                      const float* const* targets, float* grad_texels,
                      float* grad_vertex_colors, float* grad_vertices, float* loss_out,
                      uint32_t flags) {
-  (void)n; (void)views; (void)targets; (void)grad_texels; (void)grad_vertex_colors;
-  (void)grad_vertices; (void)loss_out; (void)flags;
-  return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "backward is not built yet");
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  if (n <= 0 || !views || !targets)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view or target list");
+  if (!(flags & UGU_GPU_DEVICE_POINTERS))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "backward works on device pointers");
+  cudaSetDevice(ctx->device);
+  const ugu_gpu_option& o = ctx->opt;
+  if (o.diffuse_color != 1 && o.diffuse_color != 2)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                     "backward needs texture or vertex colour as diffuse colour");
+  if (o.diffuse_shading != 0)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                     "backward differentiates the unshaded colour (diffuse_shading = kNone)");
+  int64_t max_px = 0;
+  for (int i = 0; i < n; ++i) {
+    ugu_gpu_view v = views[i];
+    if (!v.images.face_id || !targets[i])
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                       "view %d needs the forward's face_id image and a target", i);
+    int rc = validate_view(ctx, v, true);
+    if (rc) return rc;
+    max_px = std::max(max_px, (int64_t)v.camera.width * v.camera.height);
+  }
+  Scratch& s = ctx->scratch;
+  int rc = ensure_scratch(ctx, s, 0, (size_t)n, 0, 0);
+  if (rc) return rc;
+  if ((size_t)n > s.targets_cap) {
+    cudaFree(s.d_targets);
+    cudaFreeHost(s.h_targets);
+    s.d_targets = nullptr;
+    s.h_targets = nullptr;
+    s.targets_cap = 0;
+    CK(ctx, cudaMalloc(&s.d_targets, n * sizeof(float*)), "cudaMalloc(targets)");
+    CK(ctx, cudaMallocHost(&s.h_targets, n * sizeof(float*)), "cudaMallocHost(targets)");
+    s.targets_cap = n;
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  for (int i = 0; i < n; ++i) {
+    DevView& d = s.h_views[i];
+    std::memset(&d, 0, sizeof(d));
+    fill_cam(d.cam, views[i].camera);
+    d.mesh = views[i].mesh;
+    d.face_id = views[i].images.face_id;
+    s.h_targets[i] = targets[i];
+  }
+  CK(ctx, cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView), cudaMemcpyHostToDevice,
+                          ctx->stream),
+     "cudaMemcpyAsync(views)");
+  CK(ctx, cudaMemcpyAsync(s.d_targets, s.h_targets, n * sizeof(float*), cudaMemcpyHostToDevice,
+                          ctx->stream),
+     "cudaMemcpyAsync(targets)");
+  BackwardParams p{};
+  p.meshes = ctx->d_meshes;
+  p.views = s.d_views;
+  p.num_views = n;
+  p.diffuse_color = o.diffuse_color;
+  p.interp = o.interp;
+  p.targets = s.d_targets;
+  p.grad_texels = grad_texels;
+  p.grad_vertex_colors = grad_vertex_colors;
+  p.grad_vertices = grad_vertices;
+  p.loss = loss_out;
+  launch_backward(p, max_px, ctx->stream);
+  CK(ctx, cudaGetLastError(), "backward launch");
+  ctx->launches += 1;
+  if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "backward");
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_get_device_mesh(ugu_gpu_context* ctx, int32_t slot, ugu_gpu_device_mesh* out) {
+  if (!ctx || !out) return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (slot < 0 || slot >= kMaxMeshes || !ctx->meshes[slot].present)
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh has not been initialized");
+  const MeshSlot& m = ctx->meshes[slot];
+  const DevMesh& d = m.dev;
+  out->num_vertices = d.num_vertices;
+  out->num_faces = d.num_faces;
+  out->num_normals = d.num_normals;
+  out->num_uv = d.num_uv;
+  out->num_materials = d.num_materials;
+  out->vertices4 = reinterpret_cast<const float*>(d.vertices);
+  out->vertex_indices4 = reinterpret_cast<const int32_t*>(d.vidx);
+  out->face_normals4 = reinterpret_cast<const float*>(d.fnormals);
+  out->normals4 = reinterpret_cast<const float*>(d.normals);
+  out->normal_indices4 = reinterpret_cast<const int32_t*>(d.nidx);
+  out->vertex_colors4 = reinterpret_cast<const float*>(d.vcolors);
+  out->uv2 = reinterpret_cast<const float*>(d.uv);
+  out->uv_indices4 = reinterpret_cast<const int32_t*>(d.uvidx);
+  out->material_ids = d.mat_ids;
+  out->materials = m.dev_tex.empty() ? nullptr : m.dev_tex.data();
+  return UGU_GPU_OK;
 }
 
 int ugu_gpu_get_stats(const ugu_gpu_context* ctx, ugu_gpu_stats* st) {

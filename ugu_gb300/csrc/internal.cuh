@@ -122,6 +122,21 @@ struct TileParams {
   TileCounters* counters;
 };
 
+struct BackwardParams {
+  const DevMesh* meshes;
+  const DevView* views;  // face_id: the forward's visibility (device)
+  int32_t num_views;
+  int32_t diffuse_color, interp;
+  const float* const* targets;  // device array of per-view H*W*3 targets
+  float* grad_texels;           // material 0, H*W*3 (or NULL)
+  float* grad_vertex_colors;    // V*3 (or NULL)
+  float* grad_vertices;         // V*3 (or NULL)
+  float* loss;                  // one per view (or NULL)
+};
+
+// Host-side launcher (backward.cu).
+void launch_backward(const BackwardParams& p, int64_t max_pixels, cudaStream_t s);
+
 // Host-side launchers (tile.cu).
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);

@@ -14,10 +14,11 @@
 //           atomicMin, then run Loop C (rasterizer.cc:244-301) for the
 //           tile's pixels and write the outputs.
 //
-// Faces whose normal points away from the tile's centre ray are drawn after
-// the others and skipped when a proven lower bound of their depth lies
-// behind the deepest key of a fully covered tile: such a face can never win
-// the z-test there, so the result is unchanged.
+// Faces whose normal points away from the ray to their centroid (k_bin
+// marks them in bit 31 of the bin entry) are drawn after all the others and
+// skipped when a proven lower bound of their depth lies behind the deepest
+// key of a fully covered tile: such a face can never win the z-test there,
+// so the result is unchanged.
 #include <cuda_runtime.h>
 
 #include "internal.cuh"
@@ -70,19 +71,55 @@ __global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
     __syncthreads();
   }
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= sm.num_faces) return;
+  const int lane = threadIdx.x & 31;
   const Cam& c = sv.cam;
   FaceSetup s;
-  if (!setup_face_g(sm, c, f, s)) return;
-  if (s.x1 < s.x0 || s.y1 < s.y0) return;
+  bool live = false;
+  uint32_t entry = 0;
+  if (f < sm.num_faces) {
+    const int4 vi = __ldg(&sm.vidx[f]);
+    const float4 a = __ldg(&sm.vertices[vi.x]);
+    const float4 b = __ldg(&sm.vertices[vi.y]);
+    const float4 d = __ldg(&sm.vertices[vi.z]);
+    live = face_setup(c, project(c, a.x, a.y, a.z), project(c, b.x, b.y, b.z),
+                      project(c, d.x, d.y, d.z), s) &&
+           s.x1 >= s.x0 && s.y1 >= s.y0;
+    if (live) {
+      // Draw-order class only (never changes a result): faces whose normal
+      // points away from the ray to their centroid are drawn after the rest.
+      const float4 fn = __ldg(&sm.fnormals[f]);
+      const float ox = -(c.R[0] * c.t[0] + c.R[3] * c.t[1] + c.R[6] * c.t[2]);
+      const float oy = -(c.R[1] * c.t[0] + c.R[4] * c.t[1] + c.R[7] * c.t[2]);
+      const float oz = -(c.R[2] * c.t[0] + c.R[5] * c.t[1] + c.R[8] * c.t[2]);
+      const float gx = (a.x + b.x + d.x) * (1.0f / 3.0f) - ox;
+      const float gy = (a.y + b.y + d.y) * (1.0f / 3.0f) - oy;
+      const float gz = (a.z + b.z + d.z) * (1.0f / 3.0f) - oz;
+      const bool back = fn.x * gx + fn.y * gy + fn.z * gz > 0.0f;
+      entry = (uint32_t)f | (back ? 0x80000000u : 0u);
+    }
+  }
   const int ts = p.tile_log2;
-  const int tx0 = s.x0 >> ts, tx1 = s.x1 >> ts, ty0 = s.y0 >> ts, ty1 = s.y1 >> ts;
-  for (int ty = ty0; ty <= ty1; ++ty)
-    for (int tx = tx0; tx <= tx1; ++tx) {
-      const int t = sv.tile_base + ty * sv.tiles_x + tx;
-      const int slot = atomicAdd(&p.tile_count[t], 1);
+  int tx0 = 0, ty0 = 0, ntx = 0, n = 0;
+  if (live) {
+    tx0 = s.x0 >> ts;
+    ty0 = s.y0 >> ts;
+    ntx = (s.x1 >> ts) - tx0 + 1;
+    n = ntx * ((s.y1 >> ts) - ty0 + 1);
+  }
+  // Consecutive faces of a mesh are usually close on screen: the lanes that
+  // append to the same tile take their slots with one atomicAdd per tile.
+  for (int k = 0; k < n; ++k) {
+    const int t = sv.tile_base + (ty0 + k / ntx) * sv.tiles_x + tx0 + k % ntx;
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, t);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&p.tile_count[t], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const int slot = base + __popc(peers & ((1u << lane) - 1));
+    {
       if (slot < p.bin_cap) {
-        p.bins[(int64_t)t * p.bin_cap + slot] = f;
+        p.bins[(int64_t)t * p.bin_cap + slot] = (int32_t)entry;
       } else {
         const unsigned o = atomicAdd(&p.counters->overflow_count, 1u);
         if (o < (unsigned)p.overflow_cap)
@@ -91,36 +128,44 @@ __global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
           atomicAdd(&p.counters->dropped, 1ull);
       }
     }
+  }
 }
 
-struct TileSmem {
-  unsigned long long keys[kMaxTile * kMaxTile];
+// Faces of one tile set up in shared memory: one region for the faces drawn
+// first, one for the faces drawn second (so both stay available to the
+// resolve when a tile's list fits one window).
+struct Region {
   float4 r0[kChunk];  // v0.x v0.y v1.x v1.y
   float4 r1[kChunk];  // v2.x v2.y area fid-bits
   float4 r2[kChunk];  // v0.z v1.z v2.z depth lower bound
   float4 r3[kChunk];  // back-face sign: sa sb sc tolerance
   int4 r4[kChunk];    // bbox-in-tile x0 y0 width magic
-  int cnt[kChunk];    // pixels of bbox-in-tile, 0 when culled
-  unsigned char back[kChunk];
+  int cnt[kChunk];    // pixels of bbox-in-tile, 0 when skipped
   int hkey[kHash];
   short hval[kHash];
+};
+
+struct TileSmem {
+  unsigned long long keys[kMaxTile * kMaxTile];
+  Region reg[2];
   int pre[kWarps][33];
   DevView view;
   DevMesh mesh;
   int item;
   int any_back;
-  float zmax_bits;
+  unsigned zmax_bits;
 };
 
 __device__ __forceinline__ unsigned hash_fid(int f) { return ((unsigned)f * 2654435761u) >> 23; }
 
-// Loop B's per-pixel body (rasterizer.cc:196-237) for chunk face j at (x, y),
-// into the tile's shared z-buffer.
-__device__ __forceinline__ void test_pair(TileSmem& sm, const TileParams& p, const Cam& c, int j,
-                                          int x, int y, int tx0, int ty0, int tlog) {
-  const float4 r0 = sm.r0[j];
-  const float4 r1 = sm.r1[j];
-  const float4 r3 = sm.r3[j];
+// Loop B's per-pixel body (rasterizer.cc:196-237) for region face j at
+// (x, y), into the tile's shared z-buffer.
+__device__ __forceinline__ void test_pair(TileSmem& sm, const Region& R, const TileParams& p,
+                                          const Cam& c, int j, int x, int y, int tx0, int ty0,
+                                          int tlog) {
+  const float4 r0 = R.r0[j];
+  const float4 r1 = R.r1[j];
+  const float4 r3 = R.r3[j];
   const int fid = __float_as_int(r1.w);
   // sign of face_normal . ray_w: the affine surrogate decides unless it is
   // within its error bound of zero; then the reference's ray is computed.
@@ -141,7 +186,7 @@ __device__ __forceinline__ void test_pair(TileSmem& sm, const TileParams& p, con
   s.v2 = make_float3(r1.x, r1.y, 0.0f);
   Bary b = edges_at(s, x, y);
   if (!covered(b, bf)) return;
-  const float4 r2 = sm.r2[j];
+  const float4 r2 = R.r2[j];
   s.v0.z = r2.x;
   s.v1.z = r2.y;
   s.v2.z = r2.z;
@@ -156,15 +201,21 @@ __device__ __forceinline__ void test_pair(TileSmem& sm, const TileParams& p, con
   if (key < *(volatile unsigned long long*)kp) atomicMin(kp, key);
 }
 
-// Warp-cooperative pass over the chunk's faces with back == want_back.
-__device__ __forceinline__ void raster_pass(TileSmem& sm, const TileParams& p, const Cam& c,
-                                            int m, unsigned char want_back, int tx0, int ty0,
-                                            int tlog) {
+// Warp-cooperative pass over a region's faces: every lane first tests its
+// own face's first pixel; the remaining (face, pixel) pairs of the warp's 32
+// faces are spread over the lanes with a prefix scan of their counts.
+__device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const TileParams& p,
+                                            const Cam& c, int m, int tx0, int ty0, int tlog) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int base = warp * 32; base < m; base += kTileThreads) {
     const int j = base + lane;
-    const int cnt = (j < m && sm.back[j] == want_back) ? sm.cnt[j] : 0;
-    int incl = cnt;
+    const int cnt = j < m ? R.cnt[j] : 0;
+    if (cnt > 0) {
+      const int4 r4 = R.r4[j];
+      test_pair(sm, R, p, c, j, r4.x, r4.y, tx0, ty0, tlog);
+    }
+    const int rest = cnt > 1 ? cnt - 1 : 0;
+    int incl = rest;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int t = __shfl_up_sync(0xffffffffu, incl, o);
@@ -172,7 +223,7 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, const TileParams& p, c
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     int* pre = sm.pre[warp];
-    pre[lane] = incl - cnt;
+    pre[lane] = incl - rest;
     __syncwarp();
     for (int k = lane; k < total; k += 32) {
       int q = 0;
@@ -180,14 +231,25 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, const TileParams& p, c
       for (int step = 16; step > 0; step >>= 1)
         if (pre[q + step] <= k) q += step;
       const int jj = base + q;
-      const int local = k - pre[q];
-      const int4 r4 = sm.r4[jj];
+      const int local = k - pre[q] + 1;
+      const int4 r4 = R.r4[jj];
       const int yy = (local * r4.w) >> 20;
       const int xx = local - yy * r4.z;
-      test_pair(sm, p, c, jj, r4.x + xx, r4.y + yy, tx0, ty0, tlog);
+      test_pair(sm, R, p, c, jj, r4.x + xx, r4.y + yy, tx0, ty0, tlog);
     }
     __syncwarp();
   }
+}
+
+__device__ __forceinline__ int hash_lookup(const Region& R, int fid) {
+  unsigned h = hash_fid(fid) & (kHash - 1);
+  for (int probe = 0; probe < kHash; ++probe) {
+    const int k = R.hkey[h];
+    if (k == fid) return R.hval[h];
+    if (k == -1) return -1;
+    h = (h + 1) & (kHash - 1);
+  }
+  return -1;
 }
 
 __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
@@ -220,6 +282,8 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
     const int tx0 = txi << tlog, ty0 = tyi << tlog;
     const int tw = min(T, c.width - tx0), th = min(T, c.height - ty0);
     for (int i = tid; i < T * T; i += kTileThreads) sm.keys[i] = kEmptyKey;
+    for (int i = tid; i < kHash; i += kTileThreads) sm.reg[0].hkey[i] = sm.reg[1].hkey[i] = -1;
+    if (tid == 0) sm.any_back = 0;
     const int n_total = p.tile_count[item];
     const int n_bin = min(n_total, p.bin_cap);
     __syncthreads();
@@ -229,62 +293,14 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
     const float Dy = (c.height + fabsf(c.cy)) / c.fy;
     const float Dmax = 1.0f + fmaxf(fabsf(c.cx), fabsf(c.width - 1 - c.cx)) / c.fx +
                        fmaxf(fabsf(c.cy), fabsf(c.height - 1 - c.cy)) / c.fy;
-    const float xc = tx0 + 0.5f * (tw - 1), yc = ty0 + 0.5f * (th - 1);
 
-    for (int cs = 0; cs < n_bin; cs += kChunk) {
-      const int m = min(kChunk, n_bin - cs);
-      for (int i = tid; i < kHash; i += kTileThreads) sm.hkey[i] = -1;
-      if (tid == 0) sm.any_back = 0;
-      __syncthreads();
-      for (int j = tid; j < m; j += kTileThreads) {
-        const int f = p.bins[(int64_t)item * p.bin_cap + cs + j];
-        FaceSetup s;
-        setup_face_g(sm.mesh, c, f, s);  // succeeded in k_bin: same arithmetic
-        const int bx0 = max(s.x0, tx0), bx1 = min(s.x1, tx0 + tw - 1);
-        const int by0 = max(s.y0, ty0), by1 = min(s.y1, ty0 + th - 1);
-        const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;
-        const int n = (bw > 0 && bh > 0) ? bw * bh : 0;
-        // back-face surrogate: s(x, y) = (C^T n) . ((x-cx)/fx, (y-cy)/fy, 1)
-        const float4 fn = __ldg(&sm.mesh.fnormals[f]);
-        const float* C = c.C;
-        const float g0 = C[0] * fn.x + C[3] * fn.y + C[6] * fn.z;
-        const float g1 = C[1] * fn.x + C[4] * fn.y + C[7] * fn.z;
-        const float g2 = C[2] * fn.x + C[5] * fn.y + C[8] * fn.z;
-        const float G = (fabsf(C[0]) + fabsf(C[1]) + fabsf(C[2])) * fabsf(fn.x) +
-                        (fabsf(C[3]) + fabsf(C[4]) + fabsf(C[5])) * fabsf(fn.y) +
-                        (fabsf(C[6]) + fabsf(C[7]) + fabsf(C[8])) * fabsf(fn.z);
-        const float sa = g0 / c.fx, sb = g1 / c.fy;
-        const float sc = g2 - sa * c.cx - sb * c.cy;
-        const float tol = kU64 * (G * (1.0f + Dx + Dy) + fabsf(sa) * (c.width + fabsf(c.cx)) +
-                                  fabsf(sb) * (c.height + fabsf(c.cy)) + fabsf(g2)) +
-                          2.0f * kU64 * G * Dmax;
-        // lower bound of any depth the face can produce (see file comment)
-        const float zmin = fminf(fminf(s.v0.z, s.v1.z), s.v2.z);
-        const float BW = fmaxf(fmaxf(s.v0.x, s.v1.x), s.v2.x) - fminf(fminf(s.v0.x, s.v1.x), s.v2.x) + 1.0f;
-        const float BH = fmaxf(fmaxf(s.v0.y, s.v1.y), s.v2.y) - fminf(fminf(s.v0.y, s.v1.y), s.v2.y) + 1.0f;
-        const float delta = kU64 * BW * BH;
-        const float aa = fabsf(s.area);
-        float zlb = -1.0f;
-        if (aa > 2.0f * delta && zmin > 0.0f) zlb = zmin * (aa / (aa + delta)) * 0.99998474f;
-        sm.r0[j] = make_float4(s.v0.x, s.v0.y, s.v1.x, s.v1.y);
-        sm.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, __int_as_float(f));
-        sm.r2[j] = make_float4(s.v0.z, s.v1.z, s.v2.z, zlb);
-        sm.r3[j] = make_float4(sa, sb, sc, tol);
-        sm.r4[j] = make_int4(bx0, by0, bw, (1 << 20) / max(bw, 1) + ((1 << 20) % max(bw, 1) ? 1 : 0));
-        sm.cnt[j] = n;
-        const bool back = fmaf(sa, xc, fmaf(sb, yc, sc)) > 0.0f;
-        sm.back[j] = back ? 1 : 0;
-        if (back && n) sm.any_back = 1;
-        unsigned h = hash_fid(f) & (kHash - 1);
-        while (atomicCAS(&sm.hkey[h], -1, f) != -1) h = (h + 1) & (kHash - 1);
-        sm.hval[h] = (short)j;
-      }
-      __syncthreads();
-      raster_pass(sm, p, c, m, 0, tx0, ty0, tlog);
-      __syncthreads();
-      if (sm.any_back) {
+    for (int phase = 0; phase < 2; ++phase) {
+      Region& R = sm.reg[phase];
+      float zmax = __int_as_float(0x7f800000);
+      if (phase == 1) {
+        if (!sm.any_back) break;
         // deepest key of the tile (+inf while any pixel is still empty)
-        if (tid == 0) sm.zmax_bits = 0.0f;
+        if (tid == 0) sm.zmax_bits = 0u;
         __syncthreads();
         float zm = 0.0f;
         for (int i = tid; i < T * T; i += kTileThreads) {
@@ -295,13 +311,68 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) zm = fmaxf(zm, __shfl_xor_sync(0xffffffffu, zm, o));
-        if ((tid & 31) == 0) atomicMax((int*)&sm.zmax_bits, __float_as_int(zm));
+        if ((tid & 31) == 0) atomicMax(&sm.zmax_bits, __float_as_uint(zm));
         __syncthreads();
-        const float zmax = sm.zmax_bits;
-        for (int j = tid; j < m; j += kTileThreads)
-          if (sm.back[j] && sm.r2[j].w > zmax) sm.cnt[j] = 0;
+        zmax = __uint_as_float(sm.zmax_bits);
+      }
+      for (int cs = 0; cs < n_bin; cs += kChunk) {
+        const int m = min(kChunk, n_bin - cs);
+        if (cs > 0) {
+          for (int i = tid; i < kHash; i += kTileThreads) R.hkey[i] = -1;
+          __syncthreads();
+        }
+        for (int j = tid; j < m; j += kTileThreads) {
+          const uint32_t e = (uint32_t)p.bins[(int64_t)item * p.bin_cap + cs + j];
+          const int cls = (int)(e >> 31);
+          R.cnt[j] = 0;
+          if (cls != phase) {
+            if (cls) sm.any_back = 1;
+            continue;
+          }
+          const int f = (int)(e & 0x7fffffffu);
+          FaceSetup s;
+          setup_face_g(sm.mesh, c, f, s);  // succeeded in k_bin: same arithmetic
+          // lower bound of any depth the face can produce (see file comment)
+          const float zmin = fminf(fminf(s.v0.z, s.v1.z), s.v2.z);
+          const float BW = fmaxf(fmaxf(s.v0.x, s.v1.x), s.v2.x) -
+                           fminf(fminf(s.v0.x, s.v1.x), s.v2.x) + 1.0f;
+          const float BH = fmaxf(fmaxf(s.v0.y, s.v1.y), s.v2.y) -
+                           fminf(fminf(s.v0.y, s.v1.y), s.v2.y) + 1.0f;
+          const float delta = kU64 * BW * BH;
+          const float aa = fabsf(s.area);
+          float zlb = -1.0f;
+          if (aa > 2.0f * delta && zmin > 0.0f) zlb = zmin * (aa / (aa + delta)) * 0.99998474f;
+          if (zlb > zmax) continue;  // behind every key of a covered tile: cannot win
+          const int bx0 = max(s.x0, tx0), bx1 = min(s.x1, tx0 + tw - 1);
+          const int by0 = max(s.y0, ty0), by1 = min(s.y1, ty0 + th - 1);
+          const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;
+          if (bw <= 0 || bh <= 0) continue;
+          // back-face surrogate: s(x, y) = (C^T n) . ((x-cx)/fx, (y-cy)/fy, 1)
+          const float4 fn = __ldg(&sm.mesh.fnormals[f]);
+          const float* C = c.C;
+          const float g0 = C[0] * fn.x + C[3] * fn.y + C[6] * fn.z;
+          const float g1 = C[1] * fn.x + C[4] * fn.y + C[7] * fn.z;
+          const float g2 = C[2] * fn.x + C[5] * fn.y + C[8] * fn.z;
+          const float G = (fabsf(C[0]) + fabsf(C[1]) + fabsf(C[2])) * fabsf(fn.x) +
+                          (fabsf(C[3]) + fabsf(C[4]) + fabsf(C[5])) * fabsf(fn.y) +
+                          (fabsf(C[6]) + fabsf(C[7]) + fabsf(C[8])) * fabsf(fn.z);
+          const float sa = g0 / c.fx, sb = g1 / c.fy;
+          const float sc = g2 - sa * c.cx - sb * c.cy;
+          const float tol = kU64 * (G * (1.0f + Dx + Dy) + fabsf(sa) * (c.width + fabsf(c.cx)) +
+                                    fabsf(sb) * (c.height + fabsf(c.cy)) + fabsf(g2)) +
+                            2.0f * kU64 * G * Dmax;
+          R.r0[j] = make_float4(s.v0.x, s.v0.y, s.v1.x, s.v1.y);
+          R.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, __int_as_float(f));
+          R.r2[j] = make_float4(s.v0.z, s.v1.z, s.v2.z, zlb);
+          R.r3[j] = make_float4(sa, sb, sc, tol);
+          R.r4[j] = make_int4(bx0, by0, bw, (1 << 20) / bw + ((1 << 20) % bw ? 1 : 0));
+          R.cnt[j] = bw * bh;
+          unsigned h = hash_fid(f) & (kHash - 1);
+          while (atomicCAS(&R.hkey[h], -1, f) != -1) h = (h + 1) & (kHash - 1);
+          R.hval[h] = (short)j;
+        }
         __syncthreads();
-        raster_pass(sm, p, c, m, 1, tx0, ty0, tlog);
+        raster_pass(sm, R, p, c, m, tx0, ty0, tlog);
         __syncthreads();
       }
     }
@@ -352,20 +423,15 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
         fid = key_face(key);
         if (fid > 0) {  // rasterizer.cc:254: face 0 is never shaded
           mask = 255;
-          int slot = -1;
-          unsigned h = hash_fid(fid) & (kHash - 1);
-          for (int probe = 0; probe < kHash; ++probe) {
-            const int k = sm.hkey[h];
-            if (k == fid) {
-              slot = sm.hval[h];
-              break;
-            }
-            if (k == -1) break;
-            h = (h + 1) & (kHash - 1);
-          }
           FaceSetup s;
+          int r = 0, slot = hash_lookup(sm.reg[0], fid);
+          if (slot < 0) {
+            r = 1;
+            slot = hash_lookup(sm.reg[1], fid);
+          }
           if (slot >= 0) {
-            const float4 r0 = sm.r0[slot], r1 = sm.r1[slot], r2 = sm.r2[slot];
+            const Region& R = sm.reg[r];
+            const float4 r0 = R.r0[slot], r1 = R.r1[slot], r2 = R.r2[slot];
             s.v0 = make_float3(r0.x, r0.y, r2.x);
             s.v1 = make_float3(r0.z, r0.w, r2.y);
             s.v2 = make_float3(r1.x, r1.y, r2.z);

@@ -152,6 +152,28 @@ class Context:
         self.check(self.lib.ugu_gpu_autotune(self.h, len(views), C.addressof(arr), C.byref(t)))
         return t
 
+    def backward(self, views, targets, grad_texels=None, grad_vertex_colors=None,
+                 grad_vertices=None, loss=None, flags: int = capi.DEVICE_POINTERS) -> int:
+        """ugu_gpu_backward: views carry the forward's face_id images; targets,
+        gradients and loss are device pointers (ints) or None."""
+        arr = (capi.View * len(views))(*views)
+        tg = (C.c_void_p * len(targets))(*targets)
+        return self.lib.ugu_gpu_backward(self.h, len(views), C.addressof(arr), C.addressof(tg),
+                                         grad_texels, grad_vertex_colors, grad_vertices, loss,
+                                         int(flags))
+
+    def device_mesh(self, slot: int):
+        """The slot's device arrays (ugu_gpu_get_device_mesh) as a namespace
+        with .textures = [DeviceTexture, ...]."""
+        d = capi.DeviceMesh()
+        self.check(self.lib.ugu_gpu_get_device_mesh(self.h, int(slot), C.byref(d)))
+        tex = []
+        if d.materials:
+            arr = C.cast(d.materials, C.POINTER(capi.DeviceTexture))
+            tex = [arr[i] for i in range(d.num_materials)]
+        d.textures = tex
+        return d
+
     def stats(self) -> capi.Stats:
         s = capi.Stats()
         self.check(self.lib.ugu_gpu_get_stats(self.h, C.byref(s)))
