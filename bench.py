@@ -508,7 +508,7 @@ def main():
         views.append(v)
     tuned = ctx.autotune(views) if not args.no_autotune else ctx.tuning()
     tuning = {"path": ["tiled", "global"][tuned.path], "tile": 1 << tuned.tile_log2,
-              "bin_capacity": tuned.bin_capacity}
+              "entry_capacity": tuned.entry_capacity}
     plan = ctx.plan_create(views, capi.DEVICE_POINTERS)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 

@@ -141,7 +141,8 @@ enum {
 typedef struct {
   int32_t path;             /* UGU_GPU_PATH_TILED (default) or UGU_GPU_PATH_GLOBAL */
   int32_t tile_log2;        /* screen tile edge = 1 << tile_log2 pixels (4 or 5) */
-  int32_t bin_capacity;     /* tiled: face slots per tile before the overflow list */
+  int32_t entry_capacity;   /* tiled: initial (face, tile) entry buffer, 0 = automatic;
+                               grown to what a render reports it needs */
   int32_t small_bbox_max;   /* global: faces with larger bboxes are split by tile */
   int32_t group_pixels;     /* global: pixels of z-buffer kept live per view group */
   int32_t ctas_per_sm;      /* persistent-kernel blocks per SM (0 = occupancy limit) */

@@ -77,10 +77,10 @@ def test_icosphere7_textured_1080p(ctx, oracle_lib):
     compare(ref, got, "icosphere7")
 
 
-TUNINGS = [  # (path, tile_log2, bin_capacity, small_bbox_max, group_pixels)
-    (capi.PATH_TILED, 5, 2048, 256, 1 << 22),
-    (capi.PATH_TILED, 4, 512, 256, 1 << 22),
-    (capi.PATH_TILED, 5, 16, 256, 1 << 22),   # most faces go through the overflow list
+TUNINGS = [  # (path, tile_log2, entry_capacity, small_bbox_max, group_pixels)
+    (capi.PATH_TILED, 5, 0, 256, 1 << 22),
+    (capi.PATH_TILED, 4, 0, 256, 1 << 22),
+    (capi.PATH_TILED, 5, 16, 256, 1 << 22),   # entries overflow: the render is retried
     (capi.PATH_TILED, 4, 1, 256, 1 << 22),
     (capi.PATH_GLOBAL, 3, 2048, 0, 1 << 22),  # every face split into tile items
     (capi.PATH_GLOBAL, 4, 2048, 0, 1 << 22),

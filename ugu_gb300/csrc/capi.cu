@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -35,6 +36,7 @@ struct MeshSlot {
   bool all_textures_nonempty = true;
   bool all_textures_f32 = false;
   int tex0_w = 0, tex0_h = 0;
+  float centre[3] = {0.0f, 0.0f, 0.0f};  // bounding-box centre of the vertices
   size_t bytes = 0;
 };
 
@@ -55,12 +57,13 @@ struct Scratch {
   size_t d_out_cap = 0;
   bool keys_dirty = false;
   // tiled path
-  int32_t* tile_count = nullptr;
+  int32_t* tile_count = nullptr;  // 4 arrays: count, offsets (+1), lo cursor, hi cursor
   size_t tiles_cap = 0;
-  int32_t* bins = nullptr;
-  size_t bins_cap = 0;  // entries
-  int2* overflow = nullptr;
-  size_t overflow_cap = 0;
+  int2* entries = nullptr;
+  size_t entries_cap = 0;
+  size_t entries_min = 0;  // capacity asked for by the last overflow
+  float4* proj = nullptr;
+  size_t proj_cap = 0;
   TileCounters* tcounters = nullptr;
   TileCounters* h_tcounters = nullptr;  // pinned
   size_t tcounters_cap = 0;
@@ -76,8 +79,10 @@ struct Group {
   int first, count;
   int max_faces;
   int64_t max_pixels;
-  int64_t tiles;    // tiled path: screen tiles of the group's views
-  int64_t batches;  // tiled path: 32-face batches of the group's views
+  int64_t tiles;     // tiled path: screen tiles of the group's views
+  int64_t faces;     // tiled path: faces summed over the group's views
+  int64_t vertices;  // tiled path: vertices summed over the group's views
+  int max_vertices;
 };
 
 }  // namespace
@@ -154,8 +159,8 @@ void free_scratch(Scratch& s) {
   cudaFreeHost(s.h_views);
   cudaFree(s.d_out);
   cudaFree(s.tile_count);
-  cudaFree(s.bins);
-  cudaFree(s.overflow);
+  cudaFree(s.entries);
+  cudaFree(s.proj);
   cudaFree(s.tcounters);
   cudaFreeHost(s.h_tcounters);
   cudaFree(s.d_targets);
@@ -274,23 +279,26 @@ std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* 
   const ugu_gpu_tuning& t = ctx->tuning;
   const int64_t limit = t.path == UGU_GPU_PATH_GLOBAL ? (int64_t)t.group_pixels : INT64_MAX;
   std::vector<Group> g;
-  Group cur{0, 0, 0, 0, 0, 0};
+  Group cur{0, 0, 0, 0, 0, 0, 0, 0};
   int64_t acc = 0;
   for (int i = 0; i < n; ++i) {
     int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
     bool full = cur.count > 0 && (per_view || acc + px > limit);
     if (full) {
       g.push_back(cur);
-      cur = Group{i, 0, 0, 0, 0, 0};
+      cur = Group{i, 0, 0, 0, 0, 0, 0, 0};
       acc = 0;
     }
     const int F = ctx->meshes[views[i].mesh].dev.num_faces;
+    const int V = ctx->meshes[views[i].mesh].dev.num_vertices;
     cur.count++;
     acc += px;
     cur.max_faces = std::max(cur.max_faces, F);
+    cur.max_vertices = std::max(cur.max_vertices, V);
     cur.max_pixels = std::max(cur.max_pixels, px);
     cur.tiles += tiles_of(views[i].camera, t.tile_log2);
-    cur.batches += (F + 31) / 32;
+    cur.faces += F;
+    cur.vertices += V;
   }
   if (cur.count) g.push_back(cur);
   return g;
@@ -308,31 +316,38 @@ int64_t group_key_count(const std::vector<Group>& groups, const ugu_gpu_view* vi
 }
 
 int ensure_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups) {
-  size_t tiles = 0;
-  for (const Group& g : groups) tiles = std::max(tiles, (size_t)g.tiles);
-  const size_t cap = (size_t)ctx->tuning.bin_capacity;
+  size_t tiles = 0, verts = 0, faces = 0;
+  for (const Group& g : groups) {
+    tiles = std::max(tiles, (size_t)g.tiles);
+    verts = std::max(verts, (size_t)g.vertices);
+    faces = std::max(faces, (size_t)g.faces);
+  }
   if (tiles > s.tiles_cap) {
     cudaFree(s.tile_count);
     s.tile_count = nullptr;
     s.tiles_cap = 0;
-    CK(ctx, cudaMalloc(&s.tile_count, tiles * sizeof(int32_t)), "cudaMalloc(tile counts)");
+    CK(ctx, cudaMalloc(&s.tile_count, (4 * tiles + 1) * sizeof(int32_t)),
+       "cudaMalloc(tile offsets)");
     s.tiles_cap = tiles;
     s.tiles_dirty = true;
   }
-  if (tiles * cap > s.bins_cap) {
-    cudaFree(s.bins);
-    s.bins = nullptr;
-    s.bins_cap = 0;
-    CK(ctx, cudaMalloc(&s.bins, tiles * cap * sizeof(int32_t)), "cudaMalloc(tile bins)");
-    s.bins_cap = tiles * cap;
+  if (verts > s.proj_cap) {
+    cudaFree(s.proj);
+    s.proj = nullptr;
+    s.proj_cap = 0;
+    CK(ctx, cudaMalloc(&s.proj, verts * sizeof(float4)), "cudaMalloc(projected vertices)");
+    s.proj_cap = verts;
   }
-  if (s.overflow_cap < s.list_min) {
-    cudaFree(s.overflow);
-    s.overflow = nullptr;
-    s.overflow_cap = 0;
-    const size_t oc = s.list_min;
-    CK(ctx, cudaMalloc(&s.overflow, oc * sizeof(int2)), "cudaMalloc(bin overflow)");
-    s.overflow_cap = oc;
+  // (face, tile) entries: most faces touch one tile; a render that needs more
+  // reports how many, and the next attempt allocates that
+  const size_t want = std::min<size_t>(std::max(s.entries_min, faces + faces / 4 + 4096),
+                                       (size_t)INT32_MAX);
+  if (want > s.entries_cap) {
+    cudaFree(s.entries);
+    s.entries = nullptr;
+    s.entries_cap = 0;
+    CK(ctx, cudaMalloc(&s.entries, want * sizeof(int2)), "cudaMalloc(tile entries)");
+    s.entries_cap = want;
   }
   if (groups.size() > s.tcounters_cap) {
     cudaFree(s.tcounters);
@@ -442,36 +457,65 @@ int persistent_grid(ugu_gpu_context* ctx, int blocks_per_sm) {
   return ctx->num_sms * std::max(per_sm, 1);
 }
 
+TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) {
+  const ugu_gpu_option& o = ctx->opt;
+  TileParams p{};
+  p.meshes = ctx->d_meshes;
+  p.views = s.d_views + gr.first;
+  p.num_views = gr.count;
+  p.shade = shade_opts(o);
+  p.backface_culling = o.backface_culling ? 1 : 0;
+  p.tile_log2 = ctx->tuning.tile_log2;
+  p.total_tiles = (int32_t)gr.tiles;
+  p.max_vertices = gr.max_vertices;
+  p.entry_cap = (int64_t)s.entries_cap;
+  p.proj = s.proj;
+  p.tile_count = s.tile_count;
+  p.tile_off = s.tile_count + s.tiles_cap;
+  p.tile_lo = p.tile_off + s.tiles_cap + 1;
+  p.tile_hi = p.tile_lo + s.tiles_cap;
+  p.entries = s.entries;
+  p.counters = s.tcounters + gi;
+  return p;
+}
+
 int enqueue_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
                   int* kernels) {
-  const ugu_gpu_option& o = ctx->opt;
   int nk = 0;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const Group& gr = groups[gi];
-    TileParams p{};
-    p.meshes = ctx->d_meshes;
-    p.views = s.d_views + gr.first;
-    p.num_views = gr.count;
-    p.shade = shade_opts(o);
-    p.backface_culling = o.backface_culling ? 1 : 0;
-    p.tile_log2 = ctx->tuning.tile_log2;
-    p.total_tiles = (int32_t)gr.tiles;
-    p.bin_cap = ctx->tuning.bin_capacity;
-    p.total_batches = gr.batches;
-    p.tile_count = s.tile_count;
-    p.bins = s.bins;
-    p.overflow = s.overflow;
-    p.overflow_cap = (int32_t)s.overflow_cap;
-    p.counters = s.tcounters + gi;
+    TileParams p = tile_params(ctx, s, gr, gi);
     CK(ctx, cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream),
        "cudaMemsetAsync(tile counters)");
     launch_bin(p, gr.max_faces, ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
-    nk += 2;
+    nk += kBinKernels + 1;
   }
   CK(ctx, cudaGetLastError(), "kernel launch");
   *kernels = nk;
   return UGU_GPU_OK;
+}
+
+// Tiled path: count the (face, tile) entries of every group without
+// rendering, and make the entry buffer hold the largest count with room to
+// spare (a plan sizes its buffer this way before capture).
+int size_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups) {
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    TileParams p = tile_params(ctx, s, groups[gi], gi);
+    CK(ctx, cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream),
+       "cudaMemsetAsync(tile counters)");
+    launch_size(p, groups[gi].max_faces, ctx->stream);
+  }
+  CK(ctx, cudaGetLastError(), "kernel launch");
+  CK(ctx, cudaMemcpyAsync(s.h_tcounters, s.tcounters, groups.size() * sizeof(TileCounters),
+                          cudaMemcpyDeviceToHost, ctx->stream),
+     "cudaMemcpyAsync(tile counters)");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "sizing pass");
+  size_t need = 0;
+  for (size_t gi = 0; gi < groups.size(); ++gi)
+    need = std::max(need, (size_t)s.h_tcounters[gi].total_entries);
+  s.entries_min = std::max(s.entries_min, need + need / 8 + 4096);
+  return ensure_tiled(ctx, s, groups);
 }
 
 // Enqueue the kernels of every group (no synchronisation).
@@ -503,7 +547,7 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
   size_t off = 0;
   const int tlog = ctx->tuning.tile_log2;
   for (const Group& gr : groups) {
-    int64_t key_off = 0, tile_base = 0, batch_begin = 0;
+    int64_t key_off = 0, tile_base = 0, proj_off = 0;
     for (int i = gr.first; i < gr.first + gr.count; ++i) {
       const ugu_gpu_view& v = views[i];
       DevView& d = s.h_views[i];
@@ -517,8 +561,11 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
       d.tiles_x = (v.camera.width + T - 1) / T;
       d.tile_base = (int32_t)tile_base;
       tile_base += tiles_of(v.camera, tlog);
-      d.batch_begin = batch_begin;
-      batch_begin += (ctx->meshes[v.mesh].dev.num_faces + 31) / 32;
+      d.proj_offset = proj_off;
+      proj_off += ctx->meshes[v.mesh].dev.num_vertices;
+      // camera depth of the mesh's bounding-box centre (a draw-order split only)
+      const float* ce = ctx->meshes[v.mesh].centre;
+      d.split_z = d.cam.R[6] * ce[0] + d.cam.R[7] * ce[1] + d.cam.R[8] * ce[2] + d.cam.t[2];
       if (device_ptrs) {
         d.color = v.images.color;
         d.depth = v.images.depth;
@@ -565,7 +612,7 @@ int copy_back(ugu_gpu_context* ctx, const Scratch& s, int n, const ugu_gpu_view*
   return UGU_GPU_OK;
 }
 
-int check_counters(ugu_gpu_context* ctx, const Scratch& s, size_t ngroups) {
+int check_counters(ugu_gpu_context* ctx, Scratch& s, size_t ngroups) {
   uint64_t special = 0, overflow = 0, items = 0;
   for (size_t g = 0; g < ngroups; ++g) {
     if (ctx->tuning.path == UGU_GPU_PATH_GLOBAL) {
@@ -574,8 +621,13 @@ int check_counters(ugu_gpu_context* ctx, const Scratch& s, size_t ngroups) {
       items += s.h_counters[g].tile_items;
     } else {
       special += s.h_tcounters[g].special;
-      overflow += s.h_tcounters[g].dropped;
-      items += s.h_tcounters[g].overflow_count;
+      if (s.h_tcounters[g].dropped) {
+        // the next attempt allocates what this render reported it needs
+        const size_t total = (size_t)s.h_tcounters[g].total_entries;
+        overflow += total;
+        s.entries_min = std::max(s.entries_min, total + total / 8 + 4096);
+      }
+      items += s.h_tcounters[g].total_entries;
     }
   }
   ctx->special += special;
@@ -665,7 +717,9 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
     CK(ctx, cudaStreamSynchronize(ctx->stream), "render");
     rc = check_counters(ctx, s, groups.size());
     if (rc == UGU_GPU_ERR_CAPACITY && attempt == 0) {
-      s.list_min *= 8;  // a list overflowed: grow it and render again
+      // a list overflowed: grow it (the tiled path knows the exact need) and
+      // render again
+      if (ctx->tuning.path == UGU_GPU_PATH_GLOBAL) s.list_min *= 8;
       s.keys_dirty = s.tiles_dirty = true;
       continue;
     }
@@ -722,7 +776,7 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->opt.oren_nayar_sigma = 0.3f;
   ctx->tuning.path = UGU_GPU_PATH_TILED;
   ctx->tuning.tile_log2 = 5;
-  ctx->tuning.bin_capacity = 8192;  // 8 faces per pixel of a 32x32 tile
+  ctx->tuning.entry_capacity = 0;
   ctx->tuning.small_bbox_max = 256;
   ctx->tuning.group_pixels = 4 << 20;
   ctx->tuning.ctas_per_sm = 0;
@@ -783,8 +837,19 @@ int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) 
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "materials is NULL");
 
   std::vector<float4> v4(V);
-  for (int64_t i = 0; i < V; ++i)
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = 0; i < V; ++i) {
     v4[i] = make_float4(m->vertices[3 * i], m->vertices[3 * i + 1], m->vertices[3 * i + 2], 0.f);
+    for (int k = 0; k < 3; ++k) {
+      const float x = m->vertices[3 * i + k];
+      if (x < lo[k]) lo[k] = x;  // NaN coordinates are skipped
+      if (x > hi[k]) hi[k] = x;
+    }
+  }
+  float centre[3];
+  for (int k = 0; k < 3; ++k)
+    centre[k] = (V > 0 && std::isfinite(lo[k]) && std::isfinite(hi[k])) ? 0.5f * (lo[k] + hi[k])
+                                                                         : 0.0f;
   auto pad3i = [&](const int32_t* a) {
     std::vector<int4> o(F);
     for (int64_t i = 0; i < F; ++i) o[i] = make_int4(a[3 * i], a[3 * i + 1], a[3 * i + 2], 0);
@@ -871,6 +936,7 @@ int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) 
   }
   CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &d, sizeof(DevMesh), cudaMemcpyHostToDevice),
      "cudaMemcpy(mesh table)");
+  for (int k = 0; k < 3; ++k) s.centre[k] = centre[k];
   s.present = true;
   return UGU_GPU_OK;
 }
@@ -917,6 +983,7 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plan views");
   }
+  if (!rc && ctx->tuning.path != UGU_GPU_PATH_GLOBAL) rc = size_tiled(ctx, s, plan->groups);
   if (!rc) {
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaStreamBeginCapture");
@@ -988,17 +1055,19 @@ int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
   const bool tiled = t->path == UGU_GPU_PATH_TILED;
   if ((t->path != UGU_GPU_PATH_TILED && t->path != UGU_GPU_PATH_GLOBAL) ||
       (tiled && (t->tile_log2 < 4 || t->tile_log2 > 5)) ||
-      (!tiled && (t->tile_log2 < 3 || t->tile_log2 > 6)) || t->bin_capacity < 1 ||
+      (!tiled && (t->tile_log2 < 3 || t->tile_log2 > 6)) || t->entry_capacity < 0 ||
       t->small_bbox_max < 0 || t->group_pixels < 1 || t->ctas_per_sm < 0)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "tuning out of range");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-  if (t->tile_log2 != ctx->tuning.tile_log2 || t->bin_capacity != ctx->tuning.bin_capacity) {
-    // bins are laid out per tile size and capacity: start them afresh
-    cudaFree(ctx->scratch.tile_count);
-    cudaFree(ctx->scratch.bins);
-    ctx->scratch.tile_count = nullptr;
-    ctx->scratch.bins = nullptr;
-    ctx->scratch.tiles_cap = ctx->scratch.bins_cap = 0;
+  if (t->tile_log2 != ctx->tuning.tile_log2 || t->entry_capacity != ctx->tuning.entry_capacity) {
+    // tile arrays are laid out per tile size: start them and the entries afresh
+    Scratch& s = ctx->scratch;
+    cudaFree(s.tile_count);
+    cudaFree(s.entries);
+    s.tile_count = nullptr;
+    s.entries = nullptr;
+    s.tiles_cap = s.entries_cap = 0;
+    s.entries_min = (size_t)t->entry_capacity;
   }
   ctx->tuning = *t;
   return UGU_GPU_OK;
@@ -1016,18 +1085,17 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad autotune arguments");
   cudaSetDevice(ctx->device);
   const ugu_gpu_tuning start = ctx->tuning;
-  // Candidates: the tiled path at both tile sizes with two bin capacities,
-  // and the global path at its default grouping.
+  // Candidates: the tiled path at both tile sizes and the global path at
+  // its default grouping.
   std::vector<ugu_gpu_tuning> cands;
-  for (int tl : {4, 5})
-    for (int per_px : {4, 8}) {
-      ugu_gpu_tuning t = start;
-      t.path = UGU_GPU_PATH_TILED;
-      t.tile_log2 = tl;
-      t.bin_capacity = per_px << (2 * tl);
-      t.ctas_per_sm = 0;
-      cands.push_back(t);
-    }
+  for (int tl : {4, 5}) {
+    ugu_gpu_tuning t = start;
+    t.path = UGU_GPU_PATH_TILED;
+    t.tile_log2 = tl;
+    t.entry_capacity = 0;
+    t.ctas_per_sm = 0;
+    cands.push_back(t);
+  }
   {
     ugu_gpu_tuning t = start;
     t.path = UGU_GPU_PATH_GLOBAL;

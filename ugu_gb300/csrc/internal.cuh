@@ -44,9 +44,9 @@ struct DevView {
   int32_t mesh;
   int32_t tiles_x;     // tiled path: tiles per row
   int64_t key_offset;  // global path: first z-buffer key of this view within its group
-  int64_t batch_begin; // tiled path: first 32-face batch of this view
+  int64_t proj_offset; // tiled path: first projected vertex of this view
   int32_t tile_base;   // tiled path: first global tile of this view
-  int32_t pad_;
+  float split_z;       // tiled path: faces wholly deeper than this are drawn last
   uint8_t* color;
   float* depth;
   float* normal;
@@ -98,13 +98,17 @@ struct RenderParams {
 
 // Counters of one tiled render (memset before every launch).
 struct TileCounters {
-  unsigned int next_tile;       // work-queue head of k_tile
-  unsigned int overflow_count;  // entries appended to the overflow list
-  unsigned long long special;   // covered samples with unorderable depth
-  unsigned long long dropped;   // overflow entries beyond the list's capacity
-  unsigned long long pad;
+  unsigned int next_tile;             // work-queue head of k_tile
+  unsigned int pad0;
+  unsigned long long special;         // covered samples with unorderable depth
+  unsigned long long dropped;         // entries beyond the entry buffer (0: none)
+  unsigned long long total_entries;   // (face, tile) entries of this render
 };
 
+// Tiled-path buffers.  Per global tile t, k_fill writes the entries of the
+// faces drawn first to [tile_off[t], tile_lo[t]) and those drawn last to
+// [tile_lo[t], tile_off[t + 1]).  An entry is (face id, bit pattern of a
+// lower bound of every depth the face can produce).
 struct TileParams {
   const DevMesh* meshes;
   const DevView* views;
@@ -113,12 +117,14 @@ struct TileParams {
   int32_t backface_culling;
   int32_t tile_log2;
   int32_t total_tiles;
-  int32_t bin_cap;
-  int64_t total_batches;
-  int32_t* tile_count;  // faces binned per global tile (k_tile resets it to 0)
-  int32_t* bins;        // total_tiles x bin_cap face ids
-  int2* overflow;       // (global tile, face) beyond bin_cap
-  int32_t overflow_cap;
+  int32_t max_vertices;
+  int64_t entry_cap;
+  float4* proj;         // projected vertices (x, y, camera z, 0) of every view
+  int32_t* tile_count;  // entries per tile (k_count adds; k_scan reads and zeroes)
+  int32_t* tile_off;    // total_tiles + 1 offsets into entries
+  int32_t* tile_lo;     // first-drawn cursor / boundary per tile
+  int32_t* tile_hi;     // last-drawn cursor per tile
+  int2* entries;
   TileCounters* counters;
 };
 
@@ -137,11 +143,14 @@ struct BackwardParams {
 // Host-side launcher (backward.cu).
 void launch_backward(const BackwardParams& p, int64_t max_pixels, cudaStream_t s);
 
-// Host-side launchers (tile.cu).
+// Host-side launchers (tile.cu).  launch_bin enqueues projection, counting,
+// the offset scan and the fill; launch_tile the per-tile raster + resolve.
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
+void launch_size(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
 int tile_kernel_blocks_per_sm();
 int bin_kernel_blocks_per_sm();
+constexpr int kBinKernels = 4;
 
 // Host-side launchers (raster.cu).
 void launch_raster(const RenderParams& p, int max_faces, int num_sms, cudaStream_t s);

@@ -1,24 +1,30 @@
 // tile.cu -- the tiled forward path: bin faces to (view, tile) lists, then one
 // persistent kernel that rasterises and resolves each tile in shared memory.
 //
-//   k_bin   one pass over every (view, face): Loop A + the per-face culls of
-//           Loop B (rasterizer.cc:131-193) and, for each surviving face, an
-//           append of its id to the list of every screen tile its bbox
-//           touches (atomic slot per tile; past bin_cap to an overflow list).
-//   k_tile  persistent blocks pull (view, tile) items from a work queue.
-//           For one tile: set the listed faces up in shared memory, split
-//           each warp's 32 faces into (face, pixel) pairs with a warp prefix
-//           scan of their bbox-in-tile pixel counts, run Loop B's pixel test
-//           on every pair into a shared-memory z-buffer of 64-bit
-//           (depth bits << 32 | face id << 1 | back-face bit) keys with
-//           atomicMin, then run Loop C (rasterizer.cc:244-301) for the
-//           tile's pixels and write the outputs.
+//   k_proj   Loop A (rasterizer.cc:131-136): every vertex of every view through
+//            PinholeCamera::Project once, into a table of float4 (x, y, z).
+//   k_count  per (view, face): the per-face culls of Loop B
+//            (rasterizer.cc:163-193) from the table, and the number of screen
+//            tiles the face's bbox touches, summed per tile (a block first
+//            aggregates its faces' tiles in shared memory).
+//   k_scan   exclusive scan of the per-tile counts into entry offsets, so the
+//            entry buffer holds exactly the render's (face, tile) pairs.
+//   k_fill   the same pass again, writing every (face, tile) entry into its
+//            tile's range: faces drawn first from the front, faces drawn last
+//            from the back.
+//   k_tile   persistent blocks pull (view, tile) items from a work queue.
+//            For one tile: set the listed faces up in shared memory, split
+//            each warp's 32 faces into (face, pixel) pairs with a warp prefix
+//            scan of their bbox-in-tile pixel counts, run Loop B's pixel test
+//            on every pair into a shared-memory z-buffer of 64-bit
+//            (depth bits << 32 | face id << 1 | back-face bit) keys with
+//            atomicMin, then run Loop C (rasterizer.cc:244-301) for the
+//            tile's pixels and write the outputs.
 //
-// Faces whose normal points away from the ray to their centroid (k_bin
-// marks them in bit 31 of the bin entry) are drawn after all the others and
-// skipped when a proven lower bound of their depth lies behind the deepest
-// key of a fully covered tile: such a face can never win the z-test there,
-// so the result is unchanged.
+// A face whose depth lower bound lies behind the view's split depth (the
+// camera depth of the mesh's bounding-box centre) is drawn last, and skipped
+// when that bound lies behind the deepest key of a fully covered tile: such
+// a face can never win the z-test there, so the result is unchanged.
 #include <cuda_runtime.h>
 
 #include "internal.cuh"
@@ -29,11 +35,15 @@ namespace ugu_gpu {
 namespace {
 
 constexpr int kBinThreads = 256;
+constexpr int kScanThreads = 1024;
 constexpr int kTileThreads = 256;
 constexpr int kWarps = kTileThreads / 32;
 constexpr int kChunk = 256;      // faces set up in shared memory at a time
 constexpr int kHash = 512;       // fid -> chunk slot table (power of two)
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
+constexpr int kAgg = 128;        // distinct tiles a binning block aggregates
+constexpr int kAggPerFace = 4;   // faces touching more tiles append directly
+constexpr int kAggProbes = 8;
 constexpr float kU64 = 3.814697265625e-06f;  // 2^-18 = 64 ulp(1)
 
 __device__ __forceinline__ int find_view_by_tile(const TileParams& p, int t) {
@@ -45,89 +55,199 @@ __device__ __forceinline__ int find_view_by_tile(const TileParams& p, int t) {
   return lo;
 }
 
-__device__ __forceinline__ bool setup_face_g(const DevMesh& m, const Cam& c, int f,
-                                             FaceSetup& s) {
-  int4 vi = __ldg(&m.vidx[f]);
-  float4 a = __ldg(&m.vertices[vi.x]);
-  float4 b = __ldg(&m.vertices[vi.y]);
-  float4 d = __ldg(&m.vertices[vi.z]);
-  return face_setup(c, project(c, a.x, a.y, a.z), project(c, b.x, b.y, b.z),
-                    project(c, d.x, d.y, d.z), s);
+// Loop B's per-face setup (rasterizer.cc:163-193) from projected vertices.
+__device__ __forceinline__ bool setup_proj(const float4* proj, const int4* vidx, int f,
+                                           const Cam& c, FaceSetup& s) {
+  const int4 vi = __ldg(&vidx[f]);
+  const float4 a = __ldg(&proj[vi.x]);
+  const float4 b = __ldg(&proj[vi.y]);
+  const float4 d = __ldg(&proj[vi.z]);
+  return face_setup(c, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
+                    make_float3(d.x, d.y, d.z), s);
 }
 
-// One block per (256 faces, view): the view's camera and mesh descriptor are
-// staged in shared memory once per block.
-__global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
-  __shared__ DevView sv;
-  __shared__ DevMesh sm;
-  {
-    const int* src = reinterpret_cast<const int*>(&p.views[blockIdx.y]);
-    int* dst = reinterpret_cast<int*>(&sv);
-    for (int i = threadIdx.x; i < (int)(sizeof(DevView) / 4); i += blockDim.x) dst[i] = src[i];
-    __syncthreads();
-    const int* msrc = reinterpret_cast<const int*>(&p.meshes[sv.mesh]);
-    int* mdst = reinterpret_cast<int*>(&sm);
-    for (int i = threadIdx.x; i < (int)(sizeof(DevMesh) / 4); i += blockDim.x) mdst[i] = msrc[i];
-    __syncthreads();
+// A lower bound of the depth Loop B computes for the face at any covered
+// pixel: the three edge functions carry rounding errors of at most
+// delta = 2^-18 * bboxW * bboxH, so the interpolation weights' sum exceeds
+// the area by at most delta and the depth is at least
+// zmin * |A| / (|A| + delta), less a margin for this expression's own
+// roundings.  -1 when no bound is proven.
+__device__ __forceinline__ float depth_lower_bound(const FaceSetup& s) {
+  const float zmin = fminf(fminf(s.v0.z, s.v1.z), s.v2.z);
+  const float BW = fmaxf(fmaxf(s.v0.x, s.v1.x), s.v2.x) -
+                   fminf(fminf(s.v0.x, s.v1.x), s.v2.x) + 1.0f;
+  const float BH = fmaxf(fmaxf(s.v0.y, s.v1.y), s.v2.y) -
+                   fminf(fminf(s.v0.y, s.v1.y), s.v2.y) + 1.0f;
+  const float delta = kU64 * BW * BH;
+  const float aa = fabsf(s.area);
+  return (aa > 2.0f * delta && zmin > 0.0f) ? zmin * (aa / (aa + delta)) * 0.99998474f : -1.0f;
+}
+
+template <typename T>
+__device__ __forceinline__ void copy_words(T& dst, const T& src) {
+  const int* a = reinterpret_cast<const int*>(&src);
+  int* b = reinterpret_cast<int*>(&dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += blockDim.x) b[i] = a[i];
+}
+
+// Loop A for every vertex of one view (blockIdx.y).
+__global__ void __launch_bounds__(kBinThreads) k_proj(TileParams p) {
+  __shared__ Cam sc;
+  __shared__ int mesh, nv;
+  __shared__ long long off;
+  copy_words(sc, p.views[blockIdx.y].cam);
+  if (threadIdx.x == 0) {
+    mesh = p.views[blockIdx.y].mesh;
+    off = p.views[blockIdx.y].proj_offset;
+    nv = p.meshes[mesh].num_vertices;
   }
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  const Cam& c = sv.cam;
-  FaceSetup s;
-  bool live = false;
-  uint32_t entry = 0;
-  if (f < sm.num_faces) {
-    const int4 vi = __ldg(&sm.vidx[f]);
-    const float4 a = __ldg(&sm.vertices[vi.x]);
-    const float4 b = __ldg(&sm.vertices[vi.y]);
-    const float4 d = __ldg(&sm.vertices[vi.z]);
-    live = face_setup(c, project(c, a.x, a.y, a.z), project(c, b.x, b.y, b.z),
-                      project(c, d.x, d.y, d.z), s) &&
-           s.x1 >= s.x0 && s.y1 >= s.y0;
-    if (live) {
-      // Draw-order class only (never changes a result): faces whose normal
-      // points away from the ray to their centroid are drawn after the rest.
-      const float4 fn = __ldg(&sm.fnormals[f]);
-      const float ox = -(c.R[0] * c.t[0] + c.R[3] * c.t[1] + c.R[6] * c.t[2]);
-      const float oy = -(c.R[1] * c.t[0] + c.R[4] * c.t[1] + c.R[7] * c.t[2]);
-      const float oz = -(c.R[2] * c.t[0] + c.R[5] * c.t[1] + c.R[8] * c.t[2]);
-      const float gx = (a.x + b.x + d.x) * (1.0f / 3.0f) - ox;
-      const float gy = (a.y + b.y + d.y) * (1.0f / 3.0f) - oy;
-      const float gz = (a.z + b.z + d.z) * (1.0f / 3.0f) - oz;
-      const bool back = fn.x * gx + fn.y * gy + fn.z * gz > 0.0f;
-      entry = (uint32_t)f | (back ? 0x80000000u : 0u);
+  __syncthreads();
+  const int i = blockIdx.x * kBinThreads + threadIdx.x;
+  if (i >= nv) return;
+  const float4 a = __ldg(&p.meshes[mesh].vertices[i]);
+  const float3 q = project(sc, a.x, a.y, a.z);
+  p.proj[off + i] = make_float4(q.x, q.y, q.z, 0.0f);
+}
+
+struct BinSmem {
+  DevView view;
+  DevMesh mesh;
+  int tile[kAgg];
+  int cnt[kAgg][2];
+  int base[kAgg][2];
+};
+
+__device__ __forceinline__ int agg_slot(BinSmem& sb, int t) {
+  unsigned h = ((unsigned)t * 2654435761u) >> 25;  // 7 bits
+  for (int probe = 0; probe < kAggProbes; ++probe) {
+    const int cur = atomicCAS(&sb.tile[h], -1, t);
+    if (cur == -1 || cur == t) return (int)h;
+    h = (h + 1) & (kAgg - 1);
+  }
+  return -1;
+}
+
+// One block per (256 faces, view).  kFill = false: count the entries of
+// every tile; kFill = true: write them (after k_scan placed the cursors).
+template <bool kFill>
+__global__ void __launch_bounds__(kBinThreads) k_binpass(TileParams p) {
+  __shared__ BinSmem sb;
+  if (kFill && p.counters->dropped) return;  // entry buffer too small: the host retries
+  copy_words(sb.view, p.views[blockIdx.y]);
+  for (int i = threadIdx.x; i < kAgg; i += kBinThreads) {
+    sb.tile[i] = -1;
+    sb.cnt[i][0] = sb.cnt[i][1] = 0;
+  }
+  __syncthreads();
+  copy_words(sb.mesh, p.meshes[sb.view.mesh]);
+  __syncthreads();
+  const Cam& c = sb.view.cam;
+  const int f = blockIdx.x * kBinThreads + threadIdx.x;
+  int n = 0, tx0 = 0, ty0 = 0, ntx = 1, cls = 0;
+  float zlb = -1.0f;
+  if (f < sb.mesh.num_faces) {
+    FaceSetup s;
+    if (setup_proj(p.proj + sb.view.proj_offset, sb.mesh.vidx, f, c, s) && s.x1 >= s.x0 &&
+        s.y1 >= s.y0) {
+      const int ts = p.tile_log2;
+      tx0 = s.x0 >> ts;
+      ty0 = s.y0 >> ts;
+      ntx = (s.x1 >> ts) - tx0 + 1;
+      n = ntx * ((s.y1 >> ts) - ty0 + 1);
+      zlb = depth_lower_bound(s);
+      cls = zlb > sb.view.split_z ? 1 : 0;
     }
   }
-  const int ts = p.tile_log2;
-  int tx0 = 0, ty0 = 0, ntx = 0, n = 0;
-  if (live) {
-    tx0 = s.x0 >> ts;
-    ty0 = s.y0 >> ts;
-    ntx = (s.x1 >> ts) - tx0 + 1;
-    n = ntx * ((s.y1 >> ts) - ty0 + 1);
-  }
-  // Consecutive faces of a mesh are usually close on screen: the lanes that
-  // append to the same tile take their slots with one atomicAdd per tile.
-  for (int k = 0; k < n; ++k) {
-    const int t = sv.tile_base + (ty0 + k / ntx) * sv.tiles_x + tx0 + k % ntx;
-    const unsigned active = __activemask();
-    const unsigned peers = __match_any_sync(active, t);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(&p.tile_count[t], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    const int slot = base + __popc(peers & ((1u << lane) - 1));
-    {
-      if (slot < p.bin_cap) {
-        p.bins[(int64_t)t * p.bin_cap + slot] = (int32_t)entry;
-      } else {
-        const unsigned o = atomicAdd(&p.counters->overflow_count, 1u);
-        if (o < (unsigned)p.overflow_cap)
-          p.overflow[o] = make_int2(t, f);
-        else
-          atomicAdd(&p.counters->dropped, 1ull);
-      }
+  const int tbase = sb.view.tile_base, tiles_x = sb.view.tiles_x;
+  auto tile_of = [&](int k) { return tbase + (ty0 + k / ntx) * tiles_x + tx0 + k % ntx; };
+  const bool agg = n <= kAggPerFace;
+  int slot[kAggPerFace], rank[kAggPerFace];
+#pragma unroll
+  for (int k = 0; k < kAggPerFace; ++k) {
+    slot[k] = -1;
+    rank[k] = 0;
+    if (agg && k < n) {
+      slot[k] = agg_slot(sb, tile_of(k));
+      if (slot[k] >= 0)
+        rank[k] = atomicAdd(&sb.cnt[slot[k]][cls], 1);
+      else if (!kFill)
+        atomicAdd(&p.tile_count[tile_of(k)], 1);
     }
+  }
+  if (!kFill && !agg)
+    for (int k = 0; k < n; ++k) atomicAdd(&p.tile_count[tile_of(k)], 1);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kAgg; i += kBinThreads) {
+    const int t = sb.tile[i];
+    if (t < 0) continue;
+    const int c0 = sb.cnt[i][0], c1 = sb.cnt[i][1];
+    if (!kFill) {
+      atomicAdd(&p.tile_count[t], c0 + c1);
+    } else {
+      if (c0) sb.base[i][0] = atomicAdd(&p.tile_lo[t], c0);
+      if (c1) sb.base[i][1] = atomicSub(&p.tile_hi[t], c1) - c1;
+    }
+  }
+  if (!kFill) return;
+  __syncthreads();
+  const int2 e = make_int2(f, __float_as_int(zlb));
+  auto direct = [&](int t) {
+    return cls ? atomicSub(&p.tile_hi[t], 1) - 1 : atomicAdd(&p.tile_lo[t], 1);
+  };
+  if (agg) {
+#pragma unroll
+    for (int k = 0; k < kAggPerFace; ++k) {
+      if (k >= n) continue;
+      const int pos = slot[k] >= 0 ? sb.base[slot[k]][cls] + rank[k] : direct(tile_of(k));
+      p.entries[pos] = e;
+    }
+  } else {
+    for (int k = 0; k < n; ++k) p.entries[direct(tile_of(k))] = e;
+  }
+}
+
+// Exclusive scan of the per-tile counts (one block); zeroes the counts for
+// the next render and flags a render whose entries exceed the buffer.
+__global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
+  __shared__ long long warp_sum[kScanThreads / 32];
+  const int T = p.total_tiles;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int per = (T + kScanThreads - 1) / kScanThreads;
+  const int b = min(T, tid * per), e = min(T, b + per);
+  long long own = 0;
+  for (int t = b; t < e; ++t) own += p.tile_count[t];
+  long long x = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = warp_sum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_sum[lane] = w;
+  }
+  __syncthreads();
+  const long long total = warp_sum[kScanThreads / 32 - 1];
+  long long run = x - own + (warp ? warp_sum[warp - 1] : 0);
+  for (int t = b; t < e; ++t) {
+    const int cnt = p.tile_count[t];
+    p.tile_off[t] = (int)run;
+    p.tile_lo[t] = (int)run;
+    run += cnt;
+    p.tile_hi[t] = (int)run;
+    p.tile_count[t] = 0;
+  }
+  if (tid == 0) {
+    p.tile_off[T] = (int)total;
+    p.counters->total_entries = (unsigned long long)total;
+    if (total > p.entry_cap) p.counters->dropped = (unsigned long long)total;
   }
 }
 
@@ -152,7 +272,6 @@ struct TileSmem {
   DevView view;
   DevMesh mesh;
   int item;
-  int any_back;
   unsigned zmax_bits;
 };
 
@@ -258,6 +377,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
   const int tid = threadIdx.x;
   const int tlog = p.tile_log2;
   const int T = 1 << tlog;
+  if (p.counters->dropped) return;  // entries were not written: the host retries
   int cur_view = -1;
   for (;;) {
     if (tid == 0) sm.item = (int)atomicAdd(&p.counters->next_tile, 1u);
@@ -266,13 +386,9 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
     if (item >= p.total_tiles) break;
     const int v = find_view_by_tile(p, item);
     if (v != cur_view) {
-      const int* src = reinterpret_cast<const int*>(&p.views[v]);
-      int* dst = reinterpret_cast<int*>(&sm.view);
-      for (int i = tid; i < (int)(sizeof(DevView) / 4); i += kTileThreads) dst[i] = src[i];
+      copy_words(sm.view, p.views[v]);
       __syncthreads();
-      const int* msrc = reinterpret_cast<const int*>(&p.meshes[sm.view.mesh]);
-      int* mdst = reinterpret_cast<int*>(&sm.mesh);
-      for (int i = tid; i < (int)(sizeof(DevMesh) / 4); i += kTileThreads) mdst[i] = msrc[i];
+      copy_words(sm.mesh, p.meshes[sm.view.mesh]);
       cur_view = v;
     }
     const Cam& c = sm.view.cam;
@@ -283,9 +399,9 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
     const int tw = min(T, c.width - tx0), th = min(T, c.height - ty0);
     for (int i = tid; i < T * T; i += kTileThreads) sm.keys[i] = kEmptyKey;
     for (int i = tid; i < kHash; i += kTileThreads) sm.reg[0].hkey[i] = sm.reg[1].hkey[i] = -1;
-    if (tid == 0) sm.any_back = 0;
-    const int n_total = p.tile_count[item];
-    const int n_bin = min(n_total, p.bin_cap);
+    // entries drawn first: [e0, e1); drawn last: [e1, e2)
+    const int e0 = p.tile_off[item], e1 = p.tile_lo[item], e2 = p.tile_off[item + 1];
+    const float4* proj = p.proj + sm.view.proj_offset;
     __syncthreads();
 
     // Per-view constants of the back-face surrogate's error bound.
@@ -298,7 +414,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
       Region& R = sm.reg[phase];
       float zmax = __int_as_float(0x7f800000);
       if (phase == 1) {
-        if (!sm.any_back) break;
+        if (e2 == e1) break;
         // deepest key of the tile (+inf while any pixel is still empty)
         if (tid == 0) sm.zmax_bits = 0u;
         __syncthreads();
@@ -315,34 +431,21 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
         __syncthreads();
         zmax = __uint_as_float(sm.zmax_bits);
       }
-      for (int cs = 0; cs < n_bin; cs += kChunk) {
-        const int m = min(kChunk, n_bin - cs);
-        if (cs > 0) {
+      const int eb = phase ? e1 : e0, ee = phase ? e2 : e1;
+      for (int cs = eb; cs < ee; cs += kChunk) {
+        const int m = min(kChunk, ee - cs);
+        if (cs > eb) {
           for (int i = tid; i < kHash; i += kTileThreads) R.hkey[i] = -1;
           __syncthreads();
         }
         for (int j = tid; j < m; j += kTileThreads) {
-          const uint32_t e = (uint32_t)p.bins[(int64_t)item * p.bin_cap + cs + j];
-          const int cls = (int)(e >> 31);
+          const int2 e = p.entries[cs + j];
+          const float zlb = __int_as_float(e.y);
           R.cnt[j] = 0;
-          if (cls != phase) {
-            if (cls) sm.any_back = 1;
-            continue;
-          }
-          const int f = (int)(e & 0x7fffffffu);
-          FaceSetup s;
-          setup_face_g(sm.mesh, c, f, s);  // succeeded in k_bin: same arithmetic
-          // lower bound of any depth the face can produce (see file comment)
-          const float zmin = fminf(fminf(s.v0.z, s.v1.z), s.v2.z);
-          const float BW = fmaxf(fmaxf(s.v0.x, s.v1.x), s.v2.x) -
-                           fminf(fminf(s.v0.x, s.v1.x), s.v2.x) + 1.0f;
-          const float BH = fmaxf(fmaxf(s.v0.y, s.v1.y), s.v2.y) -
-                           fminf(fminf(s.v0.y, s.v1.y), s.v2.y) + 1.0f;
-          const float delta = kU64 * BW * BH;
-          const float aa = fabsf(s.area);
-          float zlb = -1.0f;
-          if (aa > 2.0f * delta && zmin > 0.0f) zlb = zmin * (aa / (aa + delta)) * 0.99998474f;
           if (zlb > zmax) continue;  // behind every key of a covered tile: cannot win
+          const int f = e.x;
+          FaceSetup s;
+          setup_proj(proj, sm.mesh.vidx, f, c, s);  // succeeded in k_fill: same arithmetic
           const int bx0 = max(s.x0, tx0), bx1 = min(s.x1, tx0 + tw - 1);
           const int by0 = max(s.y0, ty0), by1 = min(s.y1, ty0 + th - 1);
           const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;
@@ -376,32 +479,6 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
         __syncthreads();
       }
     }
-    if (n_total > p.bin_cap) {
-      // Faces past the bin's capacity: one thread per overflow entry.
-      const unsigned no = min(p.counters->overflow_count, (unsigned)p.overflow_cap);
-      for (unsigned o = tid; o < no; o += kTileThreads) {
-        const int2 e = p.overflow[o];
-        if (e.x != item) continue;
-        FaceSetup s;
-        setup_face_g(sm.mesh, c, e.y, s);
-        const float4 fn = __ldg(&sm.mesh.fnormals[e.y]);
-        for (int y = max(s.y0, ty0); y <= min(s.y1, ty0 + th - 1); ++y)
-          for (int x = max(s.x0, tx0); x <= min(s.x1, tx0 + tw - 1); ++x) {
-            const float3 r = ray_w(c, x, y);
-            const bool bf = dot3(fn.x, fn.y, fn.z, r.x, r.y, r.z) > 0.0f;
-            Bary b = edges_at(s, x, y);
-            if (!covered(b, bf)) continue;
-            const float z = perspective(s, b);
-            if (!orderable_depth(z)) {
-              atomicAdd(&p.counters->special, 1ull);
-              continue;
-            }
-            atomicMin(&sm.keys[((y - ty0) << tlog) + (x - tx0)], make_key(z, e.y, bf));
-          }
-      }
-      __syncthreads();
-    }
-
     // Loop C for the tile's pixels.
     const DevView& V = sm.view;
     const int W = c.width;
@@ -437,7 +514,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
             s.v2 = make_float3(r1.x, r1.y, r2.z);
             s.area = r1.z;
           } else {
-            s = project_face(sm.mesh, c, fid);
+            setup_proj(proj, sm.mesh.vidx, fid, c, s);
           }
           shade_face_pixel(p.shade, sm.mesh, c, fid, s, x, y, sh);
         }
@@ -461,16 +538,24 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
         V.color_f32[3 * pix + 2] = sh.cf[2];
       }
     }
-    if (tid == 0) p.tile_count[item] = 0;  // leave the bins empty for the next launch
     __syncthreads();
   }
 }
 
 }  // namespace
 
+void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
+  k_proj<<<dim3((p.max_vertices + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads, 0,
+           s>>>(p);
+  k_binpass<false><<<dim3((max_faces + kBinThreads - 1) / kBinThreads, p.num_views),
+                     kBinThreads, 0, s>>>(p);
+  k_scan<<<1, kScanThreads, 0, s>>>(p);
+}
+
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {
-  dim3 grid((max_faces + kBinThreads - 1) / kBinThreads, p.num_views);
-  k_bin<<<grid, kBinThreads, 0, s>>>(p);
+  launch_size(p, max_faces, s);
+  k_binpass<true><<<dim3((max_faces + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads,
+                     0, s>>>(p);
 }
 
 void launch_tile(const TileParams& p, int grid, cudaStream_t s) {
@@ -492,7 +577,7 @@ int tile_kernel_blocks_per_sm() {
 int bin_kernel_blocks_per_sm() {
   static int blocks = 0;
   if (!blocks) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_bin, kBinThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_binpass<true>, kBinThreads, 0);
     if (blocks < 1) blocks = 1;
   }
   return blocks;
