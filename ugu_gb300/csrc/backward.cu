@@ -229,6 +229,10 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
     fid = sv.face_id[i];
     x = (int)(i % c.width);
     y = (int)(i / c.width);
+    if (fid < -1 || fid >= sm.num_faces) {  // not a forward's face id: reported, skipped
+      atomicAdd(p.bad_ids, 1ull);
+      fid = -1;
+    }
   }
   // a run of one face never continues across an image row
   const int key = fid > 0 ? fid * 2 + (y & 1) : -1;

@@ -64,6 +64,8 @@ struct Scratch {
   size_t entries_min = 0;  // capacity asked for by the last overflow
   float4* proj = nullptr;
   size_t proj_cap = 0;
+  int32_t* fid_scratch = nullptr;  // face ids of shaded views that do not output them
+  size_t fid_cap = 0;
   TileCounters* tcounters = nullptr;
   TileCounters* h_tcounters = nullptr;  // pinned
   size_t tcounters_cap = 0;
@@ -83,6 +85,8 @@ struct Group {
   int64_t faces;     // tiled path: faces summed over the group's views
   int64_t vertices;  // tiled path: vertices summed over the group's views
   int max_vertices;
+  int64_t shade_blocks;  // tiled path: blocks of the shading grid
+  int64_t fid_scratch;   // tiled path: pixels needing a scratch face id
 };
 
 }  // namespace
@@ -161,6 +165,7 @@ void free_scratch(Scratch& s) {
   cudaFree(s.tile_count);
   cudaFree(s.entries);
   cudaFree(s.proj);
+  cudaFree(s.fid_scratch);
   cudaFree(s.tcounters);
   cudaFreeHost(s.h_tcounters);
   cudaFree(s.d_targets);
@@ -279,14 +284,14 @@ std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* 
   const ugu_gpu_tuning& t = ctx->tuning;
   const int64_t limit = t.path == UGU_GPU_PATH_GLOBAL ? (int64_t)t.group_pixels : INT64_MAX;
   std::vector<Group> g;
-  Group cur{0, 0, 0, 0, 0, 0, 0, 0};
+  Group cur{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   int64_t acc = 0;
   for (int i = 0; i < n; ++i) {
     int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
     bool full = cur.count > 0 && (per_view || acc + px > limit);
     if (full) {
       g.push_back(cur);
-      cur = Group{i, 0, 0, 0, 0, 0, 0, 0};
+      cur = Group{i, 0, 0, 0, 0, 0, 0, 0, 0, 0};
       acc = 0;
     }
     const int F = ctx->meshes[views[i].mesh].dev.num_faces;
@@ -299,6 +304,9 @@ std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* 
     cur.tiles += tiles_of(views[i].camera, t.tile_log2);
     cur.faces += F;
     cur.vertices += V;
+    const ugu_gpu_images& im = views[i].images;
+    cur.shade_blocks += (px + kShadePixels - 1) / kShadePixels;
+    if ((im.color || im.normal || im.color_f32) && !im.face_id) cur.fid_scratch += px;
   }
   if (cur.count) g.push_back(cur);
   return g;
@@ -316,11 +324,19 @@ int64_t group_key_count(const std::vector<Group>& groups, const ugu_gpu_view* vi
 }
 
 int ensure_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups) {
-  size_t tiles = 0, verts = 0, faces = 0;
+  size_t tiles = 0, verts = 0, faces = 0, fids = 0;
   for (const Group& g : groups) {
     tiles = std::max(tiles, (size_t)g.tiles);
     verts = std::max(verts, (size_t)g.vertices);
     faces = std::max(faces, (size_t)g.faces);
+    fids = std::max(fids, (size_t)g.fid_scratch);
+  }
+  if (fids > s.fid_cap) {
+    cudaFree(s.fid_scratch);
+    s.fid_scratch = nullptr;
+    s.fid_cap = 0;
+    CK(ctx, cudaMalloc(&s.fid_scratch, fids * sizeof(int32_t)), "cudaMalloc(face id scratch)");
+    s.fid_cap = fids;
   }
   if (tiles > s.tiles_cap) {
     cudaFree(s.tile_count);
@@ -476,6 +492,7 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.tile_hi = p.tile_lo + s.tiles_cap;
   p.entries = s.entries;
   p.counters = s.tcounters + gi;
+  p.shade_blocks = (int32_t)gr.shade_blocks;
   return p;
 }
 
@@ -489,7 +506,8 @@ int enqueue_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& gr
        "cudaMemsetAsync(tile counters)");
     launch_bin(p, gr.max_faces, ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
-    nk += kBinKernels + 1;
+    launch_shade(p, ctx->stream);
+    nk += kBinKernels + 1 + (p.shade_blocks > 0 ? 1 : 0);
   }
   CK(ctx, cudaGetLastError(), "kernel launch");
   *kernels = nk;
@@ -547,7 +565,7 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
   size_t off = 0;
   const int tlog = ctx->tuning.tile_log2;
   for (const Group& gr : groups) {
-    int64_t key_off = 0, tile_base = 0, proj_off = 0;
+    int64_t key_off = 0, tile_base = 0, proj_off = 0, shade_block = 0, fid_off = 0;
     for (int i = gr.first; i < gr.first + gr.count; ++i) {
       const ugu_gpu_view& v = views[i];
       DevView& d = s.h_views[i];
@@ -585,6 +603,14 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
         if (v.images.mask) d.mask = take(px);
         if (v.images.face_id) d.face_id = reinterpret_cast<int32_t*>(take(4 * px));
         if (v.images.color_f32) d.color_f32 = reinterpret_cast<float*>(take(12 * px));
+      }
+      // tiled path: k_shade reads the face ids k_tile wrote
+      d.shade_block = (int32_t)shade_block;
+      shade_block += (px + kShadePixels - 1) / kShadePixels;
+      if ((d.color || d.normal || d.color_f32) && !d.face_id &&
+          ctx->tuning.path != UGU_GPU_PATH_GLOBAL) {
+        d.face_id = s.fid_scratch + fid_off;
+        fid_off += px;
       }
     }
   }
@@ -1169,7 +1195,7 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     max_px = std::max(max_px, (int64_t)v.camera.width * v.camera.height);
   }
   Scratch& s = ctx->scratch;
-  int rc = ensure_scratch(ctx, s, 0, (size_t)n, 0, 0);
+  int rc = ensure_scratch(ctx, s, 0, (size_t)n, 1, 0);
   if (rc) return rc;
   if ((size_t)n > s.targets_cap) {
     cudaFree(s.d_targets);
@@ -1207,11 +1233,21 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   p.grad_vertex_colors = grad_vertex_colors;
   p.grad_vertices = grad_vertices;
   p.loss = loss_out;
+  p.bad_ids = &s.counters[0].pad;
+  CK(ctx, cudaMemsetAsync(s.counters, 0, sizeof(DevCounters), ctx->stream),
+     "cudaMemsetAsync(counters)");
   launch_backward(p, max_px, ctx->stream);
   CK(ctx, cudaGetLastError(), "backward launch");
   ctx->launches += 1;
+  CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, sizeof(DevCounters), cudaMemcpyDeviceToHost,
+                          ctx->stream),
+     "cudaMemcpyAsync(counters)");
   if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
   CK(ctx, cudaStreamSynchronize(ctx->stream), "backward");
+  if (s.h_counters[0].pad)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                     "%llu face_id pixels hold ids outside the mesh (not a forward's output)",
+                     (unsigned long long)s.h_counters[0].pad);
   return UGU_GPU_OK;
 }
 

@@ -47,6 +47,8 @@ struct DevView {
   int64_t proj_offset; // tiled path: first projected vertex of this view
   int32_t tile_base;   // tiled path: first global tile of this view
   float split_z;       // tiled path: faces wholly deeper than this are drawn last
+  int32_t shade_block; // tiled path: first block of this view in the shading grid
+  int32_t pad_;
   uint8_t* color;
   float* depth;
   float* normal;
@@ -126,6 +128,7 @@ struct TileParams {
   int32_t* tile_hi;     // last-drawn cursor per tile
   int2* entries;
   TileCounters* counters;
+  int32_t shade_blocks;  // blocks of the shading grid (all views)
 };
 
 struct BackwardParams {
@@ -138,6 +141,7 @@ struct BackwardParams {
   float* grad_vertex_colors;    // V*3 (or NULL)
   float* grad_vertices;         // V*3 (or NULL)
   float* loss;                  // one per view (or NULL)
+  unsigned long long* bad_ids;  // counts face ids outside [-1, num_faces)
 };
 
 // Host-side launcher (backward.cu).
@@ -148,6 +152,8 @@ void launch_backward(const BackwardParams& p, int64_t max_pixels, cudaStream_t s
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
+void launch_shade(const TileParams& p, cudaStream_t s);
+constexpr int kShadePixels = 1024;  // pixels per shading block
 int tile_kernel_blocks_per_sm();
 int bin_kernel_blocks_per_sm();
 constexpr int kBinKernels = 4;

@@ -39,7 +39,6 @@ constexpr int kScanThreads = 1024;
 constexpr int kTileThreads = 256;
 constexpr int kWarps = kTileThreads / 32;
 constexpr int kChunk = 256;      // faces set up in shared memory at a time
-constexpr int kHash = 512;       // fid -> chunk slot table (power of two)
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kAgg = 128;        // distinct tiles a binning block aggregates
 constexpr int kAggPerFace = 4;   // faces touching more tiles append directly
@@ -251,23 +250,24 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
   }
 }
 
-// Faces of one tile set up in shared memory: one region for the faces drawn
-// first, one for the faces drawn second (so both stay available to the
-// resolve when a tile's list fits one window).
+// Faces of one tile set up in shared memory, one window of kChunk entries
+// at a time.
 struct Region {
   float4 r0[kChunk];  // v0.x v0.y v1.x v1.y
   float4 r1[kChunk];  // v2.x v2.y area fid-bits
-  float4 r2[kChunk];  // v0.z v1.z v2.z depth lower bound
-  float4 r3[kChunk];  // back-face sign: sa sb sc tolerance
-  int4 r4[kChunk];    // bbox-in-tile x0 y0 width magic
-  int cnt[kChunk];    // pixels of bbox-in-tile, 0 when skipped
-  int hkey[kHash];
-  short hval[kHash];
+  float4 r2[kChunk];  // v0.z v1.z v2.z -
+  float4 r3[kChunk];  // back-face sign surrogate: sa sb sc tolerance
+  float4 r5[kChunk];  // depth pre-test: z1 z2, z0 z2, z0 z1, |area| z0 z1 z2 (1 - 2^-16)
+  int4 r4[kChunk];    // bbox-in-tile x0 y0 width, ceil(2^20 / width)
+  int cnt[kChunk];    // bbox-in-tile pixels, 0 when the face is skipped
 };
+
+constexpr int kQueue = 64;  // covered candidates a warp holds before its depth pass
 
 struct TileSmem {
   unsigned long long keys[kMaxTile * kMaxTile];
-  Region reg[2];
+  Region reg;
+  float4 queue[kWarps][kQueue];  // (w0, w1, w2, face slot | x << 8 | y << 13 | bf << 18)
   int pre[kWarps][33];
   DevView view;
   DevMesh mesh;
@@ -275,100 +275,135 @@ struct TileSmem {
   unsigned zmax_bits;
 };
 
-__device__ __forceinline__ unsigned hash_fid(int f) { return ((unsigned)f * 2654435761u) >> 23; }
+// The reference's back-face test fn . ray_w(x, y) > 0 (rasterizer.cc:199),
+// for the rare pixels the surrogate cannot decide; kept out of line so the
+// pixel loop keeps its registers.
+__device__ __noinline__ bool backface_exact(const DevMesh& m, const Cam& c, int fid, int x,
+                                            int y) {
+  const float4 fn = __ldg(&m.fnormals[fid]);
+  const float3 r = ray_w(c, x, y);
+  return dot3(fn.x, fn.y, fn.z, r.x, r.y, r.z) > 0.0f;
+}
 
-// Loop B's per-pixel body (rasterizer.cc:196-237) for region face j at
-// (x, y), into the tile's shared z-buffer.
-__device__ __forceinline__ void test_pair(TileSmem& sm, const Region& R, const TileParams& p,
-                                          const Cam& c, int j, int x, int y, int tx0, int ty0,
-                                          int tlog) {
-  const float4 r0 = R.r0[j];
+// The z-test of one covered candidate (rasterizer.cc:208-237): Loop B's
+// depth, then an atomicMin of its key into the tile's shared z-buffer.
+__device__ __forceinline__ void depth_test(TileSmem& sm, const Region& R, const TileParams& p,
+                                           const float4 q, int tlog) {
+  const int packed = __float_as_int(q.w);
+  const int j = packed & 255, lx = (packed >> 8) & 31, ly = (packed >> 13) & 31;
+  const bool bf = (packed >> 18) & 1;
+  unsigned long long* kp = &sm.keys[(ly << tlog) + lx];
+  const unsigned long long cur = *(volatile unsigned long long*)kp;
   const float4 r1 = R.r1[j];
-  const float4 r3 = R.r3[j];
-  const int fid = __float_as_int(r1.w);
-  // sign of face_normal . ray_w: the affine surrogate decides unless it is
-  // within its error bound of zero; then the reference's ray is computed.
-  const float sv = fmaf(r3.x, (float)x, fmaf(r3.y, (float)y, r3.z));
-  bool bf;
-  if (sv > r3.w) {
-    bf = true;
-  } else if (sv < -r3.w) {
-    bf = false;
-  } else {
-    const float4 fn = __ldg(&sm.mesh.fnormals[fid]);
-    const float3 r = ray_w(c, x, y);
-    bf = dot3(fn.x, fn.y, fn.z, r.x, r.y, r.z) > 0.0f;
-  }
-  FaceSetup s;
-  s.v0 = make_float3(r0.x, r0.y, 0.0f);
-  s.v1 = make_float3(r0.z, r0.w, 0.0f);
-  s.v2 = make_float3(r1.x, r1.y, 0.0f);
-  Bary b = edges_at(s, x, y);
-  if (!covered(b, bf)) return;
+  // Depth pre-test: z' = |A| z0 z1 z2 / |w0 z1 z2 + w1 z0 z2 + w2 z0 z1| is
+  // the depth Loop B computes up to 14 rounding errors of its own and of
+  // this expression (all terms share one sign on a covered pixel), so
+  // z' (1 - 2^-16) > current depth proves the candidate loses.
+  const float4 r5 = R.r5[j];
+  const float s2 = fmaf(q.x, r5.x, fmaf(q.y, r5.y, q.z * r5.z));
+  if (r5.w > key_depth(cur) * fabsf(s2) && (s2 > 0.0f) == (r1.z > 0.0f)) return;
   const float4 r2 = R.r2[j];
+  FaceSetup s;
   s.v0.z = r2.x;
   s.v1.z = r2.y;
   s.v2.z = r2.z;
   s.area = r1.z;
+  Bary b;
+  b.w0 = q.x;
+  b.w1 = q.y;
+  b.w2 = q.z;
   const float z = perspective(s, b);
   if (!orderable_depth(z)) {
     atomicAdd(&p.counters->special, 1ull);
     return;
   }
-  const unsigned long long key = make_key(z, fid, bf);
-  unsigned long long* kp = &sm.keys[((y - ty0) << tlog) + (x - tx0)];
+  const unsigned long long key = make_key(z, __float_as_int(r1.w), bf);
   if (key < *(volatile unsigned long long*)kp) atomicMin(kp, key);
 }
 
-// Warp-cooperative pass over a region's faces: every lane first tests its
-// own face's first pixel; the remaining (face, pixel) pairs of the warp's 32
-// faces are spread over the lanes with a prefix scan of their counts.
+// Loop B (rasterizer.cc:196-237) over a window's faces.  Each warp takes 32
+// faces, flattens their (face, pixel) pairs with a prefix scan and tests one
+// pair per lane: back-face sign, edge functions, coverage.  Covered pairs go
+// to the warp's queue; every 32 of them take the depth test together, one
+// per lane.
 __device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const TileParams& p,
                                             const Cam& c, int m, int tx0, int ty0, int tlog) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  float4* Q = sm.queue[warp];
+  int* pre = sm.pre[warp];
+  int qn = 0;
   for (int base = warp * 32; base < m; base += kTileThreads) {
     const int j = base + lane;
     const int cnt = j < m ? R.cnt[j] : 0;
-    if (cnt > 0) {
-      const int4 r4 = R.r4[j];
-      test_pair(sm, R, p, c, j, r4.x, r4.y, tx0, ty0, tlog);
-    }
-    const int rest = cnt > 1 ? cnt - 1 : 0;
-    int incl = rest;
+    int incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int t = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += t;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int* pre = sm.pre[warp];
-    pre[lane] = incl - rest;
+    pre[lane] = incl - cnt;
     __syncwarp();
-    for (int k = lane; k < total; k += 32) {
-      int q = 0;
+    for (int kb = 0; kb < total; kb += 32) {
+      const int k = kb + lane;
+      bool cov = false;
+      float4 ent;
+      if (k < total) {
+        int q = 0;
 #pragma unroll
-      for (int step = 16; step > 0; step >>= 1)
-        if (pre[q + step] <= k) q += step;
-      const int jj = base + q;
-      const int local = k - pre[q] + 1;
-      const int4 r4 = R.r4[jj];
-      const int yy = (local * r4.w) >> 20;
-      const int xx = local - yy * r4.z;
-      test_pair(sm, R, p, c, jj, r4.x + xx, r4.y + yy, tx0, ty0, tlog);
+        for (int step = 16; step > 0; step >>= 1)
+          if (pre[q + step] <= k) q += step;
+        const int jj = base + q;
+        const int local = k - pre[q];
+        const int4 r4 = R.r4[jj];
+        const int yy = (local * r4.w) >> 20;
+        const int x = r4.x + local - yy * r4.z, y = r4.y + yy;
+        const float4 r0 = R.r0[jj];
+        const float4 r1 = R.r1[jj];
+        const float4 r3 = R.r3[jj];
+        // sign of face_normal . ray_w: the affine surrogate decides unless
+        // it is within its error bound of zero; then the reference's ray.
+        const float sv = fmaf(r3.x, (float)x, fmaf(r3.y, (float)y, r3.z));
+        bool bf;
+        if (sv > r3.w)
+          bf = true;
+        else if (sv < -r3.w)
+          bf = false;
+        else
+          bf = backface_exact(sm.mesh, c, __float_as_int(r1.w), x, y);
+        FaceSetup s;
+        s.v0.x = r0.x;
+        s.v0.y = r0.y;
+        s.v1.x = r0.z;
+        s.v1.y = r0.w;
+        s.v2.x = r1.x;
+        s.v2.y = r1.y;
+        const Bary b = edges_at(s, x, y);
+        cov = covered(b, bf);
+        ent = make_float4(b.w0, b.w1, b.w2,
+                          __int_as_float((jj & 255) | ((x - tx0) << 8) | ((y - ty0) << 13) |
+                                         (bf ? 1 << 18 : 0)));
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, cov);
+      if (cov) Q[qn + __popc(bal & below)] = ent;
+      qn += __popc(bal);
+      if (qn >= 32) {
+        __syncwarp();
+        depth_test(sm, R, p, Q[lane], tlog);
+        const int rest = qn - 32;
+        float4 t;
+        if (lane < rest) t = Q[32 + lane];
+        __syncwarp();
+        if (lane < rest) Q[lane] = t;
+        __syncwarp();
+        qn = rest;
+      }
     }
     __syncwarp();
   }
-}
-
-__device__ __forceinline__ int hash_lookup(const Region& R, int fid) {
-  unsigned h = hash_fid(fid) & (kHash - 1);
-  for (int probe = 0; probe < kHash; ++probe) {
-    const int k = R.hkey[h];
-    if (k == fid) return R.hval[h];
-    if (k == -1) return -1;
-    h = (h + 1) & (kHash - 1);
-  }
-  return -1;
+  __syncwarp();
+  if (lane < qn) depth_test(sm, R, p, Q[lane], tlog);
 }
 
 __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
@@ -379,6 +414,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
   const int T = 1 << tlog;
   if (p.counters->dropped) return;  // entries were not written: the host retries
   int cur_view = -1;
+  Region& R = sm.reg;
   for (;;) {
     if (tid == 0) sm.item = (int)atomicAdd(&p.counters->next_tile, 1u);
     __syncthreads();
@@ -398,7 +434,6 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
     const int tx0 = txi << tlog, ty0 = tyi << tlog;
     const int tw = min(T, c.width - tx0), th = min(T, c.height - ty0);
     for (int i = tid; i < T * T; i += kTileThreads) sm.keys[i] = kEmptyKey;
-    for (int i = tid; i < kHash; i += kTileThreads) sm.reg[0].hkey[i] = sm.reg[1].hkey[i] = -1;
     // entries drawn first: [e0, e1); drawn last: [e1, e2)
     const int e0 = p.tile_off[item], e1 = p.tile_lo[item], e2 = p.tile_off[item + 1];
     const float4* proj = p.proj + sm.view.proj_offset;
@@ -411,7 +446,6 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
                        fmaxf(fabsf(c.cy), fabsf(c.height - 1 - c.cy)) / c.fy;
 
     for (int phase = 0; phase < 2; ++phase) {
-      Region& R = sm.reg[phase];
       float zmax = __int_as_float(0x7f800000);
       if (phase == 1) {
         if (e2 == e1) break;
@@ -434,10 +468,6 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
       const int eb = phase ? e1 : e0, ee = phase ? e2 : e1;
       for (int cs = eb; cs < ee; cs += kChunk) {
         const int m = min(kChunk, ee - cs);
-        if (cs > eb) {
-          for (int i = tid; i < kHash; i += kTileThreads) R.hkey[i] = -1;
-          __syncthreads();
-        }
         for (int j = tid; j < m; j += kTileThreads) {
           const int2 e = p.entries[cs + j];
           const float zlb = __int_as_float(e.y);
@@ -464,81 +494,106 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
           const float tol = kU64 * (G * (1.0f + Dx + Dy) + fabsf(sa) * (c.width + fabsf(c.cx)) +
                                     fabsf(sb) * (c.height + fabsf(c.cy)) + fabsf(g2)) +
                             2.0f * kU64 * G * Dmax;
+          // depth pre-test factors, only where every product stays normal
+          const float z0 = s.v0.z, z1 = s.v1.z, z2 = s.v2.z;
+          const float zlo = 9.5367431640625e-07f, zhi = 1048576.0f;  // 2^-20, 2^20
+          const bool pre_ok = z0 >= zlo && z0 <= zhi && z1 >= zlo && z1 <= zhi && z2 >= zlo &&
+                              z2 <= zhi && fabsf(s.area) >= 8.673617379884035e-19f;  // 2^-60
+          const float aP = pre_ok ? fabsf(s.area) * (z0 * z1 * z2) * 0.99998474f
+                                  : __int_as_float(0x7fc00000);
           R.r0[j] = make_float4(s.v0.x, s.v0.y, s.v1.x, s.v1.y);
           R.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, __int_as_float(f));
-          R.r2[j] = make_float4(s.v0.z, s.v1.z, s.v2.z, zlb);
+          R.r2[j] = make_float4(z0, z1, z2, 0.0f);
           R.r3[j] = make_float4(sa, sb, sc, tol);
-          R.r4[j] = make_int4(bx0, by0, bw, (1 << 20) / bw + ((1 << 20) % bw ? 1 : 0));
+          R.r5[j] = make_float4(z1 * z2, z0 * z2, z0 * z1, aP);
+          R.r4[j] = make_int4(bx0, by0, bw, ((1 << 20) + bw - 1) / bw);
           R.cnt[j] = bw * bh;
-          unsigned h = hash_fid(f) & (kHash - 1);
-          while (atomicCAS(&R.hkey[h], -1, f) != -1) h = (h + 1) & (kHash - 1);
-          R.hval[h] = (short)j;
         }
         __syncthreads();
         raster_pass(sm, R, p, c, m, tx0, ty0, tlog);
         __syncthreads();
       }
     }
-    // Loop C for the tile's pixels.
+
+    // Loop C's z-test outputs (rasterizer.cc:244-262); shading is k_shade's.
     const DevView& V = sm.view;
     const int W = c.width;
     for (int i = tid; i < T * T; i += kTileThreads) {
       const int ly = i >> tlog, lx = i & (T - 1);
       if (lx >= tw || ly >= th) continue;
-      const int x = tx0 + lx, y = ty0 + ly;
-      const int64_t pix = (int64_t)y * W + x;
+      const int64_t pix = (int64_t)(ty0 + ly) * W + tx0 + lx;
       const unsigned long long key = sm.keys[i];
       float depth = 0.0f;
       int32_t fid = -1;
       uint8_t mask = 0;
-      Shaded sh;
-      sh.c[0] = sh.c[1] = sh.c[2] = 0;
-      sh.cf[0] = sh.cf[1] = sh.cf[2] = 0.0f;
-      sh.n[0] = sh.n[1] = sh.n[2] = 0.0f;
       if (key != kEmptyKey && !(p.backface_culling && key_backface(key))) {
         depth = key_depth(key);
         fid = key_face(key);
-        if (fid > 0) {  // rasterizer.cc:254: face 0 is never shaded
-          mask = 255;
-          FaceSetup s;
-          int r = 0, slot = hash_lookup(sm.reg[0], fid);
-          if (slot < 0) {
-            r = 1;
-            slot = hash_lookup(sm.reg[1], fid);
-          }
-          if (slot >= 0) {
-            const Region& R = sm.reg[r];
-            const float4 r0 = R.r0[slot], r1 = R.r1[slot], r2 = R.r2[slot];
-            s.v0 = make_float3(r0.x, r0.y, r2.x);
-            s.v1 = make_float3(r0.z, r0.w, r2.y);
-            s.v2 = make_float3(r1.x, r1.y, r2.z);
-            s.area = r1.z;
-          } else {
-            setup_proj(proj, sm.mesh.vidx, fid, c, s);
-          }
-          shade_face_pixel(p.shade, sm.mesh, c, fid, s, x, y, sh);
-        }
+        if (fid > 0) mask = 255;  // rasterizer.cc:254: face 0 is never shaded
       }
       if (V.depth) V.depth[pix] = depth;
       if (V.face_id) V.face_id[pix] = fid;
       if (V.mask) V.mask[pix] = mask;
-      if (V.color) {
-        V.color[3 * pix + 0] = sh.c[0];
-        V.color[3 * pix + 1] = sh.c[1];
-        V.color[3 * pix + 2] = sh.c[2];
-      }
-      if (V.normal) {
-        V.normal[3 * pix + 0] = sh.n[0];
-        V.normal[3 * pix + 1] = sh.n[1];
-        V.normal[3 * pix + 2] = sh.n[2];
-      }
-      if (V.color_f32) {
-        V.color_f32[3 * pix + 0] = sh.cf[0];
-        V.color_f32[3 * pix + 1] = sh.cf[1];
-        V.color_f32[3 * pix + 2] = sh.cf[2];
-      }
     }
     __syncthreads();
+  }
+}
+
+// Loop C's shading (rasterizer.cc:254-299) for every pixel of every view,
+// from the face ids k_tile wrote: kShadePixels pixels per block, one view
+// per block.
+__global__ void __launch_bounds__(256) k_shade(TileParams p) {
+  // k_tile wrote no face ids when the entries did not fit: the host retries
+  if (p.counters->dropped) return;
+  int lo = 0, hi = p.num_views - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (p.views[mid].shade_block <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const DevView& V = p.views[lo];
+  if (!V.color && !V.normal && !V.color_f32) return;  // nothing to shade in this view
+  const DevMesh& M = p.meshes[V.mesh];
+  const Cam& c = V.cam;
+  const int W = c.width;
+  const int64_t npx = (int64_t)W * c.height;
+  const int64_t first = (int64_t)(blockIdx.x - V.shade_block) * kShadePixels;
+  const float4* proj = p.proj + V.proj_offset;
+  for (int k = threadIdx.x; k < kShadePixels; k += blockDim.x) {
+    const int64_t pix = first + k;
+    if (pix >= npx) break;
+    const int fid = V.face_id[pix];
+    Shaded sh;
+    sh.c[0] = sh.c[1] = sh.c[2] = 0;
+    sh.cf[0] = sh.cf[1] = sh.cf[2] = 0.0f;
+    sh.n[0] = sh.n[1] = sh.n[2] = 0.0f;
+    if (fid > 0) {
+      const int y = (int)(pix / W), x = (int)(pix - (int64_t)y * W);
+      FaceSetup s;
+      const int4 vi = __ldg(&M.vidx[fid]);
+      const float4 a = __ldg(&proj[vi.x]);
+      const float4 b = __ldg(&proj[vi.y]);
+      const float4 d = __ldg(&proj[vi.z]);
+      s.v0 = make_float3(a.x, a.y, a.z);
+      s.v1 = make_float3(b.x, b.y, b.z);
+      s.v2 = make_float3(d.x, d.y, d.z);
+      s.area = edge_fn(a.x, a.y, b.x, b.y, d.x, d.y);
+      shade_face_pixel(p.shade, M, c, fid, s, x, y, sh);
+    }
+    if (V.color) {
+      V.color[3 * pix + 0] = sh.c[0];
+      V.color[3 * pix + 1] = sh.c[1];
+      V.color[3 * pix + 2] = sh.c[2];
+    }
+    if (V.normal) {
+      V.normal[3 * pix + 0] = sh.n[0];
+      V.normal[3 * pix + 1] = sh.n[1];
+      V.normal[3 * pix + 2] = sh.n[2];
+    }
+    if (V.color_f32) {
+      V.color_f32[3 * pix + 0] = sh.cf[0];
+      V.color_f32[3 * pix + 1] = sh.cf[1];
+      V.color_f32[3 * pix + 2] = sh.cf[2];
+    }
   }
 }
 
@@ -560,6 +615,10 @@ void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {
 
 void launch_tile(const TileParams& p, int grid, cudaStream_t s) {
   k_tile<<<grid, kTileThreads, sizeof(TileSmem), s>>>(p);
+}
+
+void launch_shade(const TileParams& p, cudaStream_t s) {
+  if (p.shade_blocks > 0) k_shade<<<p.shade_blocks, 256, 0, s>>>(p);
 }
 
 int tile_kernel_blocks_per_sm() {
