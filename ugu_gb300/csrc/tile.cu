@@ -40,9 +40,11 @@ constexpr int kTileThreads = 256;
 constexpr int kWarps = kTileThreads / 32;
 constexpr int kChunk = 256;      // faces set up in shared memory at a time
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
-constexpr int kAgg = 128;        // distinct tiles a binning block aggregates
-constexpr int kAggPerFace = 4;   // faces touching more tiles append directly
+constexpr int kBinFaces = 4;     // faces per binning thread
+constexpr int kAgg = 256;        // distinct tiles a binning block aggregates
+constexpr int kAggPerFace = 2;   // faces touching more tiles append directly
 constexpr int kAggProbes = 8;
+constexpr int kScanItems = 8;    // tile counts per scan thread and round
 constexpr float kU64 = 3.814697265625e-06f;  // 2^-18 = 64 ulp(1)
 
 __device__ __forceinline__ int find_view_by_tile(const TileParams& p, int t) {
@@ -117,17 +119,48 @@ struct BinSmem {
 };
 
 __device__ __forceinline__ int agg_slot(BinSmem& sb, int t) {
-  unsigned h = ((unsigned)t * 2654435761u) >> 25;  // 7 bits
+  unsigned h = ((unsigned)t * 2654435761u) >> 24;  // 8 bits
   for (int probe = 0; probe < kAggProbes; ++probe) {
-    const int cur = atomicCAS(&sb.tile[h], -1, t);
-    if (cur == -1 || cur == t) return (int)h;
+    const int seen = *(volatile int*)&sb.tile[h];
+    if (seen == t) return (int)h;
+    if (seen == -1) {
+      const int cur = atomicCAS(&sb.tile[h], -1, t);
+      if (cur == -1 || cur == t) return (int)h;
+    }
     h = (h + 1) & (kAgg - 1);
   }
   return -1;
 }
 
-// One block per (256 faces, view).  kFill = false: count the entries of
-// every tile; kFill = true: write them (after k_scan placed the cursors).
+// The screen tiles of one face: the per-face culls of Loop B from the
+// projected-vertex table, then the tile range of its pixel bbox.
+struct FaceBins {
+  int n, tx0, ty0, ntx, cls;
+  float zlb;
+};
+
+__device__ __forceinline__ FaceBins bin_face(const TileParams& p, const BinSmem& sb, int f) {
+  FaceBins b{0, 0, 0, 1, 0, -1.0f};
+  if (f >= sb.mesh.num_faces) return b;
+  FaceSetup s;
+  if (!setup_proj(p.proj + sb.view.proj_offset, sb.mesh.vidx, f, sb.view.cam, s) ||
+      s.x1 < s.x0 || s.y1 < s.y0)
+    return b;
+  const int ts = p.tile_log2;
+  b.tx0 = s.x0 >> ts;
+  b.ty0 = s.y0 >> ts;
+  b.ntx = (s.x1 >> ts) - b.tx0 + 1;
+  b.n = b.ntx * ((s.y1 >> ts) - b.ty0 + 1);
+  b.zlb = depth_lower_bound(s);
+  b.cls = b.zlb > sb.view.split_z ? 1 : 0;
+  return b;
+}
+
+// One block per (kBinThreads * kBinFaces faces, view).  kFill = false:
+// count the entries of every tile; kFill = true: write them (after k_scan
+// placed the cursors).  Lanes appending to the same (tile, class) take
+// their ranks with one shared-memory atomic per warp, and a block takes its
+// range of a tile with one global atomic per (tile, class).
 template <bool kFill>
 __global__ void __launch_bounds__(kBinThreads) k_binpass(TileParams p) {
   __shared__ BinSmem sb;
@@ -140,41 +173,44 @@ __global__ void __launch_bounds__(kBinThreads) k_binpass(TileParams p) {
   __syncthreads();
   copy_words(sb.mesh, p.meshes[sb.view.mesh]);
   __syncthreads();
-  const Cam& c = sb.view.cam;
-  const int f = blockIdx.x * kBinThreads + threadIdx.x;
-  int n = 0, tx0 = 0, ty0 = 0, ntx = 1, cls = 0;
-  float zlb = -1.0f;
-  if (f < sb.mesh.num_faces) {
-    FaceSetup s;
-    if (setup_proj(p.proj + sb.view.proj_offset, sb.mesh.vidx, f, c, s) && s.x1 >= s.x0 &&
-        s.y1 >= s.y0) {
-      const int ts = p.tile_log2;
-      tx0 = s.x0 >> ts;
-      ty0 = s.y0 >> ts;
-      ntx = (s.x1 >> ts) - tx0 + 1;
-      n = ntx * ((s.y1 >> ts) - ty0 + 1);
-      zlb = depth_lower_bound(s);
-      cls = zlb > sb.view.split_z ? 1 : 0;
-    }
-  }
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   const int tbase = sb.view.tile_base, tiles_x = sb.view.tiles_x;
-  auto tile_of = [&](int k) { return tbase + (ty0 + k / ntx) * tiles_x + tx0 + k % ntx; };
-  const bool agg = n <= kAggPerFace;
-  int slot[kAggPerFace], rank[kAggPerFace];
+  const int f0 = blockIdx.x * (kBinThreads * kBinFaces) + threadIdx.x;
+  FaceBins fb[kBinFaces];
 #pragma unroll
-  for (int k = 0; k < kAggPerFace; ++k) {
-    slot[k] = -1;
-    rank[k] = 0;
-    if (agg && k < n) {
-      slot[k] = agg_slot(sb, tile_of(k));
-      if (slot[k] >= 0)
-        rank[k] = atomicAdd(&sb.cnt[slot[k]][cls], 1);
-      else if (!kFill)
-        atomicAdd(&p.tile_count[tile_of(k)], 1);
+  for (int u = 0; u < kBinFaces; ++u) fb[u] = bin_face(p, sb, f0 + u * kBinThreads);
+  auto tile_of = [&](const FaceBins& b, int k) {
+    return tbase + (b.ty0 + k / b.ntx) * tiles_x + b.tx0 + k % b.ntx;
+  };
+  int pk[kBinFaces][kAggPerFace];  // slot | rank << 8, or -1: append directly
+#pragma unroll
+  for (int u = 0; u < kBinFaces; ++u) {
+#pragma unroll
+    for (int k = 0; k < kAggPerFace; ++k) {
+      pk[u][k] = -1;
+      const bool act = fb[u].n <= kAggPerFace && k < fb[u].n;
+      const int t = act ? tile_of(fb[u], k) : 0;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (act) {
+        const unsigned peers = __match_any_sync(am, 2 * t + fb[u].cls);
+        const int leader = __ffs(peers) - 1;
+        int slot = 0, base = 0;
+        if (lane == leader) {
+          slot = agg_slot(sb, t);
+          if (slot >= 0)
+            base = atomicAdd(&sb.cnt[slot][fb[u].cls], __popc(peers));
+          else if (!kFill)
+            atomicAdd(&p.tile_count[t], __popc(peers));
+        }
+        slot = __shfl_sync(peers, slot, leader);
+        base = __shfl_sync(peers, base, leader);
+        if (slot >= 0) pk[u][k] = slot | ((base + __popc(peers & below)) << 8);
+      }
     }
+    if (!kFill && fb[u].n > kAggPerFace)
+      for (int k = 0; k < fb[u].n; ++k) atomicAdd(&p.tile_count[tile_of(fb[u], k)], 1);
   }
-  if (!kFill && !agg)
-    for (int k = 0; k < n; ++k) atomicAdd(&p.tile_count[tile_of(k)], 1);
   __syncthreads();
   for (int i = threadIdx.x; i < kAgg; i += kBinThreads) {
     const int t = sb.tile[i];
@@ -189,64 +225,94 @@ __global__ void __launch_bounds__(kBinThreads) k_binpass(TileParams p) {
   }
   if (!kFill) return;
   __syncthreads();
-  const int2 e = make_int2(f, __float_as_int(zlb));
-  auto direct = [&](int t) {
-    return cls ? atomicSub(&p.tile_hi[t], 1) - 1 : atomicAdd(&p.tile_lo[t], 1);
-  };
-  if (agg) {
 #pragma unroll
-    for (int k = 0; k < kAggPerFace; ++k) {
-      if (k >= n) continue;
-      const int pos = slot[k] >= 0 ? sb.base[slot[k]][cls] + rank[k] : direct(tile_of(k));
-      p.entries[pos] = e;
+  for (int u = 0; u < kBinFaces; ++u) {
+    const FaceBins& b = fb[u];
+    const int2 e = make_int2(f0 + u * kBinThreads, __float_as_int(b.zlb));
+    auto direct = [&](int t) {
+      return b.cls ? atomicSub(&p.tile_hi[t], 1) - 1 : atomicAdd(&p.tile_lo[t], 1);
+    };
+    if (b.n <= kAggPerFace) {
+#pragma unroll
+      for (int k = 0; k < kAggPerFace; ++k) {
+        if (k >= b.n) continue;
+        const int pos = pk[u][k] >= 0 ? sb.base[pk[u][k] & 255][b.cls] + (pk[u][k] >> 8)
+                                      : direct(tile_of(b, k));
+        p.entries[pos] = e;
+      }
+    } else {
+      for (int k = 0; k < b.n; ++k) p.entries[direct(tile_of(b, k))] = e;
     }
-  } else {
-    for (int k = 0; k < n; ++k) p.entries[direct(tile_of(k))] = e;
   }
 }
 
-// Exclusive scan of the per-tile counts (one block); zeroes the counts for
-// the next render and flags a render whose entries exceed the buffer.
+// Exclusive scan of the per-tile counts (one block, kScanItems consecutive
+// tiles per thread and round, staged through shared memory so that global
+// accesses coalesce); zeroes the counts for the next render and flags a
+// render whose entries exceed the buffer.
 __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
+  __shared__ int stage[kScanThreads * kScanItems];
   __shared__ long long warp_sum[kScanThreads / 32];
   const int T = p.total_tiles;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int per = (T + kScanThreads - 1) / kScanThreads;
-  const int b = min(T, tid * per), e = min(T, b + per);
-  long long own = 0;
-  for (int t = b; t < e; ++t) own += p.tile_count[t];
-  long long x = own;
+  constexpr int kRound = kScanThreads * kScanItems;
+  long long carry = 0;
+  for (int r0 = 0; r0 < T; r0 += kRound) {
+    for (int i = tid; i < kRound; i += kScanThreads) {
+      const int t = r0 + i;
+      stage[i] = t < T ? p.tile_count[t] : 0;
+      if (t < T) p.tile_count[t] = 0;
+    }
+    __syncthreads();
+    int v[kScanItems];
+    long long own = 0;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const long long y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) warp_sum[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    long long w = warp_sum[lane];
+    for (int k = 0; k < kScanItems; ++k) {
+      v[k] = stage[tid * kScanItems + k];
+      own += v[k];
+    }
+    long long x = own;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const long long y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
+      const long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
     }
-    warp_sum[lane] = w;
-  }
-  __syncthreads();
-  const long long total = warp_sum[kScanThreads / 32 - 1];
-  long long run = x - own + (warp ? warp_sum[warp - 1] : 0);
-  for (int t = b; t < e; ++t) {
-    const int cnt = p.tile_count[t];
-    p.tile_off[t] = (int)run;
-    p.tile_lo[t] = (int)run;
-    run += cnt;
-    p.tile_hi[t] = (int)run;
-    p.tile_count[t] = 0;
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      long long w = warp_sum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_sum[lane] = w;
+    }
+    __syncthreads();
+    long long run = carry + x - own + (warp ? warp_sum[warp - 1] : 0);
+    const long long round_total = warp_sum[kScanThreads / 32 - 1];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      stage[tid * kScanItems + k] = (int)run;  // offsets stay below the entry capacity
+      run += v[k];
+    }
+    __syncthreads();
+    for (int i = tid; i < kRound; i += kScanThreads) {
+      const int t = r0 + i;
+      if (t >= T) break;
+      const int off = stage[i];
+      const int nxt = i + 1 < kRound ? stage[i + 1] : (int)(carry + round_total);
+      p.tile_off[t] = off;
+      p.tile_lo[t] = off;
+      p.tile_hi[t] = nxt;
+    }
+    carry += round_total;
+    __syncthreads();
   }
   if (tid == 0) {
-    p.tile_off[T] = (int)total;
-    p.counters->total_entries = (unsigned long long)total;
-    if (total > p.entry_cap) p.counters->dropped = (unsigned long long)total;
+    p.tile_off[T] = (int)carry;
+    p.counters->total_entries = (unsigned long long)carry;
+    if (carry > p.entry_cap) p.counters->dropped = (unsigned long long)carry;
   }
 }
 
@@ -600,17 +666,19 @@ __global__ void __launch_bounds__(256) k_shade(TileParams p) {
 }  // namespace
 
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
+  constexpr int kPerBlock = kBinThreads * kBinFaces;
   k_proj<<<dim3((p.max_vertices + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads, 0,
            s>>>(p);
-  k_binpass<false><<<dim3((max_faces + kBinThreads - 1) / kBinThreads, p.num_views),
-                     kBinThreads, 0, s>>>(p);
+  k_binpass<false><<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0,
+                     s>>>(p);
   k_scan<<<1, kScanThreads, 0, s>>>(p);
 }
 
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {
+  constexpr int kPerBlock = kBinThreads * kBinFaces;
   launch_size(p, max_faces, s);
-  k_binpass<true><<<dim3((max_faces + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads,
-                     0, s>>>(p);
+  k_binpass<true><<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0,
+                     s>>>(p);
 }
 
 void launch_tile(const TileParams& p, int grid, cudaStream_t s) {
