@@ -36,9 +36,16 @@ namespace {
 
 constexpr int kBinThreads = 256;
 constexpr int kScanThreads = 1024;
-constexpr int kTileThreads = 256;
+#ifndef UGU_TILE_THREADS
+#define UGU_TILE_THREADS 128
+#endif
+#ifndef UGU_TILE_BLOCKS
+#define UGU_TILE_BLOCKS 8
+#endif
+constexpr int kTileThreads = UGU_TILE_THREADS;  // one tile per block
 constexpr int kWarps = kTileThreads / 32;
-constexpr int kChunk = 256;      // faces set up in shared memory at a time
+constexpr int kChunk = kTileThreads;  // faces set up in shared memory at a time
+static_assert(kChunk <= 256, "queue entries hold an 8-bit face slot");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kBinFaces = 4;     // faces per binning thread
 constexpr int kAgg = 256;        // distinct tiles a binning block aggregates
@@ -472,7 +479,7 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const
   if (lane < qn) depth_test(sm, R, p, Q[lane], tlog);
 }
 
-__global__ void __launch_bounds__(kTileThreads, 3) k_tile(TileParams p) {
+__global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TileParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
   const int tid = threadIdx.x;
