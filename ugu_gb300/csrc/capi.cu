@@ -59,9 +59,12 @@ struct Scratch {
   // tiled path
   int32_t* tile_count = nullptr;  // 4 arrays: count, offsets (+1), lo cursor, hi cursor
   size_t tiles_cap = 0;
-  int2* entries = nullptr;
+  int2* entries = nullptr;  // entries_cap in tile order, then entries_cap staged
   size_t entries_cap = 0;
   size_t entries_min = 0;  // capacity asked for by the last overflow
+  int4* runs = nullptr;
+  size_t runs_cap = 0;
+  size_t runs_min = 0;
   float4* proj = nullptr;
   size_t proj_cap = 0;
   int32_t* fid_scratch = nullptr;  // face ids of shaded views that do not output them
@@ -164,6 +167,7 @@ void free_scratch(Scratch& s) {
   cudaFree(s.d_out);
   cudaFree(s.tile_count);
   cudaFree(s.entries);
+  cudaFree(s.runs);
   cudaFree(s.proj);
   cudaFree(s.fid_scratch);
   cudaFree(s.tcounters);
@@ -171,6 +175,41 @@ void free_scratch(Scratch& s) {
   cudaFree(s.d_targets);
   cudaFreeHost(s.h_targets);
   s = Scratch();
+}
+
+// The faces sorted by the 30-bit Morton code of their centroid within the
+// vertices' bounding box [lo, hi].  The tiled path bins faces in this order
+// so that a binning block's faces lie close together on screen whatever
+// the mesh's own face order; results do not depend on it.
+std::vector<int32_t> morton_order(const ugu_gpu_mesh* m, const float lo[3], const float hi[3]) {
+  const int64_t F = m->num_faces;
+  std::vector<std::pair<uint32_t, int32_t>> key(F);
+  auto spread = [](uint32_t x) {  // 10 bits -> every third bit of 30
+    x &= 1023u;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+  };
+  for (int64_t f = 0; f < F; ++f) {
+    uint32_t q[3];
+    for (int k = 0; k < 3; ++k) {
+      double c = 0.0;
+      for (int j = 0; j < 3; ++j) c += m->vertices[3 * (int64_t)m->vertex_indices[3 * f + j] + k];
+      const double ext = (double)hi[k] - (double)lo[k];
+      double u = ext > 0.0 ? (c / 3.0 - lo[k]) / ext : 0.0;
+      if (!(u >= 0.0)) u = 0.0;  // NaN as well
+      if (u > 1.0) u = 1.0;
+      q[k] = (uint32_t)(u * 1023.0);
+    }
+    key[f] = {spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2), (int32_t)f};
+  }
+  std::stable_sort(key.begin(), key.end(),
+                   [](const auto& a, const auto& b) { return a.first < b.first; });
+  std::vector<int32_t> order(F);
+  for (int64_t f = 0; f < F; ++f) order[f] = key[f].second;
+  return order;
 }
 
 template <typename T>
@@ -356,14 +395,25 @@ int ensure_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& gro
   }
   // (face, tile) entries: most faces touch one tile; a render that needs more
   // reports how many, and the next attempt allocates that
-  const size_t want = std::min<size_t>(std::max(s.entries_min, faces + faces / 4 + 4096),
+  const size_t want = std::min<size_t>(s.entries_min ? s.entries_min : faces + faces / 4 + 4096,
                                        (size_t)INT32_MAX);
   if (want > s.entries_cap) {
     cudaFree(s.entries);
     s.entries = nullptr;
     s.entries_cap = 0;
-    CK(ctx, cudaMalloc(&s.entries, want * sizeof(int2)), "cudaMalloc(tile entries)");
+    CK(ctx, cudaMalloc(&s.entries, 2 * want * sizeof(int2)), "cudaMalloc(tile entries)");
     s.entries_cap = want;
+  }
+  // runs: one per (binning block, tile, draw class), one per entry of a face
+  // that touches many tiles
+  const size_t want_runs = std::min<size_t>(s.runs_min ? s.runs_min : faces / 32 + 4096,
+                                            (size_t)INT32_MAX);
+  if (want_runs > s.runs_cap) {
+    cudaFree(s.runs);
+    s.runs = nullptr;
+    s.runs_cap = 0;
+    CK(ctx, cudaMalloc(&s.runs, want_runs * sizeof(int4)), "cudaMalloc(tile runs)");
+    s.runs_cap = want_runs;
   }
   if (groups.size() > s.tcounters_cap) {
     cudaFree(s.tcounters);
@@ -473,6 +523,14 @@ int persistent_grid(ugu_gpu_context* ctx, int blocks_per_sm) {
   return ctx->num_sms * std::max(per_sm, 1);
 }
 
+// Entry and run capacities that hold what a render reported, with room to
+// spare; the next ensure_tiled allocates them.
+void want_capacity(Scratch& s, const TileCounters& c) {
+  const size_t e = (size_t)c.total_entries, r = (size_t)c.total_runs;
+  s.entries_min = std::max(s.entries_min, e + e / 8 + 4096);
+  s.runs_min = std::max(s.runs_min, r + r / 8 + 4096);
+}
+
 TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) {
   const ugu_gpu_option& o = ctx->opt;
   TileParams p{};
@@ -485,12 +543,15 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.total_tiles = (int32_t)gr.tiles;
   p.max_vertices = gr.max_vertices;
   p.entry_cap = (int64_t)s.entries_cap;
+  p.run_cap = (int64_t)s.runs_cap;
   p.proj = s.proj;
   p.tile_count = s.tile_count;
   p.tile_off = s.tile_count + s.tiles_cap;
   p.tile_lo = p.tile_off + s.tiles_cap + 1;
   p.tile_hi = p.tile_lo + s.tiles_cap;
   p.entries = s.entries;
+  p.staged = s.entries + s.entries_cap;
+  p.runs = s.runs;
   p.counters = s.tcounters + gi;
   p.shade_blocks = (int32_t)gr.shade_blocks;
   return p;
@@ -504,7 +565,7 @@ int enqueue_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& gr
     TileParams p = tile_params(ctx, s, gr, gi);
     CK(ctx, cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream),
        "cudaMemsetAsync(tile counters)");
-    launch_bin(p, gr.max_faces, ctx->stream);
+    launch_bin(p, gr.max_faces, ctx->num_sms * 8, ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
     launch_shade(p, ctx->stream);
     nk += kBinKernels + 1 + (p.shade_blocks > 0 ? 1 : 0);
@@ -529,10 +590,7 @@ int size_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& group
                           cudaMemcpyDeviceToHost, ctx->stream),
      "cudaMemcpyAsync(tile counters)");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "sizing pass");
-  size_t need = 0;
-  for (size_t gi = 0; gi < groups.size(); ++gi)
-    need = std::max(need, (size_t)s.h_tcounters[gi].total_entries);
-  s.entries_min = std::max(s.entries_min, need + need / 8 + 4096);
+  for (size_t gi = 0; gi < groups.size(); ++gi) want_capacity(s, s.h_tcounters[gi]);
   return ensure_tiled(ctx, s, groups);
 }
 
@@ -649,9 +707,8 @@ int check_counters(ugu_gpu_context* ctx, Scratch& s, size_t ngroups) {
       special += s.h_tcounters[g].special;
       if (s.h_tcounters[g].dropped) {
         // the next attempt allocates what this render reported it needs
-        const size_t total = (size_t)s.h_tcounters[g].total_entries;
-        overflow += total;
-        s.entries_min = std::max(s.entries_min, total + total / 8 + 4096);
+        overflow += s.h_tcounters[g].total_entries;
+        want_capacity(s, s.h_tcounters[g]);
       }
       items += s.h_tcounters[g].total_entries;
     }
@@ -892,6 +949,7 @@ int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) 
   d.num_faces = m->num_faces;
   if ((rc = upload(ctx, s, v4, &d.vertices))) return rc;
   if ((rc = upload(ctx, s, pad3i(m->vertex_indices), &d.vidx))) return rc;
+  if ((rc = upload(ctx, s, morton_order(m, lo, hi), &d.order))) return rc;
   if (m->face_normals && F > 0) {
     if ((rc = upload(ctx, s, pad3f(m->face_normals, F), &d.fnormals))) return rc;
     s.has_fnormals = true;
@@ -1090,10 +1148,12 @@ int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
     Scratch& s = ctx->scratch;
     cudaFree(s.tile_count);
     cudaFree(s.entries);
+    cudaFree(s.runs);
     s.tile_count = nullptr;
     s.entries = nullptr;
-    s.tiles_cap = s.entries_cap = 0;
-    s.entries_min = (size_t)t->entry_capacity;
+    s.runs = nullptr;
+    s.tiles_cap = s.entries_cap = s.runs_cap = 0;
+    s.entries_min = s.runs_min = (size_t)t->entry_capacity;
   }
   ctx->tuning = *t;
   return UGU_GPU_OK;

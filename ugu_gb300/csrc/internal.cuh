@@ -37,6 +37,7 @@ struct DevMesh {
   const int4* uvidx;
   const int32_t* mat_ids;
   const DevTexture* textures;
+  const int32_t* order;  // faces in 3D Morton order of their centroids (binning order)
 };
 
 struct DevView {
@@ -103,12 +104,15 @@ struct TileCounters {
   unsigned int next_tile;             // work-queue head of k_tile
   unsigned int pad0;
   unsigned long long special;         // covered samples with unorderable depth
-  unsigned long long dropped;         // entries beyond the entry buffer (0: none)
+  unsigned long long dropped;         // entries or runs did not fit (0: none)
   unsigned long long total_entries;   // (face, tile) entries of this render
+  unsigned long long total_runs;      // staged runs of this render
 };
 
-// Tiled-path buffers.  Per global tile t, k_fill writes the entries of the
-// faces drawn first to [tile_off[t], tile_lo[t]) and those drawn last to
+// Tiled-path buffers.  k_bin stages the (face, tile) entries as runs, each
+// run the entries of one block for one (tile, draw class); per global tile
+// t, k_gather then copies the entries of the faces drawn first to
+// [tile_off[t], tile_lo[t]) and those drawn last to
 // [tile_lo[t], tile_off[t + 1]).  An entry is (face id, bit pattern of a
 // lower bound of every depth the face can produce).
 struct TileParams {
@@ -120,13 +124,16 @@ struct TileParams {
   int32_t tile_log2;
   int32_t total_tiles;
   int32_t max_vertices;
-  int64_t entry_cap;
+  int64_t entry_cap;    // entries (and staged entries) the buffers hold
+  int64_t run_cap;      // runs the run list holds
   float4* proj;         // projected vertices (x, y, camera z, 0) of every view
-  int32_t* tile_count;  // entries per tile (k_count adds; k_scan reads and zeroes)
+  int32_t* tile_count;  // entries per tile (k_bin adds; k_scan reads and zeroes)
   int32_t* tile_off;    // total_tiles + 1 offsets into entries
   int32_t* tile_lo;     // first-drawn cursor / boundary per tile
   int32_t* tile_hi;     // last-drawn cursor per tile
-  int2* entries;
+  int2* staged;         // entries in k_bin's order
+  int4* runs;           // (tile, draw class, first staged entry, count)
+  int2* entries;        // entries in tile order
   TileCounters* counters;
   int32_t shade_blocks;  // blocks of the shading grid (all views)
 };
@@ -147,9 +154,11 @@ struct BackwardParams {
 // Host-side launcher (backward.cu).
 void launch_backward(const BackwardParams& p, int64_t max_pixels, cudaStream_t s);
 
-// Host-side launchers (tile.cu).  launch_bin enqueues projection, counting,
-// the offset scan and the fill; launch_tile the per-tile raster + resolve.
-void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
+// Host-side launchers (tile.cu).  launch_bin enqueues projection, binning,
+// the offset scan and the gather (launch_size all but the gather, to learn
+// a render's entry and run counts); launch_tile the per-tile raster and
+// launch_shade the per-pixel shading.
+void launch_bin(const TileParams& p, int max_faces, int gather_blocks, cudaStream_t s);
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
 void launch_shade(const TileParams& p, cudaStream_t s);

@@ -3,23 +3,24 @@
 //
 //   k_proj   Loop A (rasterizer.cc:131-136): every vertex of every view through
 //            PinholeCamera::Project once, into a table of float4 (x, y, z).
-//   k_count  per (view, face): the per-face culls of Loop B
-//            (rasterizer.cc:163-193) from the table, and the number of screen
-//            tiles the face's bbox touches, summed per tile (a block first
-//            aggregates its faces' tiles in shared memory).
+//   k_bin    one pass over every (view, face): the per-face culls of Loop B
+//            (rasterizer.cc:163-193) from the table and the screen tiles the
+//            face's bbox touches.  A block sorts its (face, tile) entries by
+//            tile in shared memory and stages them as runs, one per
+//            (tile, draw class), counting the entries of every tile.
 //   k_scan   exclusive scan of the per-tile counts into entry offsets, so the
 //            entry buffer holds exactly the render's (face, tile) pairs.
-//   k_fill   the same pass again, writing every (face, tile) entry into its
-//            tile's range: faces drawn first from the front, faces drawn last
-//            from the back.
+//   k_gather copies every run into its tile's range: faces drawn first from
+//            the front, faces drawn last from the back.
 //   k_tile   persistent blocks pull (view, tile) items from a work queue.
 //            For one tile: set the listed faces up in shared memory, split
 //            each warp's 32 faces into (face, pixel) pairs with a warp prefix
-//            scan of their bbox-in-tile pixel counts, run Loop B's pixel test
-//            on every pair into a shared-memory z-buffer of 64-bit
-//            (depth bits << 32 | face id << 1 | back-face bit) keys with
-//            atomicMin, then run Loop C (rasterizer.cc:244-301) for the
-//            tile's pixels and write the outputs.
+//            scan of their bbox-in-tile pixel counts, test every pair's
+//            coverage (Loop B's pixel test), queue the covered ones and run
+//            their z-test 32 at a time into a shared-memory z-buffer of
+//            64-bit (depth bits << 32 | face id << 1 | back-face bit) keys
+//            with atomicMin, then write Loop C's depth, face id and mask.
+//   k_shade  Loop C's shading (rasterizer.cc:254-299), one thread per pixel.
 //
 // A face whose depth lower bound lies behind the view's split depth (the
 // camera depth of the mesh's bounding-box centre) is drawn last, and skipped
@@ -49,7 +50,7 @@ static_assert(kChunk <= 256, "queue entries hold an 8-bit face slot");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kBinFaces = 4;     // faces per binning thread
 constexpr int kAgg = 256;        // distinct tiles a binning block aggregates
-constexpr int kAggPerFace = 2;   // faces touching more tiles append directly
+constexpr int kAggPerFace = 2;   // faces touching more tiles take cursor positions
 constexpr int kAggProbes = 8;
 constexpr int kScanItems = 8;    // tile counts per scan thread and round
 constexpr float kU64 = 3.814697265625e-06f;  // 2^-18 = 64 ulp(1)
@@ -121,8 +122,14 @@ struct BinSmem {
   DevView view;
   DevMesh mesh;
   int tile[kAgg];
-  int cnt[kAgg][2];
-  int base[kAgg][2];
+  int cnt[2 * kAgg];  // per (slot, class): entries, then their block-local offset
+  int cur[2 * kAgg];  // per (slot, class): next entry of a many-tile face
+  int warp_sum[kBinThreads / 32][2];
+  int nspill;         // entries whose tile found no slot: one run each
+  int spill_cur;
+  unsigned long long base;      // the block's first staged entry
+  unsigned long long run_base;  // the block's first run
+  int ok;
 };
 
 __device__ __forceinline__ int agg_slot(BinSmem& sb, int t) {
@@ -142,13 +149,16 @@ __device__ __forceinline__ int agg_slot(BinSmem& sb, int t) {
 // The screen tiles of one face: the per-face culls of Loop B from the
 // projected-vertex table, then the tile range of its pixel bbox.
 struct FaceBins {
-  int n, tx0, ty0, ntx, cls;
+  int f, n, tx0, ty0, ntx, cls;
   float zlb;
 };
 
-__device__ __forceinline__ FaceBins bin_face(const TileParams& p, const BinSmem& sb, int f) {
-  FaceBins b{0, 0, 0, 1, 0, -1.0f};
-  if (f >= sb.mesh.num_faces) return b;
+// Face number i of the binning order (see DevMesh::order).
+__device__ __forceinline__ FaceBins bin_face(const TileParams& p, const BinSmem& sb, int i) {
+  FaceBins b{-1, 0, 0, 0, 1, 0, -1.0f};
+  if (i >= sb.mesh.num_faces) return b;
+  const int f = sb.mesh.order ? __ldg(&sb.mesh.order[i]) : i;
+  b.f = f;
   FaceSetup s;
   if (!setup_proj(p.proj + sb.view.proj_offset, sb.mesh.vidx, f, sb.view.cam, s) ||
       s.x1 < s.x0 || s.y1 < s.y0)
@@ -163,24 +173,38 @@ __device__ __forceinline__ FaceBins bin_face(const TileParams& p, const BinSmem&
   return b;
 }
 
-// One block per (kBinThreads * kBinFaces faces, view).  kFill = false:
-// count the entries of every tile; kFill = true: write them (after k_scan
-// placed the cursors).  Lanes appending to the same (tile, class) take
-// their ranks with one shared-memory atomic per warp, and a block takes its
-// range of a tile with one global atomic per (tile, class).
-template <bool kFill>
-__global__ void __launch_bounds__(kBinThreads) k_binpass(TileParams p) {
+// Slot of tile t in the block's table, or -1 (no insertion).
+__device__ __forceinline__ int find_slot(const BinSmem& sb, int t) {
+  unsigned h = ((unsigned)t * 2654435761u) >> 24;
+  for (int probe = 0; probe < kAggProbes; ++probe) {
+    const int seen = sb.tile[h];
+    if (seen == t) return (int)h;
+    if (seen == -1) return -1;
+    h = (h + 1) & (kAgg - 1);
+  }
+  return -1;
+}
+
+// One block per (kBinThreads * kBinFaces faces, view), one pass over the
+// faces.  The block sorts its (face, tile) entries by (tile, class) in
+// shared memory, claims a range of the staging buffer and of the run list
+// with one global atomic each, and writes each (tile, class) group as one
+// run.  Faces touching at most kAggPerFace tiles take their ranks with one
+// shared atomic per warp and key; faces touching more take positions from
+// per-group cursors after the fast ones; entries whose tile finds no slot
+// in the table (at most kAggProbes probes) become runs of one.
+__global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
   __shared__ BinSmem sb;
-  if (kFill && p.counters->dropped) return;  // entry buffer too small: the host retries
   copy_words(sb.view, p.views[blockIdx.y]);
   for (int i = threadIdx.x; i < kAgg; i += kBinThreads) {
     sb.tile[i] = -1;
-    sb.cnt[i][0] = sb.cnt[i][1] = 0;
+    sb.cnt[2 * i] = sb.cnt[2 * i + 1] = 0;
   }
+  if (threadIdx.x == 0) sb.nspill = sb.spill_cur = 0;
   __syncthreads();
   copy_words(sb.mesh, p.meshes[sb.view.mesh]);
   __syncthreads();
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned below = (1u << lane) - 1u;
   const int tbase = sb.view.tile_base, tiles_x = sb.view.tiles_x;
   const int f0 = blockIdx.x * (kBinThreads * kBinFaces) + threadIdx.x;
@@ -190,7 +214,8 @@ __global__ void __launch_bounds__(kBinThreads) k_binpass(TileParams p) {
   auto tile_of = [&](const FaceBins& b, int k) {
     return tbase + (b.ty0 + k / b.ntx) * tiles_x + b.tx0 + k % b.ntx;
   };
-  int pk[kBinFaces][kAggPerFace];  // slot | rank << 8, or -1: append directly
+  // fast entries: ranks within their (slot, class) group
+  int pk[kBinFaces][kAggPerFace];  // (slot, class) | rank << 9, or -1: a spilled entry
 #pragma unroll
   for (int u = 0; u < kBinFaces; ++u) {
 #pragma unroll
@@ -206,50 +231,143 @@ __global__ void __launch_bounds__(kBinThreads) k_binpass(TileParams p) {
         if (lane == leader) {
           slot = agg_slot(sb, t);
           if (slot >= 0)
-            base = atomicAdd(&sb.cnt[slot][fb[u].cls], __popc(peers));
-          else if (!kFill)
-            atomicAdd(&p.tile_count[t], __popc(peers));
+            base = atomicAdd(&sb.cnt[2 * slot + fb[u].cls], __popc(peers));
+          else
+            atomicAdd(&sb.nspill, __popc(peers));
         }
         slot = __shfl_sync(peers, slot, leader);
         base = __shfl_sync(peers, base, leader);
-        if (slot >= 0) pk[u][k] = slot | ((base + __popc(peers & below)) << 8);
+        if (slot >= 0)
+          pk[u][k] = (2 * slot + fb[u].cls) | ((base + __popc(peers & below)) << 9);
       }
     }
-    if (!kFill && fb[u].n > kAggPerFace)
-      for (int k = 0; k < fb[u].n; ++k) atomicAdd(&p.tile_count[tile_of(fb[u], k)], 1);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < kAgg; i += kBinThreads) {
-    const int t = sb.tile[i];
-    if (t < 0) continue;
-    const int c0 = sb.cnt[i][0], c1 = sb.cnt[i][1];
-    if (!kFill) {
-      atomicAdd(&p.tile_count[t], c0 + c1);
-    } else {
-      if (c0) sb.base[i][0] = atomicAdd(&p.tile_lo[t], c0);
-      if (c1) sb.base[i][1] = atomicSub(&p.tile_hi[t], c1) - c1;
+  // many-tile faces: counted after the fast entries of every group
+  for (int i = threadIdx.x; i < 2 * kAgg; i += kBinThreads) sb.cur[i] = sb.cnt[i];
+#pragma unroll
+  for (int u = 0; u < kBinFaces; ++u) {
+    if (fb[u].n <= kAggPerFace) continue;
+    for (int k = 0; k < fb[u].n; ++k) {
+      const int slot = agg_slot(sb, tile_of(fb[u], k));
+      if (slot >= 0)
+        atomicAdd(&sb.cnt[2 * slot + fb[u].cls], 1);
+      else
+        atomicAdd(&sb.nspill, 1);
     }
   }
-  if (!kFill) return;
   __syncthreads();
+  // block-wide exclusive scan of the (slot, class) counts and of the
+  // nonempty groups (the runs); thread i owns slot i
+  static_assert(kAgg == kBinThreads, "one aggregation slot per thread");
+  const int i = threadIdx.x;
+  const int c0 = sb.cnt[2 * i], c1 = sb.cnt[2 * i + 1];
+  const int own_e = c0 + c1, own_r = (c0 > 0) + (c1 > 0);
+  int xe = own_e, xr = own_r;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int ye = __shfl_up_sync(0xffffffffu, xe, o);
+    const int yr = __shfl_up_sync(0xffffffffu, xr, o);
+    if (lane >= o) {
+      xe += ye;
+      xr += yr;
+    }
+  }
+  if (lane == 31) {
+    sb.warp_sum[warp][0] = xe;
+    sb.warp_sum[warp][1] = xr;
+  }
+  __syncthreads();
+  int pe = 0, pr = 0, te = 0, tr = 0;
+  for (int w = 0; w < kBinThreads / 32; ++w) {
+    if (w < warp) {
+      pe += sb.warp_sum[w][0];
+      pr += sb.warp_sum[w][1];
+    }
+    te += sb.warp_sum[w][0];
+    tr += sb.warp_sum[w][1];
+  }
+  // spilled entries follow the grouped ones, in the staging buffer and in
+  // the run list alike
+  const int ns = sb.nspill;
+  const int off0 = pe + xe - own_e;  // block-local offset of (slot i, class 0)
+  if (threadIdx.x == 0) {
+    const unsigned long long ne = (unsigned long long)(te + ns), nr = (unsigned long long)(tr + ns);
+    const unsigned long long b = ne ? atomicAdd(&p.counters->total_entries, ne) : 0;
+    const unsigned long long r = nr ? atomicAdd(&p.counters->total_runs, nr) : 0;
+    const bool ok = b + ne <= (unsigned long long)p.entry_cap &&
+                    r + nr <= (unsigned long long)p.run_cap;
+    if (!ok) atomicExch(&p.counters->dropped, 1ull);
+    sb.base = b;
+    sb.run_base = r;
+    sb.ok = ok;
+  }
+  __syncthreads();
+  const bool ok = sb.ok;
+  if (!ok) return;  // the render is retried with the counts this one reported
+  sb.cur[2 * i] += off0;
+  sb.cur[2 * i + 1] += off0 + c0;
+  sb.cnt[2 * i] = off0;
+  sb.cnt[2 * i + 1] = off0 + c0;
+  if (own_r) {
+    const int t = sb.tile[i];
+    unsigned long long r = sb.run_base + (pr + xr - own_r);
+    if (c0) p.runs[r++] = make_int4(t, 0, (int)(sb.base + off0), c0);
+    if (c1) p.runs[r] = make_int4(t, 1, (int)(sb.base + off0 + c0), c1);
+    atomicAdd(&p.tile_count[t], own_e);
+  }
+  __syncthreads();
+  auto spill = [&](int t, int cls, int2 e) {
+    const int k = atomicAdd(&sb.spill_cur, 1);
+    const unsigned long long pos = sb.base + te + k;
+    p.staged[pos] = e;
+    p.runs[sb.run_base + tr + k] = make_int4(t, cls, (int)pos, 1);
+    atomicAdd(&p.tile_count[t], 1);
+  };
 #pragma unroll
   for (int u = 0; u < kBinFaces; ++u) {
     const FaceBins& b = fb[u];
-    const int2 e = make_int2(f0 + u * kBinThreads, __float_as_int(b.zlb));
-    auto direct = [&](int t) {
-      return b.cls ? atomicSub(&p.tile_hi[t], 1) - 1 : atomicAdd(&p.tile_lo[t], 1);
-    };
+    const int2 e = make_int2(b.f, __float_as_int(b.zlb));
     if (b.n <= kAggPerFace) {
 #pragma unroll
       for (int k = 0; k < kAggPerFace; ++k) {
         if (k >= b.n) continue;
-        const int pos = pk[u][k] >= 0 ? sb.base[pk[u][k] & 255][b.cls] + (pk[u][k] >> 8)
-                                      : direct(tile_of(b, k));
-        p.entries[pos] = e;
+        const int q = pk[u][k];
+        if (q >= 0)
+          p.staged[sb.base + sb.cnt[q & 511] + (q >> 9)] = e;
+        else
+          spill(tile_of(b, k), b.cls, e);
       }
     } else {
-      for (int k = 0; k < b.n; ++k) p.entries[direct(tile_of(b, k))] = e;
+      for (int k = 0; k < b.n; ++k) {
+        const int t = tile_of(b, k);
+        const int slot = find_slot(sb, t);
+        if (slot >= 0)
+          p.staged[sb.base + atomicAdd(&sb.cur[2 * slot + b.cls], 1)] = e;
+        else
+          spill(t, b.cls, e);
+      }
     }
+  }
+}
+
+// Copies every run of staged entries into its tile's range (k_scan placed
+// the cursors): faces drawn first from the front, faces drawn last from the
+// back.  One warp per run.
+__global__ void __launch_bounds__(256) k_gather(TileParams p) {
+  if (p.counters->dropped) return;  // entries were not staged: the host retries
+  const unsigned long long nr = p.counters->total_runs;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+  for (unsigned long long r = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < nr;
+       r += warps) {
+    const int4 run = p.runs[r];  // (tile, class, first staged entry, count)
+    int dst = 0;
+    if (lane == 0)
+      dst = run.y ? atomicSub(&p.tile_hi[run.x], run.w) - run.w
+                  : atomicAdd(&p.tile_lo[run.x], run.w);
+    dst = __shfl_sync(0xffffffffu, dst, 0);
+    for (int k = lane; k < run.w; k += 32) p.entries[dst + k] = p.staged[run.z + k];
   }
 }
 
@@ -317,9 +435,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
     __syncthreads();
   }
   if (tid == 0) {
-    p.tile_off[T] = (int)carry;
-    p.counters->total_entries = (unsigned long long)carry;
-    if (carry > p.entry_cap) p.counters->dropped = (unsigned long long)carry;
+    p.tile_off[T] = (int)carry;  // k_bin's cursor keeps the render's entry count
+    if (carry > p.entry_cap) p.counters->dropped = 1ull;
   }
 }
 
@@ -676,16 +793,13 @@ void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
   constexpr int kPerBlock = kBinThreads * kBinFaces;
   k_proj<<<dim3((p.max_vertices + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads, 0,
            s>>>(p);
-  k_binpass<false><<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0,
-                     s>>>(p);
+  k_bin<<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0, s>>>(p);
   k_scan<<<1, kScanThreads, 0, s>>>(p);
 }
 
-void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {
-  constexpr int kPerBlock = kBinThreads * kBinFaces;
+void launch_bin(const TileParams& p, int max_faces, int gather_blocks, cudaStream_t s) {
   launch_size(p, max_faces, s);
-  k_binpass<true><<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0,
-                     s>>>(p);
+  k_gather<<<gather_blocks, 256, 0, s>>>(p);
 }
 
 void launch_tile(const TileParams& p, int grid, cudaStream_t s) {
@@ -711,7 +825,7 @@ int tile_kernel_blocks_per_sm() {
 int bin_kernel_blocks_per_sm() {
   static int blocks = 0;
   if (!blocks) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_binpass<true>, kBinThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_bin, kBinThreads, 0);
     if (blocks < 1) blocks = 1;
   }
   return blocks;
