@@ -51,157 +51,199 @@ __device__ __forceinline__ int run_id(int key, int lane) {
   return 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
 }
 
-// The per-pixel chain in double, from the float inputs (the FP64 restatement
-// the gradients are checked against): colour, loss, dL/dC and the
-// gradients of the three vertices' positions and colours; texel weights and
-// indices for the texel scatter.
-struct Pix64 {
-  double loss;
-  double gC[3];
-  double gpos[9];
-  double gcol[9];
+// One vertex of one view in double: screen x, y, camera z and 1 / z.
+struct alignas(16) Proj64 {
+  double x, y, z, iz;
+};
+
+// The pinhole projection of every vertex of one view (blockIdx.y) in
+// double, from the float vertices and camera (camera.h:380-387).
+__global__ void __launch_bounds__(kThreads) k_proj64(BackwardParams p) {
+  const DevView& V = p.views[blockIdx.y];
+  const DevMesh& M = p.meshes[V.mesh];
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= M.num_vertices) return;
+  const Cam& c = V.cam;
+  const float4 P = __ldg(&M.vertices[i]);
+  double cc[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    cc[j] = (double)c.R[3 * j] * P.x + (double)c.R[3 * j + 1] * P.y +
+            (double)c.R[3 * j + 2] * P.z + (double)c.t[j];
+  Proj64 o;
+  o.iz = 1.0 / cc[2];
+  o.x = (double)c.fx * cc[0] * o.iz + (double)c.cx;
+  o.y = (double)c.fy * cc[1] * o.iz + (double)c.cy;
+  o.z = cc[2];
+  reinterpret_cast<Proj64*>(p.proj64)[V.proj_offset + i] = o;
+}
+
+__device__ __forceinline__ Proj64 load_proj64(const Proj64* t, int i) {
+  const double2* q = reinterpret_cast<const double2*>(t + i);
+  const double2 a = __ldg(q), b = __ldg(q + 1);
+  Proj64 o;
+  o.x = a.x;
+  o.y = a.y;
+  o.z = b.x;
+  o.iz = b.y;
+  return o;
+}
+
+// Vertex-position (and colour, texel) gradients of one pixel.  The
+// quantities whose float rounding the sum over pixels would amplify are
+// formed in double from the view's double projection table: the edge
+// functions and the normalised perspective weights w = r / sum(r) with
+// r_k = e_k / z_k (the area cancels in w, so it has no gradient), the
+// texture coordinates with their texel cell and offsets, and the
+// pixel-to-vertex differences the edge derivatives multiply.  The rest of
+// the chain is float.
+struct PixGrad {
+  float loss;
+  float gpos[9];
+  float gcol[9];
   int64_t tix[4];
-  double tw[4];
+  float tg[4][3];  // per texel: dL/dt
   int ntex;
 };
 
-__device__ __noinline__ void pixel_backward_f64(const BackwardParams& p, const DevMesh& m,
-                                                const Cam& c, int fid, int x, int y,
-                                                const float* target, Pix64& o) {
+__device__ __forceinline__ void pixel_backward(const BackwardParams& p, const DevMesh& m,
+                                               const Cam& c, const Proj64* tab, int fid, int x,
+                                               int y, const float* target, PixGrad& o) {
   const int4 vi = __ldg(&m.vidx[fid]);
-  const int vid[3] = {vi.x, vi.y, vi.z};
-  double X[3], Y[3], Z[3], CX[3], CY[3];
-  for (int k = 0; k < 3; ++k) {
-    const float4 P = __ldg(&m.vertices[vid[k]]);
-    double cc[3];
-    for (int j = 0; j < 3; ++j)
-      cc[j] = (double)c.R[3 * j] * P.x + (double)c.R[3 * j + 1] * P.y +
-              (double)c.R[3 * j + 2] * P.z + (double)c.t[j];
-    CX[k] = cc[0];
-    CY[k] = cc[1];
-    Z[k] = cc[2];
-    X[k] = (double)c.fx * cc[0] / cc[2] + (double)c.cx;
-    Y[k] = (double)c.fy * cc[1] / cc[2] + (double)c.cy;
-  }
+  const Proj64 P[3] = {load_proj64(tab, vi.x), load_proj64(tab, vi.y), load_proj64(tab, vi.z)};
   const double px = x, py = y;
-  auto E = [](double ax, double ay, double bx, double by, double qx, double qy) {
-    return (qx - ax) * (by - ay) - (qy - ay) * (bx - ax);
-  };
-  const double A = E(X[0], Y[0], X[1], Y[1], X[2], Y[2]);
-  const double e[3] = {E(X[1], Y[1], X[2], Y[2], px, py), E(X[2], Y[2], X[0], Y[0], px, py),
-                       E(X[0], Y[0], X[1], Y[1], px, py)};
-  double b[3], q[3], ssum = 0.0;
+  double dx[3], dy[3];  // pixel minus vertex
+#pragma unroll
   for (int k = 0; k < 3; ++k) {
-    b[k] = e[k] / A;
-    q[k] = b[k] / Z[k];
-    ssum += q[k];
+    dx[k] = px - P[k].x;
+    dy[k] = py - P[k].y;
   }
-  const double w[3] = {q[0] / ssum, q[1] / ssum, q[2] / ssum};
-  const double u = w[1], v = w[2], s0 = 1.0 - u - v;
-  double col[3], dcu[3], dcv[3];
+  // e_k = edge(v_a, v_b, p) for (a, b) = (1, 2), (2, 0), (0, 1)
+  const double e0 = dx[1] * (P[2].y - P[1].y) - dy[1] * (P[2].x - P[1].x);
+  const double e1 = dx[2] * (P[0].y - P[2].y) - dy[2] * (P[0].x - P[2].x);
+  const double e2 = dx[0] * (P[1].y - P[0].y) - dy[0] * (P[1].x - P[0].x);
+  const double r[3] = {e0 * P[0].iz, e1 * P[1].iz, e2 * P[2].iz};
+  const double iS = 1.0 / (r[0] + r[1] + r[2]);
+  const double ud = r[1] * iS, vd = r[2] * iS, s0d = 1.0 - ud - vd;
+  const float u = (float)ud, v = (float)vd, s0 = (float)s0d;
+  float col[3], dcu[3], dcv[3];
   o.ntex = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    o.tix[j] = 0;
+    o.tg[j][0] = o.tg[j][1] = o.tg[j][2] = 0.0f;
+  }
   if (p.diffuse_color == 2) {
+    const float4 c0 = __ldg(&m.vcolors[vi.x]);
+    const float4 c1 = __ldg(&m.vcolors[vi.y]);
+    const float4 c2 = __ldg(&m.vcolors[vi.z]);
+    const float a0[3] = {c0.x, c0.y, c0.z}, a1[3] = {c1.x, c1.y, c1.z}, a2[3] = {c2.x, c2.y, c2.z};
+#pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double c0 = ((const float*)&m.vcolors[vid[0]])[k];
-      const double c1 = ((const float*)&m.vcolors[vid[1]])[k];
-      const double c2 = ((const float*)&m.vcolors[vid[2]])[k];
-      col[k] = s0 * c0 + u * c1 + v * c2;
-      dcu[k] = c1 - c0;
-      dcv[k] = c2 - c0;
+      col[k] = (float)(s0d * a0[k] + ud * a1[k] + vd * a2[k]);
+      dcu[k] = a1[k] - a0[k];
+      dcv[k] = a2[k] - a0[k];
     }
   } else {
     const int mid = __ldg(&m.mat_ids[fid]);
     const DevTexture t = m.textures[mid];
     const int4 ti = __ldg(&m.uvidx[fid]);
-    const float2 a = __ldg(&m.uv[ti.x]), bb = __ldg(&m.uv[ti.y]), d = __ldg(&m.uv[ti.z]);
-    const double uvx = s0 * a.x + u * bb.x + v * d.x;
-    const double uvy = s0 * a.y + u * bb.y + v * d.y;
+    const float2 a = __ldg(&m.uv[ti.x]), b = __ldg(&m.uv[ti.y]), d = __ldg(&m.uv[ti.z]);
+    const double uvx = s0d * a.x + ud * b.x + vd * d.x;
+    const double uvy = s0d * a.y + ud * b.y + vd * d.y;
     const double fx = uvx * (t.width - 1), fy = (1.0 - uvy) * (t.height - 1);
     if (p.interp == 0) {
-      const int64_t ix = texel_index((int64_t)llround(fy), (int64_t)llround(fx), t.width, t.height);
-      float tv[3];
-      fetch_texel(t, ix, tv);
-      for (int k = 0; k < 3; ++k) col[k] = tv[k], dcu[k] = dcv[k] = 0.0;
+      const int64_t ix = texel_index((int64_t)llrint(fy), (int64_t)llrint(fx), t.width, t.height);
+      fetch_texel(t, ix, col);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dcu[k] = dcv[k] = 0.0f;
       o.tix[0] = ix;
-      o.tw[0] = 1.0;
+      o.tg[0][0] = o.tg[0][1] = o.tg[0][2] = 1.0f;  // weights; scaled by dL/dC below
       o.ntex = mid == 0 ? 1 : 0;
     } else {
       const double x0 = floor(fx), y0 = floor(fy);
-      const double lu = fx - x0, lv = fy - y0;
-      const int64_t i00 = texel_index((int64_t)y0, (int64_t)x0, t.width, t.height);
-      const int64_t i10 = texel_index((int64_t)y0, (int64_t)x0 + 1, t.width, t.height);
-      const int64_t i01 = texel_index((int64_t)y0 + 1, (int64_t)x0, t.width, t.height);
-      const int64_t i11 = texel_index((int64_t)y0 + 1, (int64_t)x0 + 1, t.width, t.height);
+      const float lu = (float)(fx - x0), lv = (float)(fy - y0);
+      o.tix[0] = texel_index((int64_t)y0, (int64_t)x0, t.width, t.height);
+      o.tix[1] = texel_index((int64_t)y0, (int64_t)x0 + 1, t.width, t.height);
+      o.tix[2] = texel_index((int64_t)y0 + 1, (int64_t)x0, t.width, t.height);
+      o.tix[3] = texel_index((int64_t)y0 + 1, (int64_t)x0 + 1, t.width, t.height);
       float t00[3], t10[3], t01[3], t11[3];
-      fetch_texel(t, i00, t00);
-      fetch_texel(t, i10, t10);
-      fetch_texel(t, i01, t01);
-      fetch_texel(t, i11, t11);
-      const double dfx_du = ((double)bb.x - a.x) * (t.width - 1);
-      const double dfx_dv = ((double)d.x - a.x) * (t.width - 1);
-      const double dfy_du = -((double)bb.y - a.y) * (t.height - 1);
-      const double dfy_dv = -((double)d.y - a.y) * (t.height - 1);
+      fetch_texel(t, o.tix[0], t00);
+      fetch_texel(t, o.tix[1], t10);
+      fetch_texel(t, o.tix[2], t01);
+      fetch_texel(t, o.tix[3], t11);
+      const float dfx_du = (b.x - a.x) * (float)(t.width - 1);
+      const float dfx_dv = (d.x - a.x) * (float)(t.width - 1);
+      const float dfy_du = -(b.y - a.y) * (float)(t.height - 1);
+      const float dfy_dv = -(d.y - a.y) * (float)(t.height - 1);
+      const float w00 = (1.0f - lu) * (1.0f - lv), w10 = lu * (1.0f - lv);
+      const float w01 = (1.0f - lu) * lv, w11 = lu * lv;
+#pragma unroll
       for (int k = 0; k < 3; ++k) {
-        col[k] = (1 - lu) * (1 - lv) * t00[k] + lu * (1 - lv) * t10[k] +
-                 (1 - lu) * lv * t01[k] + lu * lv * t11[k];
-        const double dlu = (1 - lv) * ((double)t10[k] - t00[k]) + lv * ((double)t11[k] - t01[k]);
-        const double dlv = (1 - lu) * ((double)t01[k] - t00[k]) + lu * ((double)t11[k] - t10[k]);
+        col[k] = w00 * t00[k] + w10 * t10[k] + w01 * t01[k] + w11 * t11[k];
+        const float dlu = (1.0f - lv) * (t10[k] - t00[k]) + lv * (t11[k] - t01[k]);
+        const float dlv = (1.0f - lu) * (t01[k] - t00[k]) + lu * (t11[k] - t10[k]);
         dcu[k] = dlu * dfx_du + dlv * dfy_du;
         dcv[k] = dlu * dfx_dv + dlv * dfy_dv;
       }
-      o.tix[0] = i00; o.tix[1] = i10; o.tix[2] = i01; o.tix[3] = i11;
-      o.tw[0] = (1 - lu) * (1 - lv);
-      o.tw[1] = lu * (1 - lv);
-      o.tw[2] = (1 - lu) * lv;
-      o.tw[3] = lu * lv;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        o.tg[0][k] = w00;
+        o.tg[1][k] = w10;
+        o.tg[2][k] = w01;
+        o.tg[3][k] = w11;
+      }
       o.ntex = mid == 0 ? 4 : 0;
     }
   }
-  o.loss = 0.0;
+  float gC[3];
+  o.loss = 0.0f;
+#pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double dd = col[k] - (double)target[k];
+    const float dd = col[k] - __ldg(&target[k]);
     o.loss += dd * dd;
-    o.gC[k] = 2.0 * dd;
-    o.gcol[k] = o.gC[k] * s0;
-    o.gcol[3 + k] = o.gC[k] * u;
-    o.gcol[6 + k] = o.gC[k] * v;
+    gC[k] = 2.0f * dd;
+    o.gcol[k] = gC[k] * s0;
+    o.gcol[3 + k] = gC[k] * u;
+    o.gcol[6 + k] = gC[k] * v;
   }
-  double gw[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o.tg[j][k] *= gC[k];
+  // through w = r / S, r_k = e_k / z_k
+  const float gw1 = gC[0] * dcu[0] + gC[1] * dcu[1] + gC[2] * dcu[2];
+  const float gw2 = gC[0] * dcv[0] + gC[1] * dcv[1] + gC[2] * dcv[2];
+  const float gdotw = gw1 * u + gw2 * v;
+  const float fiS = (float)iS;
+  const float gr[3] = {-gdotw * fiS, (gw1 - gdotw) * fiS, (gw2 - gdotw) * fiS};
+  float ge[3], gZ[3];
+#pragma unroll
   for (int k = 0; k < 3; ++k) {
-    gw[1] += o.gC[k] * dcu[k];
-    gw[2] += o.gC[k] * dcv[k];
+    const float iz = (float)P[k].iz;
+    ge[k] = gr[k] * iz;
+    gZ[k] = -gr[k] * (float)r[k] * iz;
   }
-  const double gdotw = gw[1] * w[1] + gw[2] * w[2];
-  double gX[3] = {0, 0, 0}, gY[3] = {0, 0, 0}, gZ[3] = {0, 0, 0}, gb[3];
-  double gA = 0.0;
-  for (int k = 0; k < 3; ++k) {
-    const double gq = (gw[k] - gdotw) / ssum;
-    gb[k] = gq / Z[k];
-    gZ[k] = -gq * q[k] / Z[k];
-    gA -= gb[k] * b[k] / A;
-  }
+  const float fdx[3] = {(float)dx[0], (float)dx[1], (float)dx[2]};
+  const float fdy[3] = {(float)dy[0], (float)dy[1], (float)dy[2]};
+  float gX[3] = {0.0f, 0.0f, 0.0f}, gY[3] = {0.0f, 0.0f, 0.0f};
   const int ea[3] = {1, 2, 0}, eb[3] = {2, 0, 1};
-  for (int k = 0; k < 3; ++k) {  // e_k = E(v_ea, v_eb, p)
-    const double g = gb[k] / A;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {  // e_k = dy_a dx_b - dx_a dy_b (d = pixel - vertex)
     const int ia = ea[k], ib = eb[k];
-    gX[ia] += g * (py - Y[ib]);
-    gY[ia] += g * (X[ib] - px);
-    gX[ib] -= g * (py - Y[ia]);
-    gY[ib] += g * (px - X[ia]);
+    gX[ia] += ge[k] * fdy[ib];
+    gY[ia] -= ge[k] * fdx[ib];
+    gX[ib] -= ge[k] * fdy[ia];
+    gY[ib] += ge[k] * fdx[ia];
   }
-  gX[0] += gA * (Y[2] - Y[1]);
-  gY[0] += gA * (X[1] - X[2]);
-  gX[1] -= gA * (Y[2] - Y[0]);
-  gY[1] += gA * (X[2] - X[0]);
-  gX[2] += gA * (Y[1] - Y[0]);
-  gY[2] -= gA * (X[1] - X[0]);
+#pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double z = Z[k];
-    const double gcx = gX[k] * c.fx / z;
-    const double gcy = gY[k] * c.fy / z;
-    const double gcz = -gX[k] * c.fx * CX[k] / (z * z) - gY[k] * c.fy * CY[k] / (z * z) + gZ[k];
-    for (int j = 0; j < 3; ++j)
-      o.gpos[3 * k + j] = (double)c.R[j] * gcx + (double)c.R[3 + j] * gcy + (double)c.R[6 + j] * gcz;
+    const float iz = (float)P[k].iz;
+    const float gcx = gX[k] * c.fx * iz;
+    const float gcy = gY[k] * c.fy * iz;
+    const float gcz = -(gX[k] * (float)(P[k].x - c.cx) + gY[k] * (float)(P[k].y - c.cy)) * iz + gZ[k];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) o.gpos[3 * k + j] = c.R[j] * gcx + c.R[3 + j] * gcy + c.R[6 + j] * gcz;
   }
 }
 
@@ -242,21 +284,24 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
   float gc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // vertex colour grads
   int4 vi = make_int4(0, 0, 0, 0);
   if (fid > 0 && p.grad_vertices) {
-    // Position gradients sum many contributions of both signs; the float
-    // chain's rounding (e.g. of the texel coordinates) would be amplified
-    // by that cancellation, so this pixel's chain runs in double.
+    // Position gradients sum many contributions of both signs, which
+    // amplifies rounding: see pixel_backward.
     vi = __ldg(&sm.vidx[fid]);
-    Pix64 o;
-    pixel_backward_f64(p, sm, c, fid, x, y, &p.targets[blockIdx.y][3 * i], o);
-    loss = (float)o.loss;
+    PixGrad o;
+    pixel_backward(p, sm, c, reinterpret_cast<const Proj64*>(p.proj64) + sv.proj_offset, fid, x,
+                   y, &p.targets[blockIdx.y][3 * i], o);
+    loss = o.loss;
+#pragma unroll
     for (int k = 0; k < 9; ++k) {
-      gv[k] = (float)o.gpos[k];
-      gc[k] = p.diffuse_color == 2 ? (float)o.gcol[k] : 0.0f;
+      gv[k] = o.gpos[k];
+      gc[k] = p.diffuse_color == 2 ? o.gcol[k] : 0.0f;
     }
     if (p.grad_texels && p.diffuse_color == 1)
-      for (int j = 0; j < o.ntex; ++j)
-        for (int k = 0; k < 3; ++k)
-          atomicAdd(&p.grad_texels[3 * o.tix[j] + k], (float)(o.gC[k] * o.tw[j]));
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < o.ntex)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) atomicAdd(&p.grad_texels[3 * o.tix[j] + k], o.tg[j][k]);
   } else if (fid > 0) {
     // Texel and vertex-colour gradients only: the float colour equals the
     // forward's (same exact arithmetic), so the loss is the rendered one.
@@ -369,7 +414,10 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
 
 }  // namespace
 
-void launch_backward(const BackwardParams& p, int64_t max_pixels, cudaStream_t s) {
+void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices,
+                     cudaStream_t s) {
+  if (p.grad_vertices)
+    k_proj64<<<dim3((max_vertices + kThreads - 1) / kThreads, p.num_views), kThreads, 0, s>>>(p);
   dim3 grid((unsigned)((max_pixels + kThreads - 1) / kThreads), p.num_views);
   k_backward<<<grid, kThreads, 0, s>>>(p);
 }

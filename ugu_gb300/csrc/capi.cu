@@ -74,7 +74,9 @@ struct Scratch {
   size_t tcounters_cap = 0;
   bool tiles_dirty = false;
   size_t list_min = size_t(1) << 22;  // capacity of the item / overflow lists
-  // backward: per-view target pointers
+  // backward: per-view target pointers, double projection table
+  double* proj64 = nullptr;  // 4 doubles per vertex of every view
+  size_t proj64_cap = 0;     // vertices
   const float** d_targets = nullptr;
   const float** h_targets = nullptr;  // pinned
   size_t targets_cap = 0;
@@ -172,6 +174,7 @@ void free_scratch(Scratch& s) {
   cudaFree(s.fid_scratch);
   cudaFree(s.tcounters);
   cudaFreeHost(s.h_tcounters);
+  cudaFree(s.proj64);
   cudaFree(s.d_targets);
   cudaFreeHost(s.h_targets);
   s = Scratch();
@@ -1244,7 +1247,8 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   if (o.diffuse_shading != 0)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
                      "backward differentiates the unshaded colour (diffuse_shading = kNone)");
-  int64_t max_px = 0;
+  int64_t max_px = 0, sum_v = 0;
+  int max_v = 0;
   for (int i = 0; i < n; ++i) {
     ugu_gpu_view v = views[i];
     if (!v.images.face_id || !targets[i])
@@ -1253,6 +1257,9 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     int rc = validate_view(ctx, v, true);
     if (rc) return rc;
     max_px = std::max(max_px, (int64_t)v.camera.width * v.camera.height);
+    const int nv = ctx->meshes[v.mesh].dev.num_vertices;
+    max_v = std::max(max_v, nv);
+    sum_v += nv;
   }
   Scratch& s = ctx->scratch;
   int rc = ensure_scratch(ctx, s, 0, (size_t)n, 1, 0);
@@ -1267,13 +1274,24 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     CK(ctx, cudaMallocHost(&s.h_targets, n * sizeof(float*)), "cudaMallocHost(targets)");
     s.targets_cap = n;
   }
+  if (grad_vertices && (size_t)sum_v > s.proj64_cap) {
+    cudaFree(s.proj64);
+    s.proj64 = nullptr;
+    s.proj64_cap = 0;
+    CK(ctx, cudaMalloc(&s.proj64, (size_t)sum_v * 4 * sizeof(double)),
+       "cudaMalloc(double projection table)");
+    s.proj64_cap = (size_t)sum_v;
+  }
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  int64_t proj_off = 0;
   for (int i = 0; i < n; ++i) {
     DevView& d = s.h_views[i];
     std::memset(&d, 0, sizeof(d));
     fill_cam(d.cam, views[i].camera);
     d.mesh = views[i].mesh;
     d.face_id = views[i].images.face_id;
+    d.proj_offset = proj_off;
+    proj_off += ctx->meshes[views[i].mesh].dev.num_vertices;
     s.h_targets[i] = targets[i];
   }
   CK(ctx, cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView), cudaMemcpyHostToDevice,
@@ -1294,11 +1312,12 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   p.grad_vertices = grad_vertices;
   p.loss = loss_out;
   p.bad_ids = &s.counters[0].pad;
+  p.proj64 = s.proj64;
   CK(ctx, cudaMemsetAsync(s.counters, 0, sizeof(DevCounters), ctx->stream),
      "cudaMemsetAsync(counters)");
-  launch_backward(p, max_px, ctx->stream);
+  launch_backward(p, max_px, max_v, ctx->stream);
   CK(ctx, cudaGetLastError(), "backward launch");
-  ctx->launches += 1;
+  ctx->launches += grad_vertices ? 2 : 1;
   CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, sizeof(DevCounters), cudaMemcpyDeviceToHost,
                           ctx->stream),
      "cudaMemcpyAsync(counters)");

@@ -149,10 +149,13 @@ struct BackwardParams {
   float* grad_vertices;         // V*3 (or NULL)
   float* loss;                  // one per view (or NULL)
   unsigned long long* bad_ids;  // counts face ids outside [-1, num_faces)
+  double* proj64;               // per view (DevView::proj_offset): x, y, z, 1/z per vertex
 };
 
-// Host-side launcher (backward.cu).
-void launch_backward(const BackwardParams& p, int64_t max_pixels, cudaStream_t s);
+// Host-side launcher (backward.cu): the double projection table (when
+// position gradients are asked for), then the per-pixel backward.
+void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices,
+                     cudaStream_t s);
 
 // Host-side launchers (tile.cu).  launch_bin enqueues projection, binning,
 // the offset scan and the gather (launch_size all but the gather, to learn
