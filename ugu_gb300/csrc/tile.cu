@@ -603,19 +603,20 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
   const int tlog = p.tile_log2;
   const int T = 1 << tlog;
   if (p.counters->dropped) return;  // entries were not written: the host retries
-  int cur_view = -1;
+  int v_begin = 0, v_end = 0;  // global tiles of the view in shared memory
   Region& R = sm.reg;
   for (;;) {
     if (tid == 0) sm.item = (int)atomicAdd(&p.counters->next_tile, 1u);
     __syncthreads();
     const int item = sm.item;
     if (item >= p.total_tiles) break;
-    const int v = find_view_by_tile(p, item);
-    if (v != cur_view) {
+    if (item < v_begin || item >= v_end) {
+      const int v = find_view_by_tile(p, item);
       copy_words(sm.view, p.views[v]);
       __syncthreads();
       copy_words(sm.mesh, p.meshes[sm.view.mesh]);
-      cur_view = v;
+      v_begin = p.views[v].tile_base;
+      v_end = v + 1 < p.num_views ? p.views[v + 1].tile_base : p.total_tiles;
     }
     const Cam& c = sm.view.cam;
     const int local = item - sm.view.tile_base;
@@ -629,7 +630,10 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
     const float4* proj = p.proj + sm.view.proj_offset;
     __syncthreads();
 
-    // Per-view constants of the back-face surrogate's error bound.
+    // Per-view constants of the back-face surrogate and its error bound.
+    // The surrogate's coefficients use 1/fx and 1/fy: one rounding more
+    // than a division, far inside the bound's 64-ulp margins.
+    const float rfx = 1.0f / c.fx, rfy = 1.0f / c.fy;
     const float Dx = (c.width + fabsf(c.cx)) / c.fx;
     const float Dy = (c.height + fabsf(c.cy)) / c.fy;
     const float Dmax = 1.0f + fmaxf(fabsf(c.cx), fabsf(c.width - 1 - c.cx)) / c.fx +
@@ -679,7 +683,7 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           const float G = (fabsf(C[0]) + fabsf(C[1]) + fabsf(C[2])) * fabsf(fn.x) +
                           (fabsf(C[3]) + fabsf(C[4]) + fabsf(C[5])) * fabsf(fn.y) +
                           (fabsf(C[6]) + fabsf(C[7]) + fabsf(C[8])) * fabsf(fn.z);
-          const float sa = g0 / c.fx, sb = g1 / c.fy;
+          const float sa = g0 * rfx, sb = g1 * rfy;
           const float sc = g2 - sa * c.cx - sb * c.cy;
           const float tol = kU64 * (G * (1.0f + Dx + Dy) + fabsf(sa) * (c.width + fabsf(c.cx)) +
                                     fabsf(sb) * (c.height + fabsf(c.cy)) + fabsf(g2)) +
