@@ -106,6 +106,8 @@ struct ugu_gpu_context {
   int num_sms = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // device-to-host copies of host-pointer renders
+  std::vector<cudaEvent_t> events;     // one per group of a host-pointer render, and one more
   std::string last_error;
   ugu_gpu_option opt{};
   MeshSlot meshes[kMaxMeshes];
@@ -320,11 +322,16 @@ int64_t tiles_of(const ugu_gpu_camera& c, int tlog) {
 }
 
 // Views split into launch groups: per view (the baseline), by z-buffer
-// pixels (global path) or all together (tiled path).
+// pixels (global path) or all together (tiled path).  Renders into host
+// buffers are cut into groups of at most kHostChunkPixels so that each
+// group's copy to the host overlaps the next group's kernels.
+constexpr int64_t kHostChunkPixels = int64_t(4) << 20;
+
 std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views,
-                               bool per_view) {
+                               bool per_view, bool host_outputs = false) {
   const ugu_gpu_tuning& t = ctx->tuning;
-  const int64_t limit = t.path == UGU_GPU_PATH_GLOBAL ? (int64_t)t.group_pixels : INT64_MAX;
+  int64_t limit = t.path == UGU_GPU_PATH_GLOBAL ? (int64_t)t.group_pixels : INT64_MAX;
+  if (host_outputs) limit = std::min(limit, kHostChunkPixels);
   std::vector<Group> g;
   Group cur{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   int64_t acc = 0;
@@ -560,22 +567,24 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   return p;
 }
 
-int enqueue_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
-                  int* kernels) {
-  int nk = 0;
-  for (size_t gi = 0; gi < groups.size(); ++gi) {
-    const Group& gr = groups[gi];
+// Enqueue one group's kernels (no synchronisation); returns how many.
+int enqueue_group(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) {
+  if (ctx->tuning.path != UGU_GPU_PATH_GLOBAL) {
     TileParams p = tile_params(ctx, s, gr, gi);
-    CK(ctx, cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream),
-       "cudaMemsetAsync(tile counters)");
+    cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream);
     launch_bin(p, gr.max_faces, ctx->num_sms * 8, ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
     launch_shade(p, ctx->stream);
-    nk += kBinKernels + 1 + (p.shade_blocks > 0 ? 1 : 0);
+    return kBinKernels + 1 + (p.shade_blocks > 0 ? 1 : 0);
   }
-  CK(ctx, cudaGetLastError(), "kernel launch");
-  *kernels = nk;
-  return UGU_GPU_OK;
+  RenderParams p = base_params(ctx, s);
+  p.views = s.d_views + gr.first;
+  p.num_views = gr.count;
+  p.counters = s.counters + gi;
+  launch_raster(p, gr.max_faces, ctx->num_sms, ctx->stream);
+  launch_tiles(p, ctx->num_sms * 8, ctx->stream);
+  launch_resolve(p, gr.max_pixels, ctx->stream);
+  return 3;
 }
 
 // Tiled path: count the (face, tile) entries of every group without
@@ -595,29 +604,6 @@ int size_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& group
   CK(ctx, cudaStreamSynchronize(ctx->stream), "sizing pass");
   for (size_t gi = 0; gi < groups.size(); ++gi) want_capacity(s, s.h_tcounters[gi]);
   return ensure_tiled(ctx, s, groups);
-}
-
-// Enqueue the kernels of every group (no synchronisation).
-int enqueue_groups(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
-                   const ugu_gpu_view* views, int* kernels) {
-  if (ctx->tuning.path != UGU_GPU_PATH_GLOBAL) return enqueue_tiled(ctx, s, groups, kernels);
-  RenderParams base = base_params(ctx, s);
-  int nk = 0;
-  for (size_t gi = 0; gi < groups.size(); ++gi) {
-    const Group& gr = groups[gi];
-    RenderParams p = base;
-    p.views = s.d_views + gr.first;
-    p.num_views = gr.count;
-    p.counters = s.counters + gi;
-    launch_raster(p, gr.max_faces, ctx->num_sms, ctx->stream);
-    launch_tiles(p, ctx->num_sms * 8, ctx->stream);
-    launch_resolve(p, gr.max_pixels, ctx->stream);
-    nk += 3;
-  }
-  (void)views;
-  CK(ctx, cudaGetLastError(), "kernel launch");
-  *kernels = nk;
-  return UGU_GPU_OK;
 }
 
 // Fill s.h_views for the views; host-pointer outputs get device staging.
@@ -677,14 +663,15 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
   }
 }
 
-int copy_back(ugu_gpu_context* ctx, const Scratch& s, int n, const ugu_gpu_view* views) {
-  for (int i = 0; i < n; ++i) {
+int copy_back(ugu_gpu_context* ctx, const Scratch& s, int first, int count,
+              const ugu_gpu_view* views, cudaStream_t stream) {
+  for (int i = first; i < first + count; ++i) {
     const DevView& d = s.h_views[i];
     const ugu_gpu_images& im = views[i].images;
     int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
     auto cp = [&](void* dst, const void* src, size_t bytes) -> int {
       if (!dst) return UGU_GPU_OK;
-      CK(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream),
+      CK(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream),
          "cudaMemcpyAsync(output)");
       return UGU_GPU_OK;
     };
@@ -747,15 +734,41 @@ int prepare_scratch(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& 
 }
 
 // Everything one render enqueues once its view table is on the device.
+// Everything one render enqueues once its view table is on the device.  With
+// host outputs, each group's copies run on the copy stream as soon as the
+// group's kernels are done, overlapping the next group's kernels; the
+// render stream then waits for the last copy.
 int enqueue_render(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
                    const ugu_gpu_view* views, int n, bool dev, int* kernels) {
   const bool global = ctx->tuning.path == UGU_GPU_PATH_GLOBAL;
   if (global)
     CK(ctx, cudaMemsetAsync(s.counters, 0, groups.size() * sizeof(DevCounters), ctx->stream),
        "cudaMemsetAsync(counters)");
-  int rc = enqueue_groups(ctx, s, groups, views, kernels);
-  if (rc) return rc;
-  if (!dev && (rc = copy_back(ctx, s, n, views))) return rc;
+  if (!dev) {
+    while (ctx->events.size() < groups.size() + 1) {
+      cudaEvent_t e;
+      CK(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+      ctx->events.push_back(e);
+    }
+  }
+  int nk = 0;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    nk += enqueue_group(ctx, s, groups[gi], gi);
+    if (!dev) {
+      CK(ctx, cudaEventRecord(ctx->events[gi], ctx->stream), "cudaEventRecord");
+      CK(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->events[gi], 0), "cudaStreamWaitEvent");
+      int rc = copy_back(ctx, s, groups[gi].first, groups[gi].count, views, ctx->copy_stream);
+      if (rc) return rc;
+    }
+  }
+  CK(ctx, cudaGetLastError(), "kernel launch");
+  *kernels = nk;
+  (void)n;
+  if (!dev) {
+    cudaEvent_t done = ctx->events[groups.size()];
+    CK(ctx, cudaEventRecord(done, ctx->copy_stream), "cudaEventRecord");
+    CK(ctx, cudaStreamWaitEvent(ctx->stream, done, 0), "cudaStreamWaitEvent");
+  }
   if (global)
     CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, groups.size() * sizeof(DevCounters),
                             cudaMemcpyDeviceToHost, ctx->stream),
@@ -776,7 +789,8 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
   const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
   if ((flags & UGU_GPU_ASYNC) && !dev)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "UGU_GPU_ASYNC needs device pointers");
-  std::vector<Group> groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0);
+  std::vector<Group> groups =
+      make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0, !dev);
   size_t out_bytes = 0;
   if (!dev)
     for (int i = 0; i < n; ++i)
@@ -840,11 +854,13 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->device = device;
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_meshes, kMaxMeshes * sizeof(DevMesh));
   if (e == cudaSuccess) e = cudaMemset(ctx->d_meshes, 0, kMaxMeshes * sizeof(DevMesh));
   if (e != cudaSuccess) {
     set_error(nullptr, UGU_GPU_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     cudaFree(ctx->d_meshes);
     delete ctx;
     return UGU_GPU_ERR_CUDA;
@@ -878,6 +894,8 @@ int ugu_gpu_destroy(ugu_gpu_context* ctx) {
   free_scratch(ctx->scratch);
   cudaFree(ctx->d_meshes);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+  for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
   delete ctx;
   return UGU_GPU_OK;
 }
