@@ -152,6 +152,47 @@ def test_batched_views_two_meshes(ctx, oracle_lib, torch_cuda, flags, path):
         compare(ref, got, f"view{i}")
 
 
+def test_host_outputs_span_copy_chunks(ctx, torch_cuda):
+    """Host-buffer renders are cut into chunks of at most 4M pixels whose
+    copies overlap the next chunk's kernels: a batch of 8.3M pixels (three
+    chunks) into host buffers equals the same batch into device buffers,
+    including a view that asks for colour without face ids."""
+    torch = torch_cuda
+    m = scenes.icosphere_textured(5, 256)
+    cams = scenes.ring_cameras(5, 3.0, [(1920, 1080), (640, 480), (1920, 1080), (1920, 1080),
+                                        (1280, 720)])
+    ctx.check(ctx.set_mesh(0, m))
+    from gpu_helpers import to_option
+    ctx.check(ctx.set_option(to_option(adv.option(1, 1, 1, 0, True))))
+    outs = [gpu_helpers_outputs(k) for k in range(len(cams))]
+    want, dviews = [], []
+    for cam, o in zip(cams, outs):
+        t, v = device_views(torch, [cam], [0], outputs=o)
+        want += t
+        dviews += v
+    ctx.check(ctx.render_views(dviews, capi.DEVICE_POINTERS))
+    torch.cuda.synchronize()
+    from gpu_helpers import host_images
+    got, hviews = [], []
+    for cam, o in zip(cams, outs):
+        h, im = host_images(cam, o)
+        v = capi.View()
+        v.mesh = 0
+        v.camera = capi.camera_struct(cam)
+        v.images = im
+        got.append(h)
+        hviews.append(v)
+    ctx.check(ctx.render_views(hviews, 0))
+    for i in range(len(cams)):
+        for k, t in want[i].items():
+            assert np.array_equal(t.cpu().numpy(), got[i][k]), (i, k)
+
+
+def gpu_helpers_outputs(k):
+    full = ("color", "depth", "normal", "mask", "face_id")
+    return ("color", "normal") if k == 3 else full
+
+
 def test_graph_plan_replays(ctx, oracle_lib, torch_cuda):
     torch = torch_cuda
     m, cams = _ring(4, 6)
