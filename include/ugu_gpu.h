@@ -267,7 +267,10 @@ typedef struct {
 /* Device arrays of a mesh slot in the layout above (pointers owned by the
  * context, valid until the slot is set again).  Lets a caller update the
  * uploaded parameters in place, e.g. a gradient step on the float texels.
- * No counterpart in the reference. */
+ * Values (positions, normals, colours, uvs, texels) may change in place;
+ * the index arrays may not (the slot keeps derived copies of them): upload
+ * new connectivity with ugu_gpu_set_mesh.  No counterpart in the
+ * reference. */
 UGU_GPU_API int ugu_gpu_get_device_mesh(ugu_gpu_context* ctx, int32_t slot,
                                         ugu_gpu_device_mesh* out);
 

@@ -182,13 +182,11 @@ void free_scratch(Scratch& s) {
   s = Scratch();
 }
 
-// The faces sorted by the 30-bit Morton code of their centroid within the
-// vertices' bounding box [lo, hi].  The tiled path bins faces in this order
-// so that a binning block's faces lie close together on screen whatever
-// the mesh's own face order; results do not depend on it.
-std::vector<int32_t> morton_order(const ugu_gpu_mesh* m, const float lo[3], const float hi[3]) {
-  const int64_t F = m->num_faces;
-  std::vector<std::pair<uint32_t, int32_t>> key(F);
+// Indices 0..n-1 sorted by the 30-bit Morton code of point(i) within the
+// box [lo, hi] (stable: equal codes keep their order).
+template <typename Point>
+std::vector<int32_t> morton_sort(int64_t n, const float lo[3], const float hi[3], Point point) {
+  std::vector<std::pair<uint32_t, int32_t>> key(n);
   auto spread = [](uint32_t x) {  // 10 bits -> every third bit of 30
     x &= 1023u;
     x = (x | (x << 16)) & 0x030000FFu;
@@ -197,24 +195,65 @@ std::vector<int32_t> morton_order(const ugu_gpu_mesh* m, const float lo[3], cons
     x = (x | (x << 2)) & 0x09249249u;
     return x;
   };
-  for (int64_t f = 0; f < F; ++f) {
+  for (int64_t i = 0; i < n; ++i) {
+    double c[3];
+    point(i, c);
     uint32_t q[3];
     for (int k = 0; k < 3; ++k) {
-      double c = 0.0;
-      for (int j = 0; j < 3; ++j) c += m->vertices[3 * (int64_t)m->vertex_indices[3 * f + j] + k];
       const double ext = (double)hi[k] - (double)lo[k];
-      double u = ext > 0.0 ? (c / 3.0 - lo[k]) / ext : 0.0;
+      double u = ext > 0.0 ? (c[k] - lo[k]) / ext : 0.0;
       if (!(u >= 0.0)) u = 0.0;  // NaN as well
       if (u > 1.0) u = 1.0;
       q[k] = (uint32_t)(u * 1023.0);
     }
-    key[f] = {spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2), (int32_t)f};
+    key[i] = {spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2), (int32_t)i};
   }
   std::stable_sort(key.begin(), key.end(),
                    [](const auto& a, const auto& b) { return a.first < b.first; });
-  std::vector<int32_t> order(F);
-  for (int64_t f = 0; f < F; ++f) order[f] = key[f].second;
+  std::vector<int32_t> order(n);
+  for (int64_t i = 0; i < n; ++i) order[i] = key[i].second;
   return order;
+}
+
+// The tiled path's spatial orders (results never depend on them): faces by
+// centroid, vertices by position.  Projected vertices are stored by vertex
+// rank, and two index copies refer to ranks: one in face order (shading),
+// one in the faces' Morton order (binning and tile setup), so that a block's
+// neighbouring faces and their vertices sit close together in memory.
+struct SpatialOrder {
+  std::vector<int32_t> face_order, vertex_order;
+  std::vector<int4> vidx_ranked, vidx_morton;
+  std::vector<float4> fnormals_morton;
+};
+
+SpatialOrder spatial_order(const ugu_gpu_mesh* m, const float lo[3], const float hi[3]) {
+  const int64_t F = m->num_faces, V = m->num_vertices;
+  const float* P = m->vertices;
+  const int32_t* I = m->vertex_indices;
+  SpatialOrder o;
+  o.face_order = morton_sort(F, lo, hi, [&](int64_t f, double* c) {
+    for (int k = 0; k < 3; ++k)
+      c[k] = (P[3 * (int64_t)I[3 * f] + k] + P[3 * (int64_t)I[3 * f + 1] + k] +
+              (double)P[3 * (int64_t)I[3 * f + 2] + k]) / 3.0;
+  });
+  o.vertex_order = morton_sort(V, lo, hi, [&](int64_t v, double* c) {
+    for (int k = 0; k < 3; ++k) c[k] = P[3 * v + k];
+  });
+  std::vector<int32_t> rank(V);
+  for (int64_t r = 0; r < V; ++r) rank[o.vertex_order[r]] = (int32_t)r;
+  o.vidx_ranked.resize(F);
+  o.vidx_morton.resize(F);
+  for (int64_t f = 0; f < F; ++f)
+    o.vidx_ranked[f] = make_int4(rank[I[3 * f]], rank[I[3 * f + 1]], rank[I[3 * f + 2]], 0);
+  for (int64_t i = 0; i < F; ++i) o.vidx_morton[i] = o.vidx_ranked[o.face_order[i]];
+  if (m->face_normals) {
+    o.fnormals_morton.resize(F);
+    for (int64_t i = 0; i < F; ++i) {
+      const float* n = m->face_normals + 3 * (int64_t)o.face_order[i];
+      o.fnormals_morton[i] = make_float4(n[0], n[1], n[2], 0.0f);
+    }
+  }
+  return o;
 }
 
 template <typename T>
@@ -970,7 +1009,14 @@ int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) 
   d.num_faces = m->num_faces;
   if ((rc = upload(ctx, s, v4, &d.vertices))) return rc;
   if ((rc = upload(ctx, s, pad3i(m->vertex_indices), &d.vidx))) return rc;
-  if ((rc = upload(ctx, s, morton_order(m, lo, hi), &d.order))) return rc;
+  {
+    SpatialOrder so = spatial_order(m, lo, hi);
+    if ((rc = upload(ctx, s, so.face_order, &d.order))) return rc;
+    if ((rc = upload(ctx, s, so.vertex_order, &d.vorder))) return rc;
+    if ((rc = upload(ctx, s, so.vidx_ranked, &d.vidx_ranked))) return rc;
+    if ((rc = upload(ctx, s, so.vidx_morton, &d.vidx_morton))) return rc;
+    if ((rc = upload(ctx, s, so.fnormals_morton, &d.fnormals_morton))) return rc;
+  }
   if (m->face_normals && F > 0) {
     if ((rc = upload(ctx, s, pad3f(m->face_normals, F), &d.fnormals))) return rc;
     s.has_fnormals = true;

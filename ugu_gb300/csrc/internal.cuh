@@ -37,7 +37,16 @@ struct DevMesh {
   const int4* uvidx;
   const int32_t* mat_ids;
   const DevTexture* textures;
-  const int32_t* order;  // faces in 3D Morton order of their centroids (binning order)
+  // Tiled path only (results never depend on them): the faces in 3D Morton
+  // order of their centroids (the binning order), the vertices in Morton
+  // order of their positions (the order of the projected-vertex table), the
+  // vertex indices as ranks in that order, per face and per Morton face, and
+  // the face normals per Morton face.
+  const int32_t* order;
+  const int32_t* vorder;
+  const int4* vidx_ranked;
+  const int4* vidx_morton;
+  const float4* fnormals_morton;
 };
 
 struct DevView {
@@ -113,8 +122,9 @@ struct TileCounters {
 // run the entries of one block for one (tile, draw class); per global tile
 // t, k_gather then copies the entries of the faces drawn first to
 // [tile_off[t], tile_lo[t]) and those drawn last to
-// [tile_lo[t], tile_off[t + 1]).  An entry is (face id, bit pattern of a
-// lower bound of every depth the face can produce).
+// [tile_lo[t], tile_off[t + 1]).  An entry is (the face's number in the
+// binning order DevMesh::order, bit pattern of a lower bound of every depth
+// the face can produce).
 struct TileParams {
   const DevMesh* meshes;
   const DevView* views;

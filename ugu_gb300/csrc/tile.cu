@@ -99,7 +99,7 @@ __device__ __forceinline__ void copy_words(T& dst, const T& src) {
   for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += blockDim.x) b[i] = a[i];
 }
 
-// Loop A for every vertex of one view (blockIdx.y).
+// Loop A for every vertex of one view (blockIdx.y), stored by vertex rank.
 __global__ void __launch_bounds__(kBinThreads) k_proj(TileParams p) {
   __shared__ Cam sc;
   __shared__ int mesh, nv;
@@ -113,7 +113,8 @@ __global__ void __launch_bounds__(kBinThreads) k_proj(TileParams p) {
   __syncthreads();
   const int i = blockIdx.x * kBinThreads + threadIdx.x;
   if (i >= nv) return;
-  const float4 a = __ldg(&p.meshes[mesh].vertices[i]);
+  const int* vorder = p.meshes[mesh].vorder;  // the table is in vertex-rank order
+  const float4 a = __ldg(&p.meshes[mesh].vertices[vorder ? __ldg(&vorder[i]) : i]);
   const float3 q = project(sc, a.x, a.y, a.z);
   p.proj[off + i] = make_float4(q.x, q.y, q.z, 0.0f);
 }
@@ -149,18 +150,16 @@ __device__ __forceinline__ int agg_slot(BinSmem& sb, int t) {
 // The screen tiles of one face: the per-face culls of Loop B from the
 // projected-vertex table, then the tile range of its pixel bbox.
 struct FaceBins {
-  int f, n, tx0, ty0, ntx, cls;
+  int i, n, tx0, ty0, ntx, cls;  // i: the face's number in the binning order
   float zlb;
 };
 
-// Face number i of the binning order (see DevMesh::order).
+// Face number i of the binning order (DevMesh::order).
 __device__ __forceinline__ FaceBins bin_face(const TileParams& p, const BinSmem& sb, int i) {
-  FaceBins b{-1, 0, 0, 0, 1, 0, -1.0f};
+  FaceBins b{i, 0, 0, 0, 1, 0, -1.0f};
   if (i >= sb.mesh.num_faces) return b;
-  const int f = sb.mesh.order ? __ldg(&sb.mesh.order[i]) : i;
-  b.f = f;
   FaceSetup s;
-  if (!setup_proj(p.proj + sb.view.proj_offset, sb.mesh.vidx, f, sb.view.cam, s) ||
+  if (!setup_proj(p.proj + sb.view.proj_offset, sb.mesh.vidx_morton, i, sb.view.cam, s) ||
       s.x1 < s.x0 || s.y1 < s.y0)
     return b;
   const int ts = p.tile_log2;
@@ -327,7 +326,7 @@ __global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
 #pragma unroll
   for (int u = 0; u < kBinFaces; ++u) {
     const FaceBins& b = fb[u];
-    const int2 e = make_int2(b.f, __float_as_int(b.zlb));
+    const int2 e = make_int2(b.i, __float_as_int(b.zlb));
     if (b.n <= kAggPerFace) {
 #pragma unroll
       for (int k = 0; k < kAggPerFace; ++k) {
@@ -667,15 +666,15 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           const float zlb = __int_as_float(e.y);
           R.cnt[j] = 0;
           if (zlb > zmax) continue;  // behind every key of a covered tile: cannot win
-          const int f = e.x;
+          const int f = __ldg(&sm.mesh.order[e.x]);  // the entry holds the binning number
           FaceSetup s;
-          setup_proj(proj, sm.mesh.vidx, f, c, s);  // succeeded in k_fill: same arithmetic
+          setup_proj(proj, sm.mesh.vidx_morton, e.x, c, s);  // succeeded in k_bin: same arithmetic
           const int bx0 = max(s.x0, tx0), bx1 = min(s.x1, tx0 + tw - 1);
           const int by0 = max(s.y0, ty0), by1 = min(s.y1, ty0 + th - 1);
           const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;
           if (bw <= 0 || bh <= 0) continue;
           // back-face surrogate: s(x, y) = (C^T n) . ((x-cx)/fx, (y-cy)/fy, 1)
-          const float4 fn = __ldg(&sm.mesh.fnormals[f]);
+          const float4 fn = __ldg(&sm.mesh.fnormals_morton[e.x]);
           const float* C = c.C;
           const float g0 = C[0] * fn.x + C[3] * fn.y + C[6] * fn.z;
           const float g1 = C[1] * fn.x + C[4] * fn.y + C[7] * fn.z;
@@ -763,7 +762,7 @@ __global__ void __launch_bounds__(256) k_shade(TileParams p) {
     if (fid > 0) {
       const int y = (int)(pix / W), x = (int)(pix - (int64_t)y * W);
       FaceSetup s;
-      const int4 vi = __ldg(&M.vidx[fid]);
+      const int4 vi = __ldg(&M.vidx_ranked[fid]);
       const float4 a = __ldg(&proj[vi.x]);
       const float4 b = __ldg(&proj[vi.y]);
       const float4 d = __ldg(&proj[vi.z]);
