@@ -443,13 +443,21 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
 // at a time.
 struct Region {
   float4 r0[kChunk];  // v0.x v0.y v1.x v1.y
-  float4 r1[kChunk];  // v2.x v2.y area fid-bits
-  float4 r2[kChunk];  // v0.z v1.z v2.z -
+  float4 r1[kChunk];  // v2.x v2.y area box (pack_box)
+  float4 r2[kChunk];  // v0.z v1.z v2.z fid-bits
   float4 r3[kChunk];  // back-face sign surrogate: sa sb sc tolerance
   float4 r5[kChunk];  // depth pre-test: z1 z2, z0 z2, z0 z1, |area| z0 z1 z2 (1 - 2^-16)
-  int4 r4[kChunk];    // bbox-in-tile x0 y0 width, ceil(2^20 / width)
   int cnt[kChunk];    // bbox-in-tile pixels, 0 when the face is skipped
 };
+
+// A face's bbox-in-tile in 32 bits: tile-local x0 and y0, width - 1 (5 bits
+// each) and m = ceil(2^16 / width) (17 bits), so that row = (k * m) >> 16
+// for every pixel number k < width * height <= 1024 of the box.
+__device__ __forceinline__ float pack_box(int x0, int y0, int w) {
+  const unsigned m = (65536u + (unsigned)w - 1u) / (unsigned)w;
+  return __uint_as_float((unsigned)x0 | ((unsigned)y0 << 5) | ((unsigned)(w - 1) << 10) |
+                         (m << 15));
+}
 
 constexpr int kQueue = 64;  // covered candidates a warp holds before its depth pass
 
@@ -506,7 +514,7 @@ __device__ __forceinline__ void depth_test(TileSmem& sm, const Region& R, const 
     atomicAdd(&p.counters->special, 1ull);
     return;
   }
-  const unsigned long long key = make_key(z, __float_as_int(r1.w), bf);
+  const unsigned long long key = make_key(z, __float_as_int(r2.w), bf);
   if (key < *(volatile unsigned long long*)kp) atomicMin(kp, key);
 }
 
@@ -545,12 +553,14 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const
           if (pre[q + step] <= k) q += step;
         const int jj = base + q;
         const int local = k - pre[q];
-        const int4 r4 = R.r4[jj];
-        const int yy = (local * r4.w) >> 20;
-        const int x = r4.x + local - yy * r4.z, y = r4.y + yy;
         const float4 r0 = R.r0[jj];
         const float4 r1 = R.r1[jj];
         const float4 r3 = R.r3[jj];
+        const unsigned box = __float_as_uint(r1.w);
+        const int bw = (int)((box >> 10) & 31u) + 1;
+        const int yy = (local * (int)(box >> 15)) >> 16;
+        const int x = tx0 + (int)(box & 31u) + local - yy * bw;
+        const int y = ty0 + (int)((box >> 5) & 31u) + yy;
         // sign of face_normal . ray_w: the affine surrogate decides unless
         // it is within its error bound of zero; then the reference's ray.
         const float sv = fmaf(r3.x, (float)x, fmaf(r3.y, (float)y, r3.z));
@@ -560,7 +570,7 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const
         else if (sv < -r3.w)
           bf = false;
         else
-          bf = backface_exact(sm.mesh, c, __float_as_int(r1.w), x, y);
+          bf = backface_exact(sm.mesh, c, __float_as_int(R.r2[jj].w), x, y);
         FaceSetup s;
         s.v0.x = r0.x;
         s.v0.y = r0.y;
@@ -695,11 +705,10 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           const float aP = pre_ok ? fabsf(s.area) * (z0 * z1 * z2) * 0.99998474f
                                   : __int_as_float(0x7fc00000);
           R.r0[j] = make_float4(s.v0.x, s.v0.y, s.v1.x, s.v1.y);
-          R.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, __int_as_float(f));
-          R.r2[j] = make_float4(z0, z1, z2, 0.0f);
+          R.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, pack_box(bx0 - tx0, by0 - ty0, bw));
+          R.r2[j] = make_float4(z0, z1, z2, __int_as_float(f));
           R.r3[j] = make_float4(sa, sb, sc, tol);
           R.r5[j] = make_float4(z1 * z2, z0 * z2, z0 * z1, aP);
-          R.r4[j] = make_int4(bx0, by0, bw, ((1 << 20) + bw - 1) / bw);
           R.cnt[j] = bw * bh;
         }
         __syncthreads();
