@@ -375,7 +375,8 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
     """The large forward+backward: icosphere-8 (1,310,720 faces, radial noise
     0.01), a 4096^2 float texture, 256 Fibonacci-sphere cameras at distance
     3, 1280x720, fx = 1000; 20 iterations of texture gradient descent
-    (texel -= 0.1 * dL/dtexel), each a batched forward (face_id + float
+    (texel -= 0.1 * dL/dtexel with L the per-view L2 sum averaged over the
+    views), each a batched forward (face_id + float
     colour) and a backward against fixed target images (a second seeded
     texture).  The texels are updated in place in the mesh slot's device
     copy (ugu_gpu_get_device_mesh)."""
@@ -388,9 +389,12 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
     m = scenes.icosphere(8, 1.0, 0.01, seed=1)
     scenes.calc_normals(m)
     scenes.with_texture(m, 4096, seed=3, f32=True)
+    # float texels in [0, 1], as multi-view texturing optimises them (a step
+    # of 0.1 on 0..255 values overshoots and diverges)
+    m.textures_f32 = [m.textures_f32[0] / np.float32(255.0)]
     tm = m.copy()
     tm.textures = [scenes.random_u8(5, m.textures[0].shape)]
-    tm.textures_f32 = [tm.textures[0].astype(np.float32)]
+    tm.textures_f32 = [tm.textures[0].astype(np.float32) / np.float32(255.0)]
     cams = scenes.fibonacci_cameras(n_views, 3.0, 1280, 720, 1000.0)
     ctx = Context(0)
     ctx.check(ctx.set_option(RendererCpuOption(diffuse_color=1, interp=1, shading_normal=1,
@@ -438,8 +442,9 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
         loss.zero_()
         ctx.check(ctx.backward(fviews, tptr, grad.data_ptr(), None, None, loss.data_ptr(),
                                capi.DEVICE_POINTERS | capi.ASYNC))
-        tex.add_(grad, alpha=-lr)
-        losses.append(loss.sum())
+        # L = mean over views of the per-pixel L2 sum: dL/dtexel = grad / n_views
+        tex.add_(grad, alpha=-lr / n_views)
+        losses.append(loss.sum() / n_views)
     e1.record(stream)
     ctx.check(ctx.synchronize())
     ms = e0.elapsed_time(e1)
@@ -452,7 +457,8 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
         "unit": "views/s", "n_gpus": 1, "steps": iters, "warmup": 0,
         "ms_per_step": ms / iters, "gpix_per_s": iters * px / (ms / 1e3) / 1e9,
         "config": {"workload": "texdescent256_icosphere8_tex4096_f32_1280x720",
-                   "views": n_views, "iterations": iters, "lr": lr, "faces": m.num_faces},
+                   "views": n_views, "iterations": iters, "lr": lr, "faces": m.num_faces,
+                   "texels": "float32 in [0, 1]"},
         "loss_first": losses[0], "loss_last": losses[-1], "setup_s": setup_s}), flush=True)
 
 
