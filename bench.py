@@ -432,6 +432,18 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
     plan = ctx.plan_create(fviews, capi.DEVICE_POINTERS)
     tptr = [x["color_f32"].data_ptr() for x in tgt]
     setup_s = time.perf_counter() - t_setup
+    # warm-up iterations run every kernel of a step (the first use of each
+    # loads its module) and leave the texels unchanged
+    warm = max(3, args.warmup)
+    for _ in range(warm):
+        ctx.check(plan.launch())
+        grad.zero_()
+        loss.zero_()
+        ctx.check(ctx.backward(fviews, tptr, grad.data_ptr(), None, None, loss.data_ptr(),
+                               capi.DEVICE_POINTERS | capi.ASYNC))
+        tex.add_(grad, alpha=0.0)
+        loss.sum() / n_views
+    ctx.check(ctx.synchronize())
     losses = []
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -454,7 +466,7 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
     ctx.close()
     print(json.dumps({
         "metric": "views/s (forward+backward)", "value": iters * n_views / (ms / 1e3),
-        "unit": "views/s", "n_gpus": 1, "steps": iters, "warmup": 0,
+        "unit": "views/s", "n_gpus": 1, "steps": iters, "warmup": warm,
         "ms_per_step": ms / iters, "gpix_per_s": iters * px / (ms / 1e3) / 1e9,
         "config": {"workload": "texdescent256_icosphere8_tex4096_f32_1280x720",
                    "views": n_views, "iterations": iters, "lr": lr, "faces": m.num_faces,
