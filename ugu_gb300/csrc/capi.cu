@@ -67,8 +67,6 @@ struct Scratch {
   size_t runs_min = 0;
   float4* proj = nullptr;
   size_t proj_cap = 0;
-  int32_t* fid_scratch = nullptr;  // face ids of shaded views that do not output them
-  size_t fid_cap = 0;
   TileCounters* tcounters = nullptr;
   TileCounters* h_tcounters = nullptr;  // pinned
   size_t tcounters_cap = 0;
@@ -90,8 +88,6 @@ struct Group {
   int64_t faces;     // tiled path: faces summed over the group's views
   int64_t vertices;  // tiled path: vertices summed over the group's views
   int max_vertices;
-  int64_t shade_blocks;  // tiled path: blocks of the shading grid
-  int64_t fid_scratch;   // tiled path: pixels needing a scratch face id
 };
 
 }  // namespace
@@ -173,7 +169,6 @@ void free_scratch(Scratch& s) {
   cudaFree(s.entries);
   cudaFree(s.runs);
   cudaFree(s.proj);
-  cudaFree(s.fid_scratch);
   cudaFree(s.tcounters);
   cudaFreeHost(s.h_tcounters);
   cudaFree(s.proj64);
@@ -372,14 +367,14 @@ std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* 
   int64_t limit = t.path == UGU_GPU_PATH_GLOBAL ? (int64_t)t.group_pixels : INT64_MAX;
   if (host_outputs) limit = std::min(limit, kHostChunkPixels);
   std::vector<Group> g;
-  Group cur{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  Group cur{0, 0, 0, 0, 0, 0, 0, 0};
   int64_t acc = 0;
   for (int i = 0; i < n; ++i) {
     int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
     bool full = cur.count > 0 && (per_view || acc + px > limit);
     if (full) {
       g.push_back(cur);
-      cur = Group{i, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      cur = Group{i, 0, 0, 0, 0, 0, 0, 0};
       acc = 0;
     }
     const int F = ctx->meshes[views[i].mesh].dev.num_faces;
@@ -392,9 +387,6 @@ std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* 
     cur.tiles += tiles_of(views[i].camera, t.tile_log2);
     cur.faces += F;
     cur.vertices += V;
-    const ugu_gpu_images& im = views[i].images;
-    cur.shade_blocks += (px + kShadePixels - 1) / kShadePixels;
-    if ((im.color || im.normal || im.color_f32) && !im.face_id) cur.fid_scratch += px;
   }
   if (cur.count) g.push_back(cur);
   return g;
@@ -412,19 +404,11 @@ int64_t group_key_count(const std::vector<Group>& groups, const ugu_gpu_view* vi
 }
 
 int ensure_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups) {
-  size_t tiles = 0, verts = 0, faces = 0, fids = 0;
+  size_t tiles = 0, verts = 0, faces = 0;
   for (const Group& g : groups) {
     tiles = std::max(tiles, (size_t)g.tiles);
     verts = std::max(verts, (size_t)g.vertices);
     faces = std::max(faces, (size_t)g.faces);
-    fids = std::max(fids, (size_t)g.fid_scratch);
-  }
-  if (fids > s.fid_cap) {
-    cudaFree(s.fid_scratch);
-    s.fid_scratch = nullptr;
-    s.fid_cap = 0;
-    CK(ctx, cudaMalloc(&s.fid_scratch, fids * sizeof(int32_t)), "cudaMalloc(face id scratch)");
-    s.fid_cap = fids;
   }
   if (tiles > s.tiles_cap) {
     cudaFree(s.tile_count);
@@ -602,7 +586,6 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.staged = s.entries + s.entries_cap;
   p.runs = s.runs;
   p.counters = s.tcounters + gi;
-  p.shade_blocks = (int32_t)gr.shade_blocks;
   return p;
 }
 
@@ -613,8 +596,7 @@ int enqueue_group(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) 
     cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream);
     launch_bin(p, gr.max_faces, ctx->num_sms * 8, ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
-    launch_shade(p, ctx->stream);
-    return kBinKernels + 1 + (p.shade_blocks > 0 ? 1 : 0);
+    return kBinKernels + 1;
   }
   RenderParams p = base_params(ctx, s);
   p.views = s.d_views + gr.first;
@@ -651,7 +633,7 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
   size_t off = 0;
   const int tlog = ctx->tuning.tile_log2;
   for (const Group& gr : groups) {
-    int64_t key_off = 0, tile_base = 0, proj_off = 0, shade_block = 0, fid_off = 0;
+    int64_t key_off = 0, tile_base = 0, proj_off = 0;
     for (int i = gr.first; i < gr.first + gr.count; ++i) {
       const ugu_gpu_view& v = views[i];
       DevView& d = s.h_views[i];
@@ -690,14 +672,7 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
         if (v.images.face_id) d.face_id = reinterpret_cast<int32_t*>(take(4 * px));
         if (v.images.color_f32) d.color_f32 = reinterpret_cast<float*>(take(12 * px));
       }
-      // tiled path: k_shade reads the face ids k_tile wrote
-      d.shade_block = (int32_t)shade_block;
-      shade_block += (px + kShadePixels - 1) / kShadePixels;
-      if ((d.color || d.normal || d.color_f32) && !d.face_id &&
-          ctx->tuning.path != UGU_GPU_PATH_GLOBAL) {
-        d.face_id = s.fid_scratch + fid_off;
-        fid_off += px;
-      }
+
     }
   }
 }

@@ -57,8 +57,7 @@ struct DevView {
   int64_t proj_offset; // tiled path: first projected vertex of this view
   int32_t tile_base;   // tiled path: first global tile of this view
   float split_z;       // tiled path: faces wholly deeper than this are drawn last
-  int32_t shade_block; // tiled path: first block of this view in the shading grid
-  int32_t pad_;
+  int64_t pad_;
   uint8_t* color;
   float* depth;
   float* normal;
@@ -145,7 +144,6 @@ struct TileParams {
   int4* runs;           // (tile, draw class, first staged entry, count)
   int2* entries;        // entries in tile order
   TileCounters* counters;
-  int32_t shade_blocks;  // blocks of the shading grid (all views)
 };
 
 struct BackwardParams {
@@ -170,12 +168,10 @@ void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertic
 // Host-side launchers (tile.cu).  launch_bin enqueues projection, binning,
 // the offset scan and the gather (launch_size all but the gather, to learn
 // a render's entry and run counts); launch_tile the per-tile raster and
-// launch_shade the per-pixel shading.
+// resolve.
 void launch_bin(const TileParams& p, int max_faces, int gather_blocks, cudaStream_t s);
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
-void launch_shade(const TileParams& p, cudaStream_t s);
-constexpr int kShadePixels = 1024;  // pixels per shading block
 int tile_kernel_blocks_per_sm();
 int bin_kernel_blocks_per_sm();
 constexpr int kBinKernels = 4;

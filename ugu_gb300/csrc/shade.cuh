@@ -91,10 +91,15 @@ __device__ __forceinline__ void shade_face_pixel(const ShadeOpts& p, const DevMe
       float lu = fsub(fx, (float)x0);
       float lv = fsub(fy, (float)y0);
       float t00[3], t10[3], t01[3], t11[3];
-      fetch_texel(t, texel_index(y0, x0, t.width, t.height), t00);
-      fetch_texel(t, texel_index(y0, (int64_t)x0 + 1, t.width, t.height), t10);
-      fetch_texel(t, texel_index((int64_t)y0 + 1, x0, t.width, t.height), t01);
-      fetch_texel(t, texel_index((int64_t)y0 + 1, (int64_t)x0 + 1, t.width, t.height), t11);
+      // texel_index of the four taps: one linear address and its neighbours,
+      // each clamped to the allocation on its own
+      const int64_t n = (int64_t)t.width * t.height;
+      const int64_t i00 = (int64_t)y0 * t.width + x0;
+      auto clampi = [n](int64_t i) { return i < 0 ? (int64_t)0 : (i >= n ? n - 1 : i); };
+      fetch_texel(t, clampi(i00), t00);
+      fetch_texel(t, clampi(i00 + 1), t10);
+      fetch_texel(t, clampi(i00 + t.width), t01);
+      fetch_texel(t, clampi(i00 + t.width + 1), t11);
       const float a00 = fmul(fsub(1.0f, lu), fsub(1.0f, lv));
       const float a10 = fmul(lu, fsub(1.0f, lv));
       const float a01 = fmul(fsub(1.0f, lu), lv);

@@ -19,8 +19,8 @@
 //            coverage (Loop B's pixel test), queue the covered ones and run
 //            their z-test 32 at a time into a shared-memory z-buffer of
 //            64-bit (depth bits << 32 | face id << 1 | back-face bit) keys
-//            with atomicMin, then write Loop C's depth, face id and mask.
-//   k_shade  Loop C's shading (rasterizer.cc:254-299), one thread per pixel.
+//            with atomicMin, then run Loop C (rasterizer.cc:244-301) for the
+//            tile's pixels: depth, face id, mask and the shading.
 //
 // A face whose depth lower bound lies behind the view's split depth (the
 // camera depth of the mesh's bounding-box centre) is drawn last, and skipped
@@ -41,11 +41,14 @@ constexpr int kScanThreads = 1024;
 #define UGU_TILE_THREADS 128
 #endif
 #ifndef UGU_TILE_BLOCKS
-#define UGU_TILE_BLOCKS 8
+#define UGU_TILE_BLOCKS 7
 #endif
 constexpr int kTileThreads = UGU_TILE_THREADS;  // one tile per block
 constexpr int kWarps = kTileThreads / 32;
-constexpr int kChunk = kTileThreads;  // faces set up in shared memory at a time
+#ifndef UGU_TILE_CHUNK
+#define UGU_TILE_CHUNK UGU_TILE_THREADS
+#endif
+constexpr int kChunk = UGU_TILE_CHUNK;  // faces set up in shared memory at a time
 static_assert(kChunk <= 256, "queue entries hold an 8-bit face slot");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kBinFaces = 4;     // faces per binning thread
@@ -671,6 +674,7 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
       const int eb = phase ? e1 : e0, ee = phase ? e2 : e1;
       for (int cs = eb; cs < ee; cs += kChunk) {
         const int m = min(kChunk, ee - cs);
+#pragma unroll 2
         for (int j = tid; j < m; j += kTileThreads) {
           const int2 e = p.entries[cs + j];
           const float zlb = __int_as_float(e.y);
@@ -717,7 +721,7 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
       }
     }
 
-    // Loop C's z-test outputs (rasterizer.cc:244-262); shading is k_shade's.
+    // Loop C (rasterizer.cc:244-301) for the tile's pixels.
     const DevView& V = sm.view;
     const int W = c.width;
     for (int i = tid; i < T * T; i += kTileThreads) {
@@ -736,66 +740,42 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
       if (V.depth) V.depth[pix] = depth;
       if (V.face_id) V.face_id[pix] = fid;
       if (V.mask) V.mask[pix] = mask;
+      // Loop C's shading (rasterizer.cc:254-299)
+      if (V.color || V.normal || V.color_f32) {
+        Shaded sh;
+        sh.c[0] = sh.c[1] = sh.c[2] = 0;
+        sh.cf[0] = sh.cf[1] = sh.cf[2] = 0.0f;
+        sh.n[0] = sh.n[1] = sh.n[2] = 0.0f;
+        if (fid > 0) {
+          FaceSetup s;
+          const int4 vi = __ldg(&sm.mesh.vidx_ranked[fid]);
+          const float4 a = __ldg(&proj[vi.x]);
+          const float4 b = __ldg(&proj[vi.y]);
+          const float4 d = __ldg(&proj[vi.z]);
+          s.v0 = make_float3(a.x, a.y, a.z);
+          s.v1 = make_float3(b.x, b.y, b.z);
+          s.v2 = make_float3(d.x, d.y, d.z);
+          s.area = edge_fn(a.x, a.y, b.x, b.y, d.x, d.y);
+          shade_face_pixel(p.shade, sm.mesh, c, fid, s, tx0 + lx, ty0 + ly, sh);
+        }
+        if (V.color) {
+          V.color[3 * pix + 0] = sh.c[0];
+          V.color[3 * pix + 1] = sh.c[1];
+          V.color[3 * pix + 2] = sh.c[2];
+        }
+        if (V.normal) {
+          V.normal[3 * pix + 0] = sh.n[0];
+          V.normal[3 * pix + 1] = sh.n[1];
+          V.normal[3 * pix + 2] = sh.n[2];
+        }
+        if (V.color_f32) {
+          V.color_f32[3 * pix + 0] = sh.cf[0];
+          V.color_f32[3 * pix + 1] = sh.cf[1];
+          V.color_f32[3 * pix + 2] = sh.cf[2];
+        }
+      }
     }
     __syncthreads();
-  }
-}
-
-// Loop C's shading (rasterizer.cc:254-299) for every pixel of every view,
-// from the face ids k_tile wrote: kShadePixels pixels per block, one view
-// per block.
-__global__ void __launch_bounds__(256) k_shade(TileParams p) {
-  // k_tile wrote no face ids when the entries did not fit: the host retries
-  if (p.counters->dropped) return;
-  int lo = 0, hi = p.num_views - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (p.views[mid].shade_block <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
-  }
-  const DevView& V = p.views[lo];
-  if (!V.color && !V.normal && !V.color_f32) return;  // nothing to shade in this view
-  const DevMesh& M = p.meshes[V.mesh];
-  const Cam& c = V.cam;
-  const int W = c.width;
-  const int64_t npx = (int64_t)W * c.height;
-  const int64_t first = (int64_t)(blockIdx.x - V.shade_block) * kShadePixels;
-  const float4* proj = p.proj + V.proj_offset;
-  for (int k = threadIdx.x; k < kShadePixels; k += blockDim.x) {
-    const int64_t pix = first + k;
-    if (pix >= npx) break;
-    const int fid = V.face_id[pix];
-    Shaded sh;
-    sh.c[0] = sh.c[1] = sh.c[2] = 0;
-    sh.cf[0] = sh.cf[1] = sh.cf[2] = 0.0f;
-    sh.n[0] = sh.n[1] = sh.n[2] = 0.0f;
-    if (fid > 0) {
-      const int y = (int)(pix / W), x = (int)(pix - (int64_t)y * W);
-      FaceSetup s;
-      const int4 vi = __ldg(&M.vidx_ranked[fid]);
-      const float4 a = __ldg(&proj[vi.x]);
-      const float4 b = __ldg(&proj[vi.y]);
-      const float4 d = __ldg(&proj[vi.z]);
-      s.v0 = make_float3(a.x, a.y, a.z);
-      s.v1 = make_float3(b.x, b.y, b.z);
-      s.v2 = make_float3(d.x, d.y, d.z);
-      s.area = edge_fn(a.x, a.y, b.x, b.y, d.x, d.y);
-      shade_face_pixel(p.shade, M, c, fid, s, x, y, sh);
-    }
-    if (V.color) {
-      V.color[3 * pix + 0] = sh.c[0];
-      V.color[3 * pix + 1] = sh.c[1];
-      V.color[3 * pix + 2] = sh.c[2];
-    }
-    if (V.normal) {
-      V.normal[3 * pix + 0] = sh.n[0];
-      V.normal[3 * pix + 1] = sh.n[1];
-      V.normal[3 * pix + 2] = sh.n[2];
-    }
-    if (V.color_f32) {
-      V.color_f32[3 * pix + 0] = sh.cf[0];
-      V.color_f32[3 * pix + 1] = sh.cf[1];
-      V.color_f32[3 * pix + 2] = sh.cf[2];
-    }
   }
 }
 
@@ -818,9 +798,6 @@ void launch_tile(const TileParams& p, int grid, cudaStream_t s) {
   k_tile<<<grid, kTileThreads, sizeof(TileSmem), s>>>(p);
 }
 
-void launch_shade(const TileParams& p, cudaStream_t s) {
-  if (p.shade_blocks > 0) k_shade<<<p.shade_blocks, 256, 0, s>>>(p);
-}
 
 int tile_kernel_blocks_per_sm() {
   static int blocks = 0;
