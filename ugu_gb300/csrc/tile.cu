@@ -195,7 +195,10 @@ __device__ __forceinline__ int find_slot(const BinSmem& sb, int t) {
 // shared atomic per warp and key; faces touching more take positions from
 // per-group cursors after the fast ones; entries whose tile finds no slot
 // in the table (at most kAggProbes probes) become runs of one.
-__global__ void __launch_bounds__(kBinThreads) k_bin(TileParams p) {
+#ifndef UGU_BIN_BLOCKS
+#define UGU_BIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kBinThreads, UGU_BIN_BLOCKS) k_bin(TileParams p) {
   __shared__ BinSmem sb;
   copy_words(sb.view, p.views[blockIdx.y]);
   for (int i = threadIdx.x; i < kAgg; i += kBinThreads) {
