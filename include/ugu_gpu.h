@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define UGU_GPU_ABI_VERSION 1
+#define UGU_GPU_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define UGU_GPU_API __attribute__((visibility("default")))
@@ -134,7 +134,9 @@ typedef struct {
 enum {
   UGU_GPU_DEVICE_POINTERS = 1u << 0, /* images are device pointers (else host) */
   UGU_GPU_PER_VIEW = 1u << 1,        /* one launch sequence per view (baseline) */
-  UGU_GPU_ASYNC = 1u << 2            /* do not synchronise (device pointers only) */
+  UGU_GPU_ASYNC = 1u << 2,           /* do not synchronise (device pointers only) */
+  UGU_GPU_TIME_KERNELS = 1u << 3     /* time the per-tile raster kernel with CUDA events
+                                        (ugu_gpu_stats.tile_kernel_ms); not with ASYNC */
 };
 
 /* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
@@ -158,6 +160,8 @@ typedef struct {
   uint64_t special_candidates;  /* covered samples with depth < FLT_MIN or NaN */
   uint64_t large_face_tiles;    /* (face, tile) items of the last render */
   uint64_t device_bytes;        /* scratch + mesh bytes held on the device */
+  double tile_kernel_ms;        /* summed device time of timed tile-kernel launches */
+  uint64_t tile_kernel_launches; /* launches timed (UGU_GPU_TIME_KERNELS renders) */
 } ugu_gpu_stats;
 
 /* --- context ------------------------------------------------------------ */

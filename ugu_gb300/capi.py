@@ -30,6 +30,7 @@ ERR_DEGENERATE_DEPTH = 17
 DEVICE_POINTERS = 1
 PER_VIEW = 2
 ASYNC = 4
+TIME_KERNELS = 8
 
 P = C.c_void_p
 
@@ -83,7 +84,8 @@ class Tuning(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("launches", C.c_uint64), ("special_candidates", C.c_uint64),
-                ("large_face_tiles", C.c_uint64), ("device_bytes", C.c_uint64)]
+                ("large_face_tiles", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("tile_kernel_ms", C.c_double), ("tile_kernel_launches", C.c_uint64)]
 
 
 EXPORTS = [

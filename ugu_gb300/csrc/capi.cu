@@ -103,6 +103,12 @@ struct ugu_gpu_context {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // device-to-host copies of host-pointer renders
+  // UGU_GPU_TIME_KERNELS: events around each tile-kernel launch of a render
+  std::vector<cudaEvent_t> tile_events;
+  bool time_tile = false;
+  int timed_groups = 0;
+  double tile_ms = 0.0;
+  uint64_t tile_launches = 0;
   std::vector<cudaEvent_t> events;     // one per group of a host-pointer render, and one more
   std::string last_error;
   ugu_gpu_option opt{};
@@ -595,7 +601,13 @@ int enqueue_group(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) 
     TileParams p = tile_params(ctx, s, gr, gi);
     cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream);
     launch_bin(p, gr.max_faces, ctx->num_sms * 8, ctx->stream);
+    const bool timed = ctx->time_tile && 2 * (size_t)(gi + 1) <= ctx->tile_events.size();
+    if (timed) cudaEventRecord(ctx->tile_events[2 * gi], ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
+    if (timed) {
+      cudaEventRecord(ctx->tile_events[2 * gi + 1], ctx->stream);
+      ctx->timed_groups = (int)gi + 1;
+    }
     return kBinKernels + 1;
   }
   RenderParams p = base_params(ctx, s);
@@ -709,6 +721,10 @@ int check_counters(ugu_gpu_context* ctx, Scratch& s, size_t ngroups) {
       items += s.h_counters[g].tile_items;
     } else {
       special += s.h_tcounters[g].special;
+      if (s.h_tcounters[g].invalid)
+        return set_error(ctx, UGU_GPU_ERR_CUDA,
+                         "internal error: %u invalid tile entries (outputs not valid)",
+                         s.h_tcounters[g].invalid);
       if (s.h_tcounters[g].dropped) {
         // the next attempt allocates what this render reported it needs
         overflow += s.h_tcounters[g].total_entries;
@@ -803,6 +819,9 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
   const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
   if ((flags & UGU_GPU_ASYNC) && !dev)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "UGU_GPU_ASYNC needs device pointers");
+  if ((flags & UGU_GPU_TIME_KERNELS) && (flags & UGU_GPU_ASYNC))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                     "UGU_GPU_TIME_KERNELS reads its events at the end of the render (no ASYNC)");
   std::vector<Group> groups =
       make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0, !dev);
   size_t out_bytes = 0;
@@ -821,7 +840,15 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
                             ctx->stream),
        "cudaMemcpyAsync(views)");
     int kernels = 0;
+    ctx->time_tile = (flags & UGU_GPU_TIME_KERNELS) != 0;
+    ctx->timed_groups = 0;
+    while (ctx->time_tile && ctx->tile_events.size() < 2 * groups.size()) {
+      cudaEvent_t e;
+      CK(ctx, cudaEventCreate(&e), "cudaEventCreate");
+      ctx->tile_events.push_back(e);
+    }
     rc = enqueue_render(ctx, s, groups, views, n, dev, &kernels);
+    ctx->time_tile = false;
     if (rc) {
       s.keys_dirty = s.tiles_dirty = true;
       return rc;
@@ -830,6 +857,15 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
     if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
     CK(ctx, cudaStreamSynchronize(ctx->stream), "render");
     rc = check_counters(ctx, s, groups.size());
+    if (!rc)
+      for (int g = 0; g < ctx->timed_groups; ++g) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ctx->tile_events[2 * g], ctx->tile_events[2 * g + 1]) ==
+            cudaSuccess) {
+          ctx->tile_ms += ms;
+          ++ctx->tile_launches;
+        }
+      }
     if (rc == UGU_GPU_ERR_CAPACITY && attempt == 0) {
       // a list overflowed: grow it (the tiled path knows the exact need) and
       // render again
@@ -910,6 +946,7 @@ int ugu_gpu_destroy(ugu_gpu_context* ctx) {
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->tile_events) cudaEventDestroy(e);
   delete ctx;
   return UGU_GPU_OK;
 }
@@ -1403,6 +1440,8 @@ int ugu_gpu_get_stats(const ugu_gpu_context* ctx, ugu_gpu_stats* st) {
   const Scratch& s = ctx->scratch;
   b += s.keys_cap * 8 + s.items_cap * sizeof(TileItem) + s.d_out_cap;
   st->device_bytes = b;
+  st->tile_kernel_ms = ctx->tile_ms;
+  st->tile_kernel_launches = ctx->tile_launches;
   return UGU_GPU_OK;
 }
 

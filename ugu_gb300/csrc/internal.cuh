@@ -110,7 +110,7 @@ struct RenderParams {
 // Counters of one tiled render (memset before every launch).
 struct TileCounters {
   unsigned int next_tile;             // work-queue head of k_tile
-  unsigned int pad0;
+  unsigned int invalid;                // runs or entries outside their arrays (a bug)
   unsigned long long special;         // covered samples with unorderable depth
   unsigned long long dropped;         // entries or runs did not fit (0: none)
   unsigned long long total_entries;   // (face, tile) entries of this render

@@ -248,8 +248,10 @@ __global__ void __launch_bounds__(kBinThreads, UGU_BIN_BLOCKS) k_bin(TileParams 
     }
   }
   __syncthreads();
-  // many-tile faces: counted after the fast entries of every group
+  // many-tile faces: counted after the fast entries of every group, whose
+  // counts the cursors keep (copied before any many-tile count is added)
   for (int i = threadIdx.x; i < 2 * kAgg; i += kBinThreads) sb.cur[i] = sb.cnt[i];
+  __syncthreads();
 #pragma unroll
   for (int u = 0; u < kBinFaces; ++u) {
     if (fb[u].n <= kAggPerFace) continue;
@@ -367,6 +369,11 @@ __global__ void __launch_bounds__(256) k_gather(TileParams p) {
   for (unsigned long long r = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < nr;
        r += warps) {
     const int4 run = p.runs[r];  // (tile, class, first staged entry, count)
+    if (run.x < 0 || run.x >= p.total_tiles || run.z < 0 || run.w < 0 ||
+        (int64_t)run.z + run.w > p.entry_cap) {  // never for k_bin's runs: reported, skipped
+      if (lane == 0) atomicAdd(&p.counters->invalid, 1u);
+      continue;
+    }
     int dst = 0;
     if (lane == 0)
       dst = run.y ? atomicSub(&p.tile_hi[run.x], run.w) - run.w
@@ -682,6 +689,10 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           const int2 e = p.entries[cs + j];
           const float zlb = __int_as_float(e.y);
           R.cnt[j] = 0;
+          if ((unsigned)e.x >= (unsigned)sm.mesh.num_faces) {  // never for k_bin's entries
+            atomicAdd(&p.counters->invalid, 1u);
+            continue;
+          }
           if (zlb > zmax) continue;  // behind every key of a covered tile: cannot win
           const int f = __ldg(&sm.mesh.order[e.x]);  // the entry holds the binning number
           FaceSetup s;
