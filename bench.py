@@ -138,14 +138,17 @@ def measured_peak_hbm():
 
 
 def committed_traffic():
-    """Per-launch DRAM bytes of the batched render from an ncu capture, as
-    summarised in profiles/traffic.json (null when absent)."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+    """Per-launch DRAM bytes of the tile kernel from an ncu capture, as
+    summarised in profiles/k_tile_traffic.txt (null when absent)."""
+    p = os.path.join(ROOT, "profiles", "k_tile_traffic.txt")
     try:
         with open(p) as f:
-            return json.load(f).get("batched_forward_dram_bytes_per_launch")
+            for line in f:
+                if line.strip().startswith("k_tile_dram_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1])
     except Exception:
-        return None
+        pass
+    return None
 
 
 def workload(n_views):
