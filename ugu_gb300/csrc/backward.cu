@@ -19,6 +19,8 @@
 // which issues the atomics (warp-aggregated scatter).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "internal.cuh"
 #include "shade.cuh"
 
@@ -51,13 +53,37 @@ __device__ __forceinline__ int run_id(int key, int lane) {
   return 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
 }
 
-// One vertex of one view in double: screen x, y, camera z and 1 / z.
-struct alignas(16) Proj64 {
-  double x, y, z, iz;
+// Adds (g0, g1, g2) to the 3 consecutive floats of element `tix` (a texel's
+// RGB, a vertex's xyz or colour): one 8-byte and one 4-byte atomic add when
+// the buffer is 8-byte aligned (the pair starts at the element's even
+// float), else three 4-byte ones.
+__device__ __forceinline__ void add3(float* g, int64_t tix, float g0, float g1,
+                                               float g2, bool aligned8) {
+  float* t = g + 3 * tix;
+  if (!aligned8) {
+    atomicAdd(t, g0);
+    atomicAdd(t + 1, g1);
+    atomicAdd(t + 2, g2);
+  } else if ((tix & 1) == 0) {
+    atomicAdd(reinterpret_cast<float2*>(t), make_float2(g0, g1));
+    atomicAdd(t + 2, g2);
+  } else {
+    atomicAdd(t, g0);
+    atomicAdd(reinterpret_cast<float2*>(t + 1), make_float2(g1, g2));
+  }
+}
+
+// One vertex of one view: its screen x and y, projected in double, as
+// unevaluated sums hi + lo of two floats (about 48 significant bits), and
+// 1 / z.  32 bytes per vertex.
+struct alignas(16) ProjHL {
+  float xh, yh, xl, yl;
+  float iz, pad_[3];
 };
 
 // The pinhole projection of every vertex of one view (blockIdx.y) in
-// double, from the float vertices and camera (camera.h:380-387).
+// double, from the float vertices and camera (camera.h:380-387), split
+// into hi + lo floats.
 __global__ void __launch_bounds__(kThreads) k_proj64(BackwardParams p) {
   const DevView& V = p.views[blockIdx.y];
   const DevMesh& M = p.meshes[V.mesh];
@@ -70,33 +96,61 @@ __global__ void __launch_bounds__(kThreads) k_proj64(BackwardParams p) {
   for (int j = 0; j < 3; ++j)
     cc[j] = (double)c.R[3 * j] * P.x + (double)c.R[3 * j + 1] * P.y +
             (double)c.R[3 * j + 2] * P.z + (double)c.t[j];
-  Proj64 o;
-  o.iz = 1.0 / cc[2];
-  o.x = (double)c.fx * cc[0] * o.iz + (double)c.cx;
-  o.y = (double)c.fy * cc[1] * o.iz + (double)c.cy;
-  o.z = cc[2];
-  reinterpret_cast<Proj64*>(p.proj64)[V.proj_offset + i] = o;
+  const double iz = 1.0 / cc[2];
+  const double x = (double)c.fx * cc[0] * iz + (double)c.cx;
+  const double y = (double)c.fy * cc[1] * iz + (double)c.cy;
+  ProjHL o;
+  o.xh = (float)x;
+  o.yh = (float)y;
+  o.xl = (float)(x - (double)o.xh);
+  o.yl = (float)(y - (double)o.yh);
+  o.iz = (float)iz;
+  o.pad_[0] = o.pad_[1] = o.pad_[2] = 0.0f;
+  float4* dst = reinterpret_cast<float4*>(reinterpret_cast<ProjHL*>(p.proj64) + V.proj_offset + i);
+  dst[0] = make_float4(o.xh, o.yh, o.xl, o.yl);
+  dst[1] = make_float4(o.iz, 0.0f, 0.0f, 0.0f);
 }
 
-__device__ __forceinline__ Proj64 load_proj64(const Proj64* t, int i) {
-  const double2* q = reinterpret_cast<const double2*>(t + i);
-  const double2 a = __ldg(q), b = __ldg(q + 1);
-  Proj64 o;
-  o.x = a.x;
-  o.y = a.y;
-  o.z = b.x;
-  o.iz = b.y;
-  return o;
+// Error-free transformations (Knuth's TwoSum, and the FMA product error):
+// a + b = s + e and a * b = p + e exactly.  The library is compiled without
+// FMA contraction, so the separate roundings these rely on are kept.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
 }
 
-// Vertex-position (and colour, texel) gradients of one pixel.  The
-// quantities whose float rounding the sum over pixels would amplify are
-// formed in double from the view's double projection table: the edge
-// functions and the normalised perspective weights w = r / sum(r) with
-// r_k = e_k / z_k (the area cancels in w, so it has no gradient), the
-// texture coordinates with their texel cell and offsets, and the
-// pixel-to-vertex differences the edge derivatives multiply.  The rest of
-// the chain is float.
+// Texel coordinate base + t (t small: the offset of the pixel's texture
+// coordinate from one vertex's, in texels) split into an integer cell and a
+// fraction in [0, 1).  base = hi + lo is exact; the cell is found from hi's
+// integer part first, so the fraction keeps float precision relative to a
+// texel rather than to the coordinate.
+__device__ __forceinline__ void texel_cell(float hi, float lo, float t, int64_t& cell,
+                                           float& frac) {
+  const float ih = floorf(hi);
+  const float rem = (hi - ih) + (lo + t);  // hi - ih is exact for |hi| < 2^23
+  const float ir = floorf(rem);
+  cell = (int64_t)f2i_sat(ih) + (int64_t)f2i_sat(ir);
+  frac = rem - ir;
+}
+
+// The same for rounding to the nearest texel (round half away from zero).
+__device__ __forceinline__ int64_t texel_nearest(float hi, float lo, float t) {
+  const float ih = floorf(hi);
+  const float rem = (hi - ih) + (lo + t);
+  return (int64_t)f2i_sat(ih) + (int64_t)f2i_sat(roundf(rem));
+}
+
+// Vertex-position (and colour, texel) gradients of one pixel, in float.
+// The sum over pixels amplifies systematic rounding and the gradients of
+// sliver faces are large, so three quantities keep more than float
+// precision: the pixel-to-vertex differences (from the double projection's
+// hi + lo parts, accurate relative to the difference rather than to the
+// screen coordinate), the edge functions (accurate relative to themselves
+// however thin the face), and the texture coordinate (a texel-exact base
+// at one vertex plus a small offset, texel_cell).  The perspective weights
+// are w = r / sum(r) with r_k = e_k / z_k (the area cancels in w, so it has
+// no gradient).
 struct PixGrad {
   float loss;
   float gpos[9];
@@ -107,25 +161,52 @@ struct PixGrad {
 };
 
 __device__ __forceinline__ void pixel_backward(const BackwardParams& p, const DevMesh& m,
-                                               const Cam& c, const Proj64* tab, int fid, int x,
+                                               const Cam& c, const ProjHL* tab, int fid, int x,
                                                int y, const float* target, PixGrad& o) {
   const int4 vi = __ldg(&m.vidx[fid]);
-  const Proj64 P[3] = {load_proj64(tab, vi.x), load_proj64(tab, vi.y), load_proj64(tab, vi.z)};
-  const double px = x, py = y;
-  double dx[3], dy[3];  // pixel minus vertex
+  const int vv[3] = {vi.x, vi.y, vi.z};
+  float xh[3], yh[3], xl[3], yl[3], iz[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    dx[k] = px - P[k].x;
-    dy[k] = py - P[k].y;
+    const float4 a = __ldg(reinterpret_cast<const float4*>(tab + vv[k]));
+    xh[k] = a.x;
+    yh[k] = a.y;
+    xl[k] = a.z;
+    yl[k] = a.w;
+    iz[k] = __ldg(&tab[vv[k]].iz);
   }
-  // e_k = edge(v_a, v_b, p) for (a, b) = (1, 2), (2, 0), (0, 1)
-  const double e0 = dx[1] * (P[2].y - P[1].y) - dy[1] * (P[2].x - P[1].x);
-  const double e1 = dx[2] * (P[0].y - P[2].y) - dy[2] * (P[0].x - P[2].x);
-  const double e2 = dx[0] * (P[1].y - P[0].y) - dy[0] * (P[1].x - P[0].x);
-  const double r[3] = {e0 * P[0].iz, e1 * P[1].iz, e2 * P[2].iz};
-  const double iS = 1.0 / (r[0] + r[1] + r[2]);
-  const double ud = r[1] * iS, vd = r[2] * iS, s0d = 1.0 - ud - vd;
-  const float u = (float)ud, v = (float)vd, s0 = (float)s0d;
+  // pixel minus vertex as unevaluated sums dh + dl (about 48 bits)
+  const float px = (float)x, py = (float)y;
+  float dxh[3], dxl[3], dyh[3], dyl[3], dx[3], dy[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float e;
+    two_sum(px, -xh[k], dxh[k], e);
+    dxl[k] = e - xl[k];
+    two_sum(py, -yh[k], dyh[k], e);
+    dyl[k] = e - yl[k];
+    dx[k] = dxh[k] + dxl[k];
+    dy[k] = dyh[k] + dyl[k];
+  }
+  // e_k = edge(v_a, v_b, p) = dy_a dx_b - dx_a dy_b for (a, b) = (1, 2),
+  // (2, 0), (0, 1).  On a sliver face the two products nearly cancel, so
+  // they are formed exactly (FMA product errors) and the lo parts enter
+  // as first-order terms: e_k is then accurate relative to itself.
+  const int ea[3] = {1, 2, 0}, eb[3] = {2, 0, 1};
+  float r[3], rs = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int ia = ea[k], ib = eb[k];
+    const float p1 = dyh[ia] * dxh[ib], q1 = fmaf(dyh[ia], dxh[ib], -p1);
+    const float p2 = dxh[ia] * dyh[ib], q2 = fmaf(dxh[ia], dyh[ib], -p2);
+    const float cross = (dyh[ia] * dxl[ib] + dyl[ia] * dxh[ib]) -
+                        (dxh[ia] * dyl[ib] + dxl[ia] * dyh[ib]);
+    const float e = (p1 - p2) + ((q1 - q2) + cross);
+    r[k] = e * iz[k];
+    rs += r[k];
+  }
+  const float iS = 1.0f / rs;
+  const float u = r[1] * iS, v = r[2] * iS, s0 = (1.0f - u) - v;
   float col[3], dcu[3], dcv[3];
   o.ntex = 0;
 #pragma unroll
@@ -140,20 +221,29 @@ __device__ __forceinline__ void pixel_backward(const BackwardParams& p, const De
     const float a0[3] = {c0.x, c0.y, c0.z}, a1[3] = {c1.x, c1.y, c1.z}, a2[3] = {c2.x, c2.y, c2.z};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      col[k] = (float)(s0d * a0[k] + ud * a1[k] + vd * a2[k]);
       dcu[k] = a1[k] - a0[k];
       dcv[k] = a2[k] - a0[k];
+      col[k] = a0[k] + (u * dcu[k] + v * dcv[k]);
     }
   } else {
     const int mid = __ldg(&m.mat_ids[fid]);
     const DevTexture t = m.textures[mid];
     const int4 ti = __ldg(&m.uvidx[fid]);
     const float2 a = __ldg(&m.uv[ti.x]), b = __ldg(&m.uv[ti.y]), d = __ldg(&m.uv[ti.z]);
-    const double uvx = s0d * a.x + ud * b.x + vd * d.x;
-    const double uvy = s0d * a.y + ud * b.y + vd * d.y;
-    const double fx = uvx * (t.width - 1), fy = (1.0 - uvy) * (t.height - 1);
+    const float Wm = (float)(t.width - 1), Hm = (float)(t.height - 1);
+    // fx = Wm * uvx, fy = Hm * (1 - uvy), uv = a + u (b - a) + v (d - a)
+    const float dfx_du = (b.x - a.x) * Wm, dfx_dv = (d.x - a.x) * Wm;
+    const float dfy_du = -(b.y - a.y) * Hm, dfy_dv = -(d.y - a.y) * Hm;
+    const float ox = u * dfx_du + v * dfx_dv;
+    const float oy = u * dfy_du + v * dfy_dv;
+    const float bxh = Wm * a.x, bxl = fmaf(Wm, a.x, -bxh);  // Wm a.x, exactly
+    const float pyh = Hm * a.y, pyl = fmaf(Hm, a.y, -pyh);  // Hm a.y, exactly
+    float byh, bye;
+    two_sum(Hm, -pyh, byh, bye);  // Hm - Hm a.y = byh + bye - pyl
+    const float byl = bye - pyl;
     if (p.interp == 0) {
-      const int64_t ix = texel_index((int64_t)llrint(fy), (int64_t)llrint(fx), t.width, t.height);
+      const int64_t ix =
+          texel_index(texel_nearest(byh, byl, oy), texel_nearest(bxh, bxl, ox), t.width, t.height);
       fetch_texel(t, ix, col);
 #pragma unroll
       for (int k = 0; k < 3; ++k) dcu[k] = dcv[k] = 0.0f;
@@ -161,21 +251,19 @@ __device__ __forceinline__ void pixel_backward(const BackwardParams& p, const De
       o.tg[0][0] = o.tg[0][1] = o.tg[0][2] = 1.0f;  // weights; scaled by dL/dC below
       o.ntex = mid == 0 ? 1 : 0;
     } else {
-      const double x0 = floor(fx), y0 = floor(fy);
-      const float lu = (float)(fx - x0), lv = (float)(fy - y0);
-      o.tix[0] = texel_index((int64_t)y0, (int64_t)x0, t.width, t.height);
-      o.tix[1] = texel_index((int64_t)y0, (int64_t)x0 + 1, t.width, t.height);
-      o.tix[2] = texel_index((int64_t)y0 + 1, (int64_t)x0, t.width, t.height);
-      o.tix[3] = texel_index((int64_t)y0 + 1, (int64_t)x0 + 1, t.width, t.height);
+      int64_t x0, y0;
+      float lu, lv;
+      texel_cell(bxh, bxl, ox, x0, lu);
+      texel_cell(byh, byl, oy, y0, lv);
+      o.tix[0] = texel_index(y0, x0, t.width, t.height);
+      o.tix[1] = texel_index(y0, x0 + 1, t.width, t.height);
+      o.tix[2] = texel_index(y0 + 1, x0, t.width, t.height);
+      o.tix[3] = texel_index(y0 + 1, x0 + 1, t.width, t.height);
       float t00[3], t10[3], t01[3], t11[3];
       fetch_texel(t, o.tix[0], t00);
       fetch_texel(t, o.tix[1], t10);
       fetch_texel(t, o.tix[2], t01);
       fetch_texel(t, o.tix[3], t11);
-      const float dfx_du = (b.x - a.x) * (float)(t.width - 1);
-      const float dfx_dv = (d.x - a.x) * (float)(t.width - 1);
-      const float dfy_du = -(b.y - a.y) * (float)(t.height - 1);
-      const float dfy_dv = -(d.y - a.y) * (float)(t.height - 1);
       const float w00 = (1.0f - lu) * (1.0f - lv), w10 = lu * (1.0f - lv);
       const float w01 = (1.0f - lu) * lv, w11 = lu * lv;
 #pragma unroll
@@ -215,62 +303,52 @@ __device__ __forceinline__ void pixel_backward(const BackwardParams& p, const De
   const float gw1 = gC[0] * dcu[0] + gC[1] * dcu[1] + gC[2] * dcu[2];
   const float gw2 = gC[0] * dcv[0] + gC[1] * dcv[1] + gC[2] * dcv[2];
   const float gdotw = gw1 * u + gw2 * v;
-  const float fiS = (float)iS;
-  const float gr[3] = {-gdotw * fiS, (gw1 - gdotw) * fiS, (gw2 - gdotw) * fiS};
+  const float gr[3] = {-gdotw * iS, (gw1 - gdotw) * iS, (gw2 - gdotw) * iS};
   float ge[3], gZ[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float iz = (float)P[k].iz;
-    ge[k] = gr[k] * iz;
-    gZ[k] = -gr[k] * (float)r[k] * iz;
+    ge[k] = gr[k] * iz[k];
+    gZ[k] = -gr[k] * r[k] * iz[k];
   }
-  const float fdx[3] = {(float)dx[0], (float)dx[1], (float)dx[2]};
-  const float fdy[3] = {(float)dy[0], (float)dy[1], (float)dy[2]};
   float gX[3] = {0.0f, 0.0f, 0.0f}, gY[3] = {0.0f, 0.0f, 0.0f};
-  const int ea[3] = {1, 2, 0}, eb[3] = {2, 0, 1};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {  // e_k = dy_a dx_b - dx_a dy_b (d = pixel - vertex)
     const int ia = ea[k], ib = eb[k];
-    gX[ia] += ge[k] * fdy[ib];
-    gY[ia] -= ge[k] * fdx[ib];
-    gX[ib] -= ge[k] * fdy[ia];
-    gY[ib] += ge[k] * fdx[ia];
+    gX[ia] += ge[k] * dy[ib];
+    gY[ia] -= ge[k] * dx[ib];
+    gX[ib] -= ge[k] * dy[ia];
+    gY[ib] += ge[k] * dx[ia];
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float iz = (float)P[k].iz;
-    const float gcx = gX[k] * c.fx * iz;
-    const float gcy = gY[k] * c.fy * iz;
-    const float gcz = -(gX[k] * (float)(P[k].x - c.cx) + gY[k] * (float)(P[k].y - c.cy)) * iz + gZ[k];
+    const float gcx = gX[k] * c.fx * iz[k];
+    const float gcy = gY[k] * c.fy * iz[k];
+    const float sx = (xh[k] - c.cx) + xl[k], sy = (yh[k] - c.cy) + yl[k];
+    const float gcz = -(gX[k] * sx + gY[k] * sy) * iz[k] + gZ[k];
 #pragma unroll
     for (int j = 0; j < 3; ++j) o.gpos[3 * k + j] = c.R[j] * gcx + c.R[3 + j] * gcy + c.R[6 + j] * gcz;
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
-  __shared__ DevView sv;
-  __shared__ DevMesh sm;
-  __shared__ float s_loss[kThreads / 32];
-  {
-    const int* src = reinterpret_cast<const int*>(&p.views[blockIdx.y]);
-    int* dst = reinterpret_cast<int*>(&sv);
-    for (int i = threadIdx.x; i < (int)(sizeof(DevView) / 4); i += blockDim.x) dst[i] = src[i];
-    __syncthreads();
-    const int* msrc = reinterpret_cast<const int*>(&p.meshes[sv.mesh]);
-    int* mdst = reinterpret_cast<int*>(&sm);
-    for (int i = threadIdx.x; i < (int)(sizeof(DevMesh) / 4); i += blockDim.x) mdst[i] = msrc[i];
-    __syncthreads();
-  }
+// One pixel of one view (the thread's pixel i of the view's image; i may
+// lie past its end): its gradients, scattered, and its loss returned.  All
+// lanes of the warp take part (the run reductions shuffle across them).
+__device__ __forceinline__ float backward_pixel(const BackwardParams& p, const DevView& sv,
+                                                const DevMesh& sm, int64_t i, int lane,
+                                                bool aligned8) {
   const Cam& c = sv.cam;
-  const int lane = threadIdx.x & 31;
   const int64_t npx = (int64_t)c.width * c.height;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int fid = -1;
   int x = 0, y = 0;
   if (i < npx) {
     fid = sv.face_id[i];
-    x = (int)(i % c.width);
-    y = (int)(i / c.width);
+    if (npx <= 0x7fffffff) {  // 32-bit division for every image below 2^31 pixels
+      y = (int)((uint32_t)i / (uint32_t)c.width);
+      x = (int)((uint32_t)i - (uint32_t)y * (uint32_t)c.width);
+    } else {
+      x = (int)(i % c.width);
+      y = (int)(i / c.width);
+    }
     if (fid < -1 || fid >= sm.num_faces) {  // not a forward's face id: reported, skipped
       atomicAdd(p.bad_ids, 1ull);
       fid = -1;
@@ -288,7 +366,7 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
     // amplifies rounding: see pixel_backward.
     vi = __ldg(&sm.vidx[fid]);
     PixGrad o;
-    pixel_backward(p, sm, c, reinterpret_cast<const Proj64*>(p.proj64) + sv.proj_offset, fid, x,
+    pixel_backward(p, sm, c, reinterpret_cast<const ProjHL*>(p.proj64) + sv.proj_offset, fid, x,
                    y, &p.targets[blockIdx.y][3 * i], o);
     loss = o.loss;
 #pragma unroll
@@ -300,8 +378,7 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
 #pragma unroll
       for (int j = 0; j < 4; ++j)
         if (j < o.ntex)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) atomicAdd(&p.grad_texels[3 * o.tix[j] + k], o.tg[j][k]);
+          add3(p.grad_texels, o.tix[j], o.tg[j][0], o.tg[j][1], o.tg[j][2], aligned8);
   } else if (fid > 0) {
     // Texel and vertex-colour gradients only: the float colour equals the
     // forward's (same exact arithmetic), so the loss is the rendered one.
@@ -371,13 +448,17 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
           col[k] = fadd(fadd(fadd(fmul(tw[0], t00[k]), fmul(tw[1], t10[k])), fmul(tw[2], t01[k])),
                         fmul(tw[3], t11[k]));
       }
+      float gC[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const float dd = col[k] - __ldg(&tg[k]);
         loss += dd * dd;
-        if (mid == 0 && p.grad_texels)
-          for (int j = 0; j < nt; ++j) atomicAdd(&p.grad_texels[3 * tix[j] + k], 2.0f * dd * tw[j]);
+        gC[k] = 2.0f * dd;
       }
+      if (mid == 0 && p.grad_texels)
+        for (int j = 0; j < nt; ++j)
+          add3(p.grad_texels, tix[j], gC[0] * tw[j], gC[1] * tw[j], gC[2] * tw[j],
+                         aligned8);
     }
   }
 
@@ -386,19 +467,50 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
   const bool head = run == lane;
   const int vids[3] = {vi.x, vi.y, vi.z};
   if (p.grad_vertices) {
+    const bool al = (reinterpret_cast<uintptr_t>(p.grad_vertices) & 7) == 0;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const float t = run_sum(gv[k], run, lane);
-      if (head) atomicAdd(&p.grad_vertices[3 * vids[k / 3] + (k % 3)], t);
-    }
+    for (int k = 0; k < 9; ++k) gv[k] = run_sum(gv[k], run, lane);
+    if (head)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) add3(p.grad_vertices, vids[k], gv[3 * k], gv[3 * k + 1], gv[3 * k + 2], al);
   }
   if (p.grad_vertex_colors && p.diffuse_color == 2) {
+    const bool al = (reinterpret_cast<uintptr_t>(p.grad_vertex_colors) & 7) == 0;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const float t = run_sum(gc[k], run, lane);
-      if (head) atomicAdd(&p.grad_vertex_colors[3 * vids[k / 3] + (k % 3)], t);
-    }
+    for (int k = 0; k < 9; ++k) gc[k] = run_sum(gc[k], run, lane);
+    if (head)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        add3(p.grad_vertex_colors, vids[k], gc[3 * k], gc[3 * k + 1], gc[3 * k + 2], al);
   }
+  return loss;
+}
+
+// 4 blocks of 256 per SM: at most 64 registers a thread
+__global__ void __launch_bounds__(kThreads, 4) k_backward(BackwardParams p) {
+  // blockIdx.y: the view; blockIdx.x: every gridDim.x-th chunk of kThreads
+  // pixels of it, so the descriptor copies and the loss reduction below are
+  // paid once per block
+  __shared__ DevView sv;
+  __shared__ DevMesh sm;
+  __shared__ float s_loss[kThreads / 32];
+  {
+    const int* src = reinterpret_cast<const int*>(&p.views[blockIdx.y]);
+    int* dst = reinterpret_cast<int*>(&sv);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevView) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    const int* msrc = reinterpret_cast<const int*>(&p.meshes[sv.mesh]);
+    int* mdst = reinterpret_cast<int*>(&sm);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevMesh) / 4); i += blockDim.x) mdst[i] = msrc[i];
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const bool aligned8 = (reinterpret_cast<uintptr_t>(p.grad_texels) & 7) == 0;
+  const int64_t npx = (int64_t)sv.cam.width * sv.cam.height;
+  const int64_t nchunks = (npx + kThreads - 1) / kThreads;
+  float loss = 0.0f;
+  for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x)
+    loss += backward_pixel(p, sv, sm, ch * kThreads + threadIdx.x, lane, aligned8);
   if (p.loss) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
@@ -414,11 +526,14 @@ __global__ void __launch_bounds__(kThreads) k_backward(BackwardParams p) {
 
 }  // namespace
 
-void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices,
+void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices, int num_sms,
                      cudaStream_t s) {
   if (p.grad_vertices)
     k_proj64<<<dim3((max_vertices + kThreads - 1) / kThreads, p.num_views), kThreads, 0, s>>>(p);
-  dim3 grid((unsigned)((max_pixels + kThreads - 1) / kThreads), p.num_views);
+  // about 4 waves of 4 blocks per SM over all views
+  const int64_t chunks = (max_pixels + kThreads - 1) / kThreads;
+  const int64_t per_view = std::max<int64_t>(1, ((int64_t)num_sms * 16 + p.num_views - 1) / p.num_views);
+  dim3 grid((unsigned)std::max<int64_t>(1, std::min(chunks, per_view)), p.num_views);
   k_backward<<<grid, kThreads, 0, s>>>(p);
 }
 

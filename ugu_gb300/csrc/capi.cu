@@ -72,8 +72,8 @@ struct Scratch {
   size_t tcounters_cap = 0;
   bool tiles_dirty = false;
   size_t list_min = size_t(1) << 22;  // capacity of the item / overflow lists
-  // backward: per-view target pointers, double projection table
-  double* proj64 = nullptr;  // 4 doubles per vertex of every view
+  // backward: per-view target pointers, hi + lo projection table
+  void* proj64 = nullptr;    // 32 bytes per vertex of every view
   size_t proj64_cap = 0;     // vertices
   const float** d_targets = nullptr;
   const float** h_targets = nullptr;  // pinned
@@ -1354,8 +1354,8 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     cudaFree(s.proj64);
     s.proj64 = nullptr;
     s.proj64_cap = 0;
-    CK(ctx, cudaMalloc(&s.proj64, (size_t)sum_v * 4 * sizeof(double)),
-       "cudaMalloc(double projection table)");
+    CK(ctx, cudaMalloc(&s.proj64, (size_t)sum_v * 32),
+       "cudaMalloc(projection table)");
     s.proj64_cap = (size_t)sum_v;
   }
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
@@ -1391,7 +1391,7 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   p.proj64 = s.proj64;
   CK(ctx, cudaMemsetAsync(s.counters, 0, sizeof(DevCounters), ctx->stream),
      "cudaMemsetAsync(counters)");
-  launch_backward(p, max_px, max_v, ctx->stream);
+  launch_backward(p, max_px, max_v, ctx->num_sms, ctx->stream);
   CK(ctx, cudaGetLastError(), "backward launch");
   ctx->launches += grad_vertices ? 2 : 1;
   CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, sizeof(DevCounters), cudaMemcpyDeviceToHost,

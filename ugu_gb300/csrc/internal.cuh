@@ -157,12 +157,13 @@ struct BackwardParams {
   float* grad_vertices;         // V*3 (or NULL)
   float* loss;                  // one per view (or NULL)
   unsigned long long* bad_ids;  // counts face ids outside [-1, num_faces)
-  double* proj64;               // per view (DevView::proj_offset): x, y, z, 1/z per vertex
+  void* proj64;                 // per view (DevView::proj_offset), 32 bytes per vertex: screen
+                                // x, y projected in double as hi + lo floats, and 1/z
 };
 
-// Host-side launcher (backward.cu): the double projection table (when
+// Host-side launcher (backward.cu): the hi + lo projection table (when
 // position gradients are asked for), then the per-pixel backward.
-void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices,
+void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices, int num_sms,
                      cudaStream_t s);
 
 // Host-side launchers (tile.cu).  launch_bin enqueues projection, binning,
