@@ -50,9 +50,10 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-backward", action="store_true")
     ap.add_argument("--workload", default="ring64",
-                    choices=["ring64", "uvsphere", "single1080", "texdescent256"],
+                    choices=["ring64", "uvsphere", "single1080", "texdescent256", "raytrace64"],
                     help="ring64 (default): the batched-forward workload; the others "
-                         "measure the single-view and large fwd+bwd configurations")
+                         "measure the single-view and large fwd+bwd configurations, and "
+                         "the ring64 views through the raytracer")
     return ap.parse_args()
 
 
@@ -477,6 +478,91 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
         "loss_first": losses[0], "loss_last": losses[-1], "setup_s": setup_s}), flush=True)
 
 
+def run_raytrace(args):
+    """The ring64 views (icosphere-7, 2048^2 texture, 64 views, 54.1 Mpx)
+    through the raytracer (UGU_GPU_RAYTRACE: ugu::Raytracer's naive BVH and
+    double-precision ray hits), one captured plan replay per step; the
+    oracle's raytracer on a bounded sample beside it."""
+    import torch
+
+    from ugu_gb300 import build as b
+    from ugu_gb300 import capi, scenes
+    from ugu_gb300.rasterizer import Context
+    b.build()
+    m, cams = workload(args.views)
+    total_px = sum(c.width * c.height for c in cams)
+    ctx = Context(0)
+    ctx.check(ctx.set_mesh(0, m))
+    ctx.check(ctx.set_option(option()))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.check(ctx.set_stream(stream.cuda_stream))
+    outs, views = [], []
+    for c in cams:
+        H, W = c.height, c.width
+        t = {"color": torch.empty((H, W, 3), dtype=torch.uint8, device="cuda"),
+             "depth": torch.empty((H, W), dtype=torch.float32, device="cuda"),
+             "normal": torch.empty((H, W, 3), dtype=torch.float32, device="cuda"),
+             "mask": torch.empty((H, W), dtype=torch.uint8, device="cuda"),
+             "face_id": torch.empty((H, W), dtype=torch.int32, device="cuda")}
+        v = capi.View()
+        v.mesh = 0
+        v.camera = capi.camera_struct(c)
+        for k, x in t.items():
+            setattr(v.images, k, x.data_ptr())
+        outs.append(t)
+        views.append(v)
+    t0 = time.perf_counter()
+    plan = ctx.plan_create(views, capi.DEVICE_POINTERS | capi.RAYTRACE)  # builds the BVH
+    bvh_s = time.perf_counter() - t0
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        ctx.check(plan.launch())
+    ctx.check(ctx.synchronize())
+    ev = []
+    sampler = ClockSampler(0)
+    sampler.start()
+    for _ in range(args.steps):
+        flush.zero_()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.check(plan.launch())
+        e.record(stream)
+        ev.append((a, e))
+    ctx.check(ctx.synchronize())
+    clocks = sampler.stop()
+    ms = sum(a.elapsed_time(e) for a, e in ev) / len(ev)
+    plan.close()
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        # bounded sample: the first ring camera at 160x120 (same field of view)
+        c0 = cams[0]
+        s = 160.0 / c0.width
+        cs = scenes.camera_desc(160, int(round(c0.height * s)), c0.fx * s, c0.fy * s,
+                                c0.cx * s, c0.cy * s, c0.c2w)
+        t0 = time.perf_counter()
+        rc, _ = oracle.raytrace(m, cs, option(), outputs=("color", "depth", "normal", "mask",
+                                                          "face_id"))
+        dt = time.perf_counter() - t0
+        px = cs.width * cs.height
+        cpu = {"value": px / dt / (total_px / len(cams)), "unit": "views/s", "cores": 1,
+               "kind": "port", "sample": f"one {cs.width}x{cs.height} view of the ring "
+                                         f"({px} rays), scaled to the mean view's pixels"}
+    print(json.dumps({
+        "metric": "views/s", "value": len(cams) / (ms / 1e3), "unit": "views/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic",
+        "grays_per_s": total_px / (ms / 1e3) / 1e9,
+        "config": {"workload": "raytrace64_icosphere7_tex2048_bilinear", "views": len(cams),
+                   "pixels": total_px, "mesh_faces": m.num_faces,
+                   "renderer": "raytracer (naive BVH, double-precision hits)",
+                   "l2": "flushed (256 MB write) between timed steps",
+                   "bvh_build_and_plan_s": bvh_s},
+        "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": 1}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -487,6 +573,9 @@ def main():
         return
     if args.workload == "texdescent256":
         run_texdescent(args)
+        return
+    if args.workload == "raytrace64":
+        run_raytrace(args)
         return
     rank, world, local = dist_env()
     import torch

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define UGU_GPU_ABI_VERSION 2
+#define UGU_GPU_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define UGU_GPU_API __attribute__((visibility("default")))
@@ -66,7 +66,8 @@ typedef struct {
   int32_t interp;          /* 0 kNn, 1 kBilinear */
   int32_t shading_normal;  /* 0 kFace, 1 kVertex */
   int32_t diffuse_shading; /* 0 kNone, 1 kLambertian, 2 kOrenNayar */
-  float depth_scale;       /* accepted and ignored, as ugu::Rasterizer does */
+  float depth_scale;       /* raytracer: multiplies the output depth (raytracer.cc:185);
+                              the rasterizer ignores it, as ugu::Rasterizer does */
   int32_t backface_culling;
   float oren_nayar_sigma;
 } ugu_gpu_option;
@@ -103,6 +104,8 @@ typedef struct {
  *   w2c_R = camera->w2c().rotation().cast<float>()      (row-major)
  *   w2c_t = camera->w2c().translation().cast<float>()
  *   c2w_R = camera->c2w().matrix().block<3,3>(0,0).cast<float>() (row-major)
+ *   c2w_t = camera->c2w().matrix().block<3,1>(0,3).cast<float>() (camera.h:322:
+ *           the raytracer's ray origin, org_ray_w)
  *   fx, fy = focal_length(); cx, cy = principal_point(). */
 typedef struct {
   int32_t width, height;
@@ -110,6 +113,7 @@ typedef struct {
   float w2c_R[9];
   float w2c_t[3];
   float c2w_R[9];
+  float c2w_t[3];
 } ugu_gpu_camera;
 
 /* Output images of one view; NULL skips an output (Render's nullptr rule,
@@ -135,8 +139,12 @@ enum {
   UGU_GPU_DEVICE_POINTERS = 1u << 0, /* images are device pointers (else host) */
   UGU_GPU_PER_VIEW = 1u << 1,        /* one launch sequence per view (baseline) */
   UGU_GPU_ASYNC = 1u << 2,           /* do not synchronise (device pointers only) */
-  UGU_GPU_TIME_KERNELS = 1u << 3     /* time the per-tile raster kernel with CUDA events
+  UGU_GPU_TIME_KERNELS = 1u << 3,    /* time the per-tile raster kernel with CUDA events
                                         (ugu_gpu_stats.tile_kernel_ms); not with ASYNC */
+  UGU_GPU_RAYTRACE = 1u << 4         /* render with ugu::Raytracer's semantics
+                                        (src/renderer/cpu/raytracer.cc:127-224: naive BVH,
+                                        nearest double-precision ray hit) instead of
+                                        ugu::Rasterizer's */
 };
 
 /* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
@@ -193,6 +201,8 @@ UGU_GPU_API int ugu_gpu_render_views(ugu_gpu_context* ctx, int32_t n, const ugu_
 UGU_GPU_API int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                         uint32_t flags, ugu_gpu_plan** out);
 UGU_GPU_API int ugu_gpu_plan_launch(ugu_gpu_plan* plan);
+/* Also done by ugu_gpu_destroy for the plans of the context still alive:
+ * a plan must not be used or destroyed after its context. */
 UGU_GPU_API int ugu_gpu_plan_destroy(ugu_gpu_plan* plan);
 
 /* Backward of the per-pixel L2 loss sum_p |C(p) - T(p)|^2 over pixels with

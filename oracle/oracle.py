@@ -12,20 +12,28 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "liboracle.so")
 SRC = os.path.join(HERE, "raster_oracle.c")
+SRC_CC = os.path.join(HERE, "ray_oracle.cc")  # the raytracer's BVH (std::sort order)
 
 # -ffp-contract=off: every float operation rounds once, in source order, on
 # x86-64 and on aarch64 alike (GCC contracts to FMA by default on aarch64).
-CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+CFLAGS = ["-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
 
 
 def build(force: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     hdr = os.path.join(HERE, "raster_oracle.h")
+    srcs = (SRC, SRC_CC, hdr)
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(f) for f in srcs)):
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    subprocess.check_call(["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"])
+    oc, occ = tmp + ".c.o", tmp + ".cc.o"
+    subprocess.check_call(["gcc", *CFLAGS, "-c", SRC, "-o", oc])
+    subprocess.check_call(["g++", *CXXFLAGS, "-c", SRC_CC, "-o", occ])
+    subprocess.check_call(["g++", "-shared", oc, occ, "-o", tmp, "-lm"])
+    os.remove(oc)
+    os.remove(occ)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -53,7 +61,8 @@ class MeshS(C.Structure):
 class CameraS(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32),
                 ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
-                ("w2c_R", C.c_float * 9), ("w2c_t", C.c_float * 3), ("c2w_R", C.c_float * 9)]
+                ("w2c_R", C.c_float * 9), ("w2c_t", C.c_float * 3), ("c2w_R", C.c_float * 9),
+                ("c2w_t", C.c_float * 3)]
 
 
 class OptionS(C.Structure):
@@ -99,6 +108,8 @@ def load():
         lib.oracle_backward_f64.argtypes = [P, P, P, P, P, P, P, P, P]
         lib.oracle_backward_f64.restype = C.c_double
         lib.oracle_calc_normals.argtypes = [C.c_int32, P, C.c_int32, P, P, P]
+        lib.oracle_raytrace.argtypes = [P, P, P, C.c_float, P, P, P, P, P, P, P]
+        lib.oracle_raytrace.restype = C.c_int
         _lib = lib
     return _lib
 
@@ -174,6 +185,9 @@ def camera_struct(cam) -> CameraS:
         c.w2c_t[i] = float(x)
     for i, x in enumerate(np.asarray(cam.c2w_R, dtype=np.float32).reshape(-1)):
         c.c2w_R[i] = float(x)
+    c2w = np.eye(4) if getattr(cam, "c2w", None) is None else np.asarray(cam.c2w, np.float64)
+    for i, x in enumerate(c2w[:3, 3].astype(np.float32)):
+        c.c2w_t[i] = float(x)
     return c
 
 
@@ -216,6 +230,33 @@ def render(mesh, cam, opt, outputs=("color", "depth", "normal", "mask", "face_id
                            _ptr(out.get("face_id")), _ptr(out.get("color_f32")),
                            C.addressof(st))
     return rc, out, Stats(st.bbox_pixels, st.covered, st.special_candidates, st.texel_clamps)
+
+
+def raytrace(mesh, cam, opt, outputs=("color", "depth", "normal", "mask", "face_id"),
+             color_f32=False, depth_scale=None, sort_dependent=False):
+    """ugu::Raytracer's Render for one view; returns (status, images).  With
+    sort_dependent, images["sort_dependent"] marks the pixels whose face the
+    reference's std::sort picks among equal distances (more than 16 hits)."""
+    lib = load()
+    H, W = cam.height, cam.width
+    shapes = {"color": ((H, W, 3), np.uint8), "depth": ((H, W), np.float32),
+              "normal": ((H, W, 3), np.float32), "mask": ((H, W), np.uint8),
+              "face_id": ((H, W), np.int32)}
+    out = {k: np.empty(*shapes[k]) for k in outputs}
+    if color_f32:
+        out["color_f32"] = np.empty((H, W, 3), np.float32)
+    if sort_dependent:
+        out["sort_dependent"] = np.empty((H, W), np.uint8)
+    mh = _MeshHandle(mesh)
+    cs = camera_struct(cam)
+    os_ = option_struct(opt)
+    ds = float(getattr(opt, "depth_scale", 1.0) if depth_scale is None else depth_scale)
+    rc = lib.oracle_raytrace(C.addressof(mh.s), C.addressof(cs), C.addressof(os_), ds,
+                             _ptr(out.get("color")), _ptr(out.get("depth")),
+                             _ptr(out.get("normal")), _ptr(out.get("mask")),
+                             _ptr(out.get("face_id")), _ptr(out.get("color_f32")),
+                             _ptr(out.get("sort_dependent")))
+    return rc, out
 
 
 def ray_w(cam, x: int, y: int) -> np.ndarray:

@@ -412,6 +412,78 @@ int oracle_render(const oracle_mesh* m, const oracle_camera* cam,
 
 /* ------------------------------------------------------------------------ */
 /* FP64 recomputation (no reference counterpart: the error yardstick).       */
+/* ugu::Raytracer::Impl::Render (raytracer.cc:127-224), same validation and
+ * output initialisation as the rasterizer (util_private.cc:12-90). */
+int oracle_raytrace(const oracle_mesh* m, const oracle_camera* cam,
+                    const oracle_option* o, float depth_scale, uint8_t* color,
+                    float* depth, float* normal, uint8_t* mask, int32_t* face_id,
+                    float* color_f32, uint8_t* sort_dependent) {
+  int rc = validate(m, o, color, depth, normal, mask, face_id, color_f32);
+  if (rc) return rc;
+  const int W = cam->width, H = cam->height;
+  const size_t npx = (size_t)W * (size_t)H;
+  if (depth) for (size_t i = 0; i < npx; i++) depth[i] = 0.0f;
+  if (face_id) for (size_t i = 0; i < npx; i++) face_id[i] = -1;
+  if (color) memset(color, 0, 3 * npx);
+  if (normal) memset(normal, 0, 3 * npx * sizeof(float));
+  if (mask) memset(mask, 0, npx);
+  if (color_f32) memset(color_f32, 0, 3 * npx * sizeof(float));
+  if (sort_dependent) memset(sort_dependent, 0, npx);
+  void* bvh = oracle_bvh_build(m->vertices, m->num_faces, m->vertex_indices);
+  if (!bvh) return ORACLE_ERR_ALLOC;
+  float sigma_2 = o->oren_nayar_sigma * o->oren_nayar_sigma;
+  float on_A = 1.0f - (0.5f * sigma_2 / (sigma_2 + 0.33f));
+  float on_B = 0.45f * sigma_2 / (sigma_2 + 0.09f);
+  for (int y = 0; y < H; y++) {
+    for (int x = 0; x < W; x++) {
+      size_t p = (size_t)y * (size_t)W + (size_t)x;
+      float ray[3];
+      oracle_ray_w(cam, x, y, ray);
+      float t, u, v;
+      int32_t fid, sd = 0;
+      int hit = oracle_bvh_nearest(bvh, cam->c2w_t, ray, &t, &u, &v, &fid, &sd);
+      if (sort_dependent) sort_dependent[p] = (uint8_t)sd;
+      if (!hit) continue;
+      /* back face: the face normal points along the ray (:166-171) */
+      if (o->backface_culling && dot3(&m->face_normals[3 * fid], ray) > 0.0f) continue;
+      if (face_id) face_id[p] = fid;
+      if (mask) mask[p] = 255;
+      if (depth) {
+        float hw[3], hc2;
+        for (int k = 0; k < 3; k++) hw[k] = cam->c2w_t[k] + ray[k] * t;
+        hc2 = SUM3(cam->w2c_R[6] * hw[0], cam->w2c_R[7] * hw[1], cam->w2c_R[8] * hw[2]) +
+              cam->w2c_t[2];
+        depth[p] = hc2 * depth_scale;
+      }
+      float sn[3] = {0.0f, 0.0f, 0.0f};
+      if (o->shading_normal == 0) {
+        for (int k = 0; k < 3; k++) sn[k] = m->face_normals[3 * fid + k];
+      } else if (o->shading_normal == 1) {
+        /* (1.0f - u - v) * n0 + u * n1 + v * n2 (:196-199) */
+        const int32_t* ni = &m->normal_indices[3 * fid];
+        const float* n0 = &m->normals[3 * ni[0]];
+        const float* n1 = &m->normals[3 * ni[1]];
+        const float* n2 = &m->normals[3 * ni[2]];
+        float s = 1.0f - u - v;
+        for (int k = 0; k < 3; k++) sn[k] = (s * n0[k] + u * n1[k]) + v * n2[k];
+      }
+      if (normal) matvec3(cam->w2c_R, sn, &normal[3 * p]);
+      if (color || color_f32) {
+        uint8_t c[3];
+        shade_color(m, o, fid, u, v, ray, sn, on_A, on_B, c,
+                    color_f32 ? &color_f32[3 * p] : NULL, NULL);
+        if (color) {
+          color[3 * p + 0] = c[0];
+          color[3 * p + 1] = c[1];
+          color[3 * p + 2] = c[2];
+        }
+      }
+    }
+  }
+  oracle_bvh_free(bvh);
+  return ORACLE_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 
 typedef struct {

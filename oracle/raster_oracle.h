@@ -61,6 +61,8 @@ typedef struct {
   float w2c_R[9]; /* row-major, = camera->w2c().rotation().cast<float>() */
   float w2c_t[3]; /* = camera->w2c().translation().cast<float>() */
   float c2w_R[9]; /* row-major, = c2w block<3,3> cast to float */
+  float c2w_t[3]; /* = c2w block<3,1>(0,3) cast to float (camera.h:322), the
+                     raytracer's ray origin */
 } oracle_camera;
 
 typedef struct {
@@ -101,6 +103,23 @@ int oracle_render(const oracle_mesh* mesh, const oracle_camera* cam,
                   const oracle_option* opt, uint8_t* color, float* depth,
                   float* normal, uint8_t* mask, int32_t* face_id,
                   float* color_f32, oracle_stats* stats);
+
+/* ugu::Raytracer::Impl::Render (src/renderer/cpu/raytracer.cc:127-224):
+ * one ray per pixel through the naive BVH (ray_oracle.cc), nearest hit,
+ * back faces culled after the search, depth scaled by depth_scale.
+ * sort_dependent (H*W, or NULL) marks the pixels whose reported face the
+ * reference's std::sort decides among equal distances (ray_oracle.cc). */
+int oracle_raytrace(const oracle_mesh* mesh, const oracle_camera* cam,
+                    const oracle_option* opt, float depth_scale, uint8_t* color,
+                    float* depth, float* normal, uint8_t* mask, int32_t* face_id,
+                    float* color_f32, uint8_t* sort_dependent);
+
+/* ray_oracle.cc: ugu::BvhNaive over the mesh (NULL when it has no face) and
+ * its nearest hit along a ray (1 and t, u, v, face, or 0). */
+void* oracle_bvh_build(const float* vertices, int32_t num_faces, const int32_t* faces);
+void oracle_bvh_free(void* bvh);
+int oracle_bvh_nearest(const void* bvh, const float* org, const float* dir, float* t,
+                       float* u, float* v, int32_t* fid, int32_t* sort_dependent);
 
 /* The camera ray the reference tabulates (camera.h:438-448, 482-513). */
 void oracle_ray_w(const oracle_camera* cam, int32_t x, int32_t y, float out[3]);

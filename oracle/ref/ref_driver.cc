@@ -1,16 +1,18 @@
 // ref_driver.cc -- TEST INFRASTRUCTURE ONLY.
 //
-// A C entry point around the reference's own ugu::Rasterizer
-// (src/renderer/cpu/rasterizer.cc, compiled unmodified from the reference
-// checkout against the Eigen-compatible shim), used to pin the oracle's
-// restatement and to generate golden fixtures.  It builds a ugu::Mesh and a
-// ugu::PinholeCamera from plain arrays, calls Rasterizer::Render, and copies
-// the images out together with the camera floats Render derived.
+// C entry points around the reference's own ugu::Rasterizer and
+// ugu::Raytracer (src/renderer/cpu/rasterizer.cc and raytracer.cc, compiled
+// unmodified from the reference checkout against the Eigen-compatible shim),
+// used to pin the oracle's restatements and to generate golden fixtures.
+// Each builds a ugu::Mesh and a ugu::PinholeCamera from plain arrays, calls
+// Render, and copies the images out together with the camera floats Render
+// derived.
 #include <cstring>
 #include <memory>
 #include <vector>
 
 #include "ugu/renderer/cpu/rasterizer.h"
+#include "ugu/renderer/cpu/raytracer.h"
 
 namespace ugu {
 // The camera classes' vtables name these camera_util functions
@@ -51,14 +53,18 @@ struct ref_mesh {
 struct ref_option {
   int diffuse_color, interp, shading_normal, diffuse_shading, backface_culling;
   float oren_nayar_sigma;
+  float depth_scale;
 };
+
+}  // extern "C"
 
 // c2w: 4x4 row-major double.  cam_out: w2c_R[9], w2c_t[3], c2w_R[9] (row-major
 // floats) as Render and the ray table use them.
-int ref_render(const ref_mesh* m, int width, int height, float fx, float fy, float cx,
-               float cy, const double* c2w, const ref_option* o, unsigned char* color,
-               float* depth, float* normal, unsigned char* mask, int* face_id,
-               float* cam_out) {
+template <typename Renderer>
+static int render_with(const ref_mesh* m, int width, int height, float fx, float fy, float cx,
+                       float cy, const double* c2w, const ref_option* o, unsigned char* color,
+                       float* depth, float* normal, unsigned char* mask, int* face_id,
+                       float* cam_out) {
   ugu::set_log_level(ugu::LogLevel::kError);
   auto mesh = std::make_shared<ugu::Mesh>();
   std::vector<Eigen::Vector3f> v(m->num_vertices);
@@ -115,8 +121,9 @@ int ref_render(const ref_mesh* m, int width, int height, float fx, float fy, flo
   opt.diffuse_shading = static_cast<ugu::DiffuseShading>(o->diffuse_shading);
   opt.backface_culling = o->backface_culling != 0;
   opt.oren_nayar_sigma = o->oren_nayar_sigma;
+  opt.depth_scale = o->depth_scale;
 
-  ugu::Rasterizer r(opt);
+  Renderer r(opt);
   r.set_mesh(mesh);
   if (!r.PrepareMesh()) return 100;
   r.set_camera(cam);
@@ -147,6 +154,24 @@ int ref_render(const ref_mesh* m, int width, int height, float fx, float fy, flo
     for (int a = 0; a < 3; ++a) cam_out[9 + a] = t[a];
   }
   return 0;
+}
+
+extern "C" {
+
+int ref_render(const ref_mesh* m, int width, int height, float fx, float fy, float cx,
+               float cy, const double* c2w, const ref_option* o, unsigned char* color,
+               float* depth, float* normal, unsigned char* mask, int* face_id,
+               float* cam_out) {
+  return render_with<ugu::Rasterizer>(m, width, height, fx, fy, cx, cy, c2w, o, color, depth,
+                                      normal, mask, face_id, cam_out);
+}
+
+int ref_raytrace(const ref_mesh* m, int width, int height, float fx, float fy, float cx,
+                 float cy, const double* c2w, const ref_option* o, unsigned char* color,
+                 float* depth, float* normal, unsigned char* mask, int* face_id,
+                 float* cam_out) {
+  return render_with<ugu::Raytracer>(m, width, height, fx, fy, cx, cy, c2w, o, color, depth,
+                                     normal, mask, face_id, cam_out);
 }
 
 }  // extern "C"

@@ -41,7 +41,7 @@ class RefMesh(C.Structure):
 class RefOption(C.Structure):
     _fields_ = [("diffuse_color", C.c_int), ("interp", C.c_int), ("shading_normal", C.c_int),
                 ("diffuse_shading", C.c_int), ("backface_culling", C.c_int),
-                ("oren_nayar_sigma", C.c_float)]
+                ("oren_nayar_sigma", C.c_float), ("depth_scale", C.c_float)]
 
 
 _lib = None
@@ -54,10 +54,11 @@ def load():
             if build_if_available() is None:
                 return None
         lib = C.CDLL(LIB)
-        lib.ref_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float,
-                                   C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
-                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
-        lib.ref_render.restype = C.c_int
+        for f in (lib.ref_render, lib.ref_raytrace):
+            f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                          C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                          C.c_void_p, C.c_void_p, C.c_void_p]
+            f.restype = C.c_int
         _lib = lib
     return _lib
 
@@ -66,7 +67,15 @@ def render(mesh, cam, opt):
     """Render with the reference's Rasterizer.  Returns (rc, images, camera
     floats) where the camera floats are the w2c_R / w2c_t / c2w_R the
     reference derived from cam.c2w."""
-    lib = load()
+    return _render(load().ref_render, mesh, cam, opt)
+
+
+def raytrace(mesh, cam, opt):
+    """The same through the reference's Raytracer (naive BVH)."""
+    return _render(load().ref_raytrace, mesh, cam, opt)
+
+
+def _render(fn, mesh, cam, opt):
     keep = []
 
     def a(x, dt):
@@ -95,14 +104,14 @@ def render(mesh, cam, opt):
     m.tex = C.addressof(ptrs)
     o = RefOption(int(opt.diffuse_color), int(opt.interp), int(opt.shading_normal),
                   int(opt.diffuse_shading), 1 if opt.backface_culling else 0,
-                  float(opt.oren_nayar_sigma))
+                  float(opt.oren_nayar_sigma), float(getattr(opt, "depth_scale", 1.0)))
     H, W = cam.height, cam.width
     out = {"color": np.zeros((H, W, 3), np.uint8), "depth": np.zeros((H, W), np.float32),
            "normal": np.zeros((H, W, 3), np.float32), "mask": np.zeros((H, W), np.uint8),
            "face_id": np.zeros((H, W), np.int32)}
     c2w = np.ascontiguousarray(cam.c2w if cam.c2w is not None else np.eye(4), np.float64)
     camf = np.zeros(21, np.float32)
-    rc = lib.ref_render(C.addressof(m), W, H, cam.fx, cam.fy, cam.cx, cam.cy, c2w.ctypes.data,
+    rc = fn(C.addressof(m), W, H, cam.fx, cam.fy, cam.cx, cam.cy, c2w.ctypes.data,
                         C.addressof(o), out["color"].ctypes.data, out["depth"].ctypes.data,
                         out["normal"].ctypes.data, out["mask"].ctypes.data,
                         out["face_id"].ctypes.data, camf.ctypes.data)

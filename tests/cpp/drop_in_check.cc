@@ -1,11 +1,13 @@
 // drop_in_check.cc -- renders one scene with the reference's ugu::Rasterizer
-// and with ugu::RasterizerGpu (ugu_gb300/host) and counts differing bytes.
-// Built by tests/test_drop_in_cpu.py against the reference headers.
+// (ugu::Raytracer) and with ugu::RasterizerGpu (ugu::RaytracerGpu,
+// ugu_gb300/host) and counts differing bytes.  Built by
+// tests/test_drop_in_cpu.py against the reference headers.
 #include <cstring>
 #include <memory>
 
 #include "rasterizer_gpu.h"
 #include "ugu/renderer/cpu/rasterizer.h"
+#include "ugu/renderer/cpu/raytracer.h"
 
 namespace ugu {
 Eigen::Matrix4f GetProjectionMatrixOpenGlForPinhole(int, int, float, float, float, float,
@@ -28,11 +30,12 @@ static long diff(const ugu::Image<T>& a, const ugu::Image<T>& b) {
   return d;
 }
 
-extern "C" int drop_in_check(int nv, const float* v, int nf, const int* f, const float* fn,
-                             const float* vn, const float* vc, int nuv, const float* uv,
-                             const int* uvi, int tw, int th, const unsigned char* tex, int W,
-                             int H, float fx, float fy, float cx, float cy, const double* c2w,
-                             int dc, int interp, int sn, int shading, int cull, long* out6) {
+template <typename Ref, typename Gpu>
+static int check(int nv, const float* v, int nf, const int* f, const float* fn, const float* vn,
+                 const float* vc, int nuv, const float* uv, const int* uvi, int tw, int th,
+                 const unsigned char* tex, int W, int H, float fx, float fy, float cx, float cy,
+                 const double* c2w, int dc, int interp, int sn, int shading, int cull,
+                 float depth_scale, long* out6) {
   ugu::set_log_level(ugu::LogLevel::kError);
   auto mesh = std::make_shared<ugu::Mesh>();
   std::vector<Eigen::Vector3f> V(nv), N(nv), C(nv), FN(nf);
@@ -73,9 +76,10 @@ extern "C" int drop_in_check(int nv, const float* v, int nf, const int* f, const
   opt.shading_normal = static_cast<ugu::ShadingNormal>(sn);
   opt.diffuse_shading = static_cast<ugu::DiffuseShading>(shading);
   opt.backface_culling = cull != 0;
+  opt.depth_scale = depth_scale;
 
-  ugu::Rasterizer ref(opt);
-  ugu::RasterizerGpu gpu(opt);
+  Ref ref(opt);
+  Gpu gpu(opt);
   std::shared_ptr<ugu::RendererCpu> r0(&ref, [](ugu::RendererCpu*) {});
   std::shared_ptr<ugu::RendererCpu> r1(&gpu, [](ugu::RendererCpu*) {});
   ugu::Image3b c[2];
@@ -102,6 +106,27 @@ extern "C" int drop_in_check(int nv, const float* v, int nf, const int* f, const
   return 0;
 }
 
+extern "C" int drop_in_check(int nv, const float* v, int nf, const int* f, const float* fn,
+                             const float* vn, const float* vc, int nuv, const float* uv,
+                             const int* uvi, int tw, int th, const unsigned char* tex, int W,
+                             int H, float fx, float fy, float cx, float cy, const double* c2w,
+                             int dc, int interp, int sn, int shading, int cull, long* out6) {
+  return check<ugu::Rasterizer, ugu::RasterizerGpu>(nv, v, nf, f, fn, vn, vc, nuv, uv, uvi, tw,
+                                                    th, tex, W, H, fx, fy, cx, cy, c2w, dc,
+                                                    interp, sn, shading, cull, 1.0f, out6);
+}
+
+extern "C" int drop_in_check_ray(int nv, const float* v, int nf, const int* f, const float* fn,
+                                 const float* vn, const float* vc, int nuv, const float* uv,
+                                 const int* uvi, int tw, int th, const unsigned char* tex, int W,
+                                 int H, float fx, float fy, float cx, float cy, const double* c2w,
+                                 int dc, int interp, int sn, int shading, int cull,
+                                 float depth_scale, long* out6) {
+  return check<ugu::Raytracer, ugu::RaytracerGpu>(nv, v, nf, f, fn, vn, vc, nuv, uv, uvi, tw,
+                                                  th, tex, W, H, fx, fy, cx, cy, c2w, dc, interp,
+                                                  sn, shading, cull, depth_scale, out6);
+}
+
 // Error paths that need no backend: no camera, mesh not prepared.
 extern "C" int drop_in_errors() {
   ugu::set_log_level(ugu::LogLevel::kNone);
@@ -113,5 +138,9 @@ extern "C" int drop_in_errors() {
   if (gpu.PrepareMesh()) return 3;      // mesh has not been set
   ugu::Image1w dw;
   if (gpu.RenderW(nullptr, nullptr, nullptr, nullptr, nullptr)) return 4;
+  ugu::RaytracerGpu ray;
+  if (ray.PrepareMesh()) return 5;  // mesh has not been set
+  ray.set_mesh(std::make_shared<ugu::Mesh>());
+  if (ray.PrepareMesh()) return 6;  // mesh is empty
   return 0;
 }

@@ -72,8 +72,8 @@ int ugu_gpu_set_mesh(ugu_gpu_context* c, int32_t, const ugu_gpu_mesh* m) {
   c->has_mesh = true;
   return 0;
 }
-int ugu_gpu_render(ugu_gpu_context* c, int32_t, const ugu_gpu_camera* cam,
-                   const ugu_gpu_images* im) {
+static int fake_render(ugu_gpu_context* c, const ugu_gpu_camera* cam, const ugu_gpu_images* im,
+                       bool ray) {
   oracle_mesh m;
   std::memset(&m, 0, sizeof(m));
   m.num_vertices = c->nv;
@@ -106,16 +106,23 @@ int ugu_gpu_render(ugu_gpu_context* c, int32_t, const ugu_gpu_camera* cam,
   std::memcpy(oc.w2c_R, cam->w2c_R, sizeof(oc.w2c_R));
   std::memcpy(oc.w2c_t, cam->w2c_t, sizeof(oc.w2c_t));
   std::memcpy(oc.c2w_R, cam->c2w_R, sizeof(oc.c2w_R));
+  std::memcpy(oc.c2w_t, cam->c2w_t, sizeof(oc.c2w_t));
   oracle_option o{c->opt.diffuse_color, c->opt.interp, c->opt.shading_normal,
                   c->opt.diffuse_shading, c->opt.backface_culling, c->opt.oren_nayar_sigma};
-  int rc = oracle_render(&m, &oc, &o, im->color, im->depth, im->normal, im->mask, im->face_id,
-                         im->color_f32, nullptr);
+  int rc = ray ? oracle_raytrace(&m, &oc, &o, c->opt.depth_scale, im->color, im->depth,
+                                 im->normal, im->mask, im->face_id, im->color_f32, nullptr)
+               : oracle_render(&m, &oc, &o, im->color, im->depth, im->normal, im->mask,
+                               im->face_id, im->color_f32, nullptr);
   if (rc) c->err = "oracle validation failed";
   return rc;
 }
-int ugu_gpu_render_views(ugu_gpu_context* c, int32_t n, const ugu_gpu_view* v, uint32_t) {
+int ugu_gpu_render(ugu_gpu_context* c, int32_t, const ugu_gpu_camera* cam,
+                   const ugu_gpu_images* im) {
+  return fake_render(c, cam, im, false);
+}
+int ugu_gpu_render_views(ugu_gpu_context* c, int32_t n, const ugu_gpu_view* v, uint32_t flags) {
   for (int i = 0; i < n; ++i) {
-    int rc = ugu_gpu_render(c, v[i].mesh, &v[i].camera, &v[i].images);
+    int rc = fake_render(c, &v[i].camera, &v[i].images, (flags & UGU_GPU_RAYTRACE) != 0);
     if (rc) return rc;
   }
   return 0;

@@ -16,7 +16,8 @@ def to_option(opt) -> RendererCpuOption:
                              shading_normal=opt.shading_normal,
                              diffuse_shading=opt.diffuse_shading,
                              backface_culling=bool(opt.backface_culling),
-                             oren_nayar_sigma=opt.oren_nayar_sigma)
+                             oren_nayar_sigma=opt.oren_nayar_sigma,
+                             depth_scale=float(getattr(opt, "depth_scale", 1.0)))
 
 
 def host_images(cam, outputs=OUTPUTS):
@@ -37,6 +38,20 @@ def gpu_render(ctx: Context, mesh, cam, opt, slot=0, outputs=OUTPUTS, upload=Tru
     ctx.check(ctx.set_option(to_option(opt)))
     out, im = host_images(cam, outputs)
     rc = ctx.render(slot, cam, im)
+    return rc, out
+
+
+def gpu_raytrace(ctx: Context, mesh, cam, opt, slot=0, outputs=OUTPUTS, upload=True):
+    """One view through render_views with UGU_GPU_RAYTRACE, host buffers."""
+    if upload:
+        ctx.check(ctx.set_mesh(slot, mesh))
+    ctx.check(ctx.set_option(to_option(opt)))
+    out, im = host_images(cam, outputs)
+    v = capi.View()
+    v.mesh = slot
+    v.camera = capi.camera_struct(cam)
+    v.images = im
+    rc = ctx.render_views([v], capi.RAYTRACE)
     return rc, out
 
 

@@ -8,6 +8,7 @@ that checks its marshalling of ugu::Mesh / PinholeCamera / RendererCpuOption
 into include/ugu_gpu.h and the outputs back.  Linked against the real
 libugugpu.so without a GPU, every render must fail cleanly (false + LOGE)."""
 import ctypes as C
+import dataclasses
 import os
 import subprocess
 
@@ -28,12 +29,15 @@ OUT = os.path.join(ROOT, "oracle", "_ref")
 def _build(name, backend):
     os.makedirs(OUT, exist_ok=True)
     lib = os.path.join(OUT, name)
-    srcs = [f"{REF}/src/renderer/cpu/rasterizer.cc", f"{REF}/src/renderer/cpu/util_private.cc",
+    srcs = [f"{REF}/src/renderer/cpu/rasterizer.cc", f"{REF}/src/renderer/cpu/raytracer.cc",
+            f"{REF}/src/renderer/cpu/util_private.cc",
             f"{REF}/src/log.cc", f"{REF}/src/image.cc", f"{REF}/src/util/thread_util.cc",
             f"{REF}/src/common.cc", os.path.join(ROOT, "oracle/ref/mesh_min.cc"),
+            os.path.join(ROOT, "oracle/ref/geom_min.cc"),
             os.path.join(ROOT, "ugu_gb300/host/rasterizer_gpu.cc"),
             os.path.join(ROOT, "tests/cpp/drop_in_check.cc")]
-    inc = ["-I", os.path.join(ROOT, "oracle/ref/eigen_shim"), "-I", f"{REF}/include",
+    inc = ["-I", os.path.join(ROOT, "oracle/ref/override"),
+           "-I", os.path.join(ROOT, "oracle/ref/eigen_shim"), "-I", f"{REF}/include",
            "-I", f"{REF}/src", "-I", os.path.join(ROOT, "include"),
            "-I", os.path.join(ROOT, "ugu_gb300/host"), "-I", os.path.join(ROOT, "oracle")]
     extra = []
@@ -42,6 +46,7 @@ def _build(name, backend):
         subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-c",
                                os.path.join(ROOT, "oracle/raster_oracle.c"), "-o", obj])
         srcs.append(os.path.join(ROOT, "tests/cpp/fake_ugu_gpu.cc"))
+        srcs.append(os.path.join(ROOT, "oracle/ray_oracle.cc"))
         extra = [obj, "-lm"]
     else:
         from ugu_gb300 import build
@@ -57,7 +62,7 @@ def fake_lib():
     return _build("libdropin_fake.so", "fake")
 
 
-def run(lib, m, cam, opt):
+def run(lib, m, cam, opt, ray=False):
     f = lambda a, dt: np.ascontiguousarray(a, dt)  # noqa: E731
     arrs = [f(m.vertices, np.float32), f(m.vertex_indices, np.int32),
             f(m.face_normals, np.float32), f(m.normals, np.float32),
@@ -66,15 +71,17 @@ def run(lib, m, cam, opt):
     c2w = np.ascontiguousarray(cam.c2w if cam.c2w is not None else np.eye(4), np.float64)
     out = np.zeros(6, np.int64)
     P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
-    lib.drop_in_check.restype = C.c_int
-    rc = lib.drop_in_check(
+    fn = lib.drop_in_check_ray if ray else lib.drop_in_check
+    fn.restype = C.c_int
+    extra = (C.c_float(getattr(opt, "depth_scale", 1.0)),) if ray else ()
+    rc = fn(
         C.c_int(m.num_vertices), P(arrs[0]), C.c_int(m.num_faces), P(arrs[1]), P(arrs[2]),
         P(arrs[3]), P(arrs[4]), C.c_int(len(m.uv)), P(arrs[5]), P(arrs[6]),
         C.c_int(m.textures[0].shape[1]), C.c_int(m.textures[0].shape[0]), P(arrs[7]),
         C.c_int(cam.width), C.c_int(cam.height), C.c_float(cam.fx), C.c_float(cam.fy),
         C.c_float(cam.cx), C.c_float(cam.cy), P(c2w), C.c_int(opt.diffuse_color),
         C.c_int(opt.interp), C.c_int(opt.shading_normal), C.c_int(opt.diffuse_shading),
-        C.c_int(int(opt.backface_culling)), P(out))
+        C.c_int(int(opt.backface_culling)), *extra, P(out))
     return rc, out
 
 
@@ -94,6 +101,20 @@ def test_drop_in_matches_reference_soup(fake_lib):
     m = adv.triangle_soup(cam, n_faces=600, seed=4)
     rc, diffs = run(fake_lib, m, cam, adv.option(1, 1, 0, 1, False))
     assert rc == 0 and diffs.tolist() == [0] * 6
+
+
+@pytest.mark.parametrize("optname", ["vertex_vnormal_cull", "tex_bilinear_lambert",
+                                     "white_orennayar"])
+def test_raytracer_drop_in_matches_reference_ring_view(fake_lib, optname):
+    m = scenes.icosphere_textured(4, 64)
+    cam = scenes.ring_cameras(5, 3.0, [(120, 90)] * 5)[3]
+    opt = dataclasses.replace(adv.OPTIONS[optname]) if dataclasses.is_dataclass(
+        adv.OPTIONS[optname]) else type(adv.OPTIONS[optname])(**vars(adv.OPTIONS[optname]))
+    opt.depth_scale = 1.5
+    rc, diffs = run(fake_lib, m, cam, opt, ray=True)
+    assert rc == 0
+    assert diffs.tolist() == [0] * 6, dict(zip(["color", "depth", "normal", "mask", "face_id",
+                                                "depthW"], diffs.tolist()))
 
 
 def test_drop_in_error_paths(fake_lib):

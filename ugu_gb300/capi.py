@@ -31,6 +31,7 @@ DEVICE_POINTERS = 1
 PER_VIEW = 2
 ASYNC = 4
 TIME_KERNELS = 8
+RAYTRACE = 16
 
 P = C.c_void_p
 
@@ -60,7 +61,8 @@ class MeshDesc(C.Structure):
 class CameraDesc(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32),
                 ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
-                ("w2c_R", C.c_float * 9), ("w2c_t", C.c_float * 3), ("c2w_R", C.c_float * 9)]
+                ("w2c_R", C.c_float * 9), ("w2c_t", C.c_float * 3), ("c2w_R", C.c_float * 9),
+                ("c2w_t", C.c_float * 3)]
 
 
 class Images(C.Structure):
@@ -167,6 +169,9 @@ def camera_struct(cam) -> CameraDesc:
     c.w2c_R[:] = [float(x) for x in np.asarray(cam.w2c_R, np.float32).reshape(-1)]
     c.w2c_t[:] = [float(x) for x in np.asarray(cam.w2c_t, np.float32).reshape(-1)]
     c.c2w_R[:] = [float(x) for x in np.asarray(cam.c2w_R, np.float32).reshape(-1)]
+    # camera.h:322: c2w_t_f_ = c2w_.matrix().block<3, 1>(0, 3).cast<float>()
+    c2w = np.eye(4) if getattr(cam, "c2w", None) is None else np.asarray(cam.c2w, np.float64)
+    c.c2w_t[:] = [float(x) for x in c2w[:3, 3].astype(np.float32)]
     return c
 
 

@@ -38,6 +38,10 @@ struct MeshSlot {
   int tex0_w = 0, tex0_h = 0;
   float centre[3] = {0.0f, 0.0f, 0.0f};  // bounding-box centre of the vertices
   size_t bytes = 0;
+  // raytracer: host copies of positions and faces, its BVH built on first use
+  std::vector<float> h_vertices;
+  std::vector<int32_t> h_faces;
+  bool bvh = false;
 };
 
 // Device scratch of one render sequence.  A plan owns its own so that later
@@ -88,6 +92,7 @@ struct Group {
   int64_t faces;     // tiled path: faces summed over the group's views
   int64_t vertices;  // tiled path: vertices summed over the group's views
   int max_vertices;
+  int64_t ray_tiles;  // raytracer: the most kRayTileW x kRayTileH tiles of a view
 };
 
 }  // namespace
@@ -121,6 +126,10 @@ struct ugu_gpu_context {
   uint64_t large_items = 0;
   // counters of the last asynchronous plan replay, checked at synchronize
   ugu_gpu_plan* pending_plan = nullptr;
+  // set while a UGU_GPU_RAYTRACE render or plan is being prepared and enqueued
+  bool raytrace = false;
+  // plans created on this context and not destroyed yet (destroyed with it)
+  std::vector<ugu_gpu_plan*> plans;
 };
 
 struct ugu_gpu_plan {
@@ -130,6 +139,7 @@ struct ugu_gpu_plan {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int kernels = 0;
+  bool raytrace = false;
 };
 
 namespace {
@@ -341,6 +351,7 @@ void fill_cam(Cam& d, const ugu_gpu_camera& c) {
   std::memcpy(d.R, c.w2c_R, sizeof(d.R));
   std::memcpy(d.t, c.w2c_t, sizeof(d.t));
   std::memcpy(d.C, c.c2w_R, sizeof(d.C));
+  std::memcpy(d.T, c.c2w_t, sizeof(d.T));
 }
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -391,6 +402,9 @@ std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* 
     cur.max_vertices = std::max(cur.max_vertices, V);
     cur.max_pixels = std::max(cur.max_pixels, px);
     cur.tiles += tiles_of(views[i].camera, t.tile_log2);
+    cur.ray_tiles = std::max(cur.ray_tiles,
+                             (int64_t)((views[i].camera.width + kRayTileW - 1) / kRayTileW) *
+                                 ((views[i].camera.height + kRayTileH - 1) / kRayTileH));
     cur.faces += F;
     cur.vertices += V;
   }
@@ -597,6 +611,17 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
 
 // Enqueue one group's kernels (no synchronisation); returns how many.
 int enqueue_group(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) {
+  if (ctx->raytrace) {
+    RayParams p{};
+    p.meshes = ctx->d_meshes;
+    p.views = s.d_views + gr.first;
+    p.num_views = gr.count;
+    p.shade = shade_opts(ctx->opt);
+    p.backface_culling = ctx->opt.backface_culling ? 1 : 0;
+    p.depth_scale = ctx->opt.depth_scale;
+    launch_ray(p, gr.ray_tiles, ctx->stream);
+    return 1;
+  }
   if (ctx->tuning.path != UGU_GPU_PATH_GLOBAL) {
     TileParams p = tile_params(ctx, s, gr, gi);
     cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream);
@@ -757,6 +782,7 @@ int validate_views(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views) {
 
 int prepare_scratch(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
                     const ugu_gpu_view* views, int n, size_t out_bytes) {
+  if (ctx->raytrace) return ensure_scratch(ctx, s, 0, (size_t)n, groups.size(), out_bytes);
   int rc = ensure_scratch(ctx, s, (size_t)group_key_count(groups, views), (size_t)n,
                           groups.size(), out_bytes);
   if (rc || ctx->tuning.path == UGU_GPU_PATH_GLOBAL) return rc;
@@ -770,7 +796,7 @@ int prepare_scratch(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& 
 // render stream then waits for the last copy.
 int enqueue_render(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
                    const ugu_gpu_view* views, int n, bool dev, int* kernels) {
-  const bool global = ctx->tuning.path == UGU_GPU_PATH_GLOBAL;
+  const bool global = ctx->tuning.path == UGU_GPU_PATH_GLOBAL && !ctx->raytrace;
   if (global)
     CK(ctx, cudaMemsetAsync(s.counters, 0, groups.size() * sizeof(DevCounters), ctx->stream),
        "cudaMemsetAsync(counters)");
@@ -799,6 +825,7 @@ int enqueue_render(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& g
     CK(ctx, cudaEventRecord(done, ctx->copy_stream), "cudaEventRecord");
     CK(ctx, cudaStreamWaitEvent(ctx->stream, done, 0), "cudaStreamWaitEvent");
   }
+  if (ctx->raytrace) return UGU_GPU_OK;  // the ray kernel keeps no counters
   if (global)
     CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, groups.size() * sizeof(DevCounters),
                             cudaMemcpyDeviceToHost, ctx->stream),
@@ -810,12 +837,52 @@ int enqueue_render(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& g
   return UGU_GPU_OK;
 }
 
+// Raytracer::PrepareMesh (raytracer.cc:90-110) for one slot, on first use:
+// the naive BVH built on the host and uploaded with the mesh.
+int ensure_bvh(ugu_gpu_context* ctx, int slot) {
+  MeshSlot& s = ctx->meshes[slot];
+  if (s.bvh) return UGU_GPU_OK;
+  if (s.h_vertices.empty() || s.h_faces.empty())
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh is empty");
+  HostBvh hb;
+  if (!build_bvh(s.h_vertices.data(), s.h_faces.data(), (int)(s.h_faces.size() / 3), hb))
+    return set_error(ctx, UGU_GPU_ERR_CAPACITY, "BVH deeper than %d levels", kMaxBvhDepth);
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  int rc;
+  if ((rc = upload(ctx, s, hb.nodes, &s.dev.bvh_nodes))) return rc;
+  if ((rc = upload(ctx, s, hb.tris, &s.dev.bvh_tris))) return rc;
+  s.dev.bvh_depth = hb.depth;
+  s.dev.bvh_entries = (int32_t)(hb.tris.size() / 3);
+  CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &s.dev, sizeof(DevMesh), cudaMemcpyHostToDevice),
+     "cudaMemcpy(mesh table)");
+  s.bvh = true;
+  return UGU_GPU_OK;
+}
+
+// The raytracer mode of the context for the lifetime of one call.
+struct RayMode {
+  ugu_gpu_context* ctx;
+  RayMode(ugu_gpu_context* c, bool on) : ctx(c) { ctx->raytrace = on; }
+  ~RayMode() { ctx->raytrace = false; }
+};
+
+int ensure_bvhs(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views) {
+  for (int i = 0; i < n; ++i) {
+    int rc = ensure_bvh(ctx, views[i].mesh);
+    if (rc) return rc;
+  }
+  return UGU_GPU_OK;
+}
+
 int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t flags) {
   if (n < 0 || (n > 0 && !views))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view list");
   if (n == 0) return UGU_GPU_OK;
   int rc = validate_views(ctx, n, views);
   if (rc) return rc;
+  const bool ray = (flags & UGU_GPU_RAYTRACE) != 0;
+  if (ray && (rc = ensure_bvhs(ctx, n, views))) return rc;
+  RayMode mode(ctx, ray);
   const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
   if ((flags & UGU_GPU_ASYNC) && !dev)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "UGU_GPU_ASYNC needs device pointers");
@@ -856,6 +923,7 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
     ctx->launches += kernels;
     if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
     CK(ctx, cudaStreamSynchronize(ctx->stream), "render");
+    if (ray) return UGU_GPU_OK;
     rc = check_counters(ctx, s, groups.size());
     if (!rc)
       for (int g = 0; g < ctx->timed_groups; ++g) {
@@ -940,6 +1008,7 @@ int ugu_gpu_destroy(ugu_gpu_context* ctx) {
   if (!ctx) return UGU_GPU_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  while (!ctx->plans.empty()) ugu_gpu_plan_destroy(ctx->plans.back());
   for (MeshSlot& s : ctx->meshes) free_slot(s);
   free_scratch(ctx->scratch);
   cudaFree(ctx->d_meshes);
@@ -1100,6 +1169,8 @@ int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) 
   CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &d, sizeof(DevMesh), cudaMemcpyHostToDevice),
      "cudaMemcpy(mesh table)");
   for (int k = 0; k < 3; ++k) s.centre[k] = centre[k];
+  s.h_vertices.assign(m->vertices, m->vertices + 3 * V);
+  s.h_faces.assign(m->vertex_indices, m->vertex_indices + 3 * F);
   s.present = true;
   return UGU_GPU_OK;
 }
@@ -1134,8 +1205,12 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
   cudaSetDevice(ctx->device);
   int rc = validate_views(ctx, n, views);
   if (rc) return rc;
+  const bool ray = (flags & UGU_GPU_RAYTRACE) != 0;
+  if (ray && (rc = ensure_bvhs(ctx, n, views))) return rc;
+  RayMode mode(ctx, ray);
   ugu_gpu_plan* plan = new ugu_gpu_plan();
   plan->ctx = ctx;
+  plan->raytrace = ray;
   plan->groups = make_groups(ctx, n, views, (flags & UGU_GPU_PER_VIEW) != 0);
   Scratch& s = plan->scratch;
   rc = prepare_scratch(ctx, s, plan->groups, views, n, 0);
@@ -1146,7 +1221,7 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plan views");
   }
-  if (!rc && ctx->tuning.path != UGU_GPU_PATH_GLOBAL) rc = size_tiled(ctx, s, plan->groups);
+  if (!rc && !ray && ctx->tuning.path != UGU_GPU_PATH_GLOBAL) rc = size_tiled(ctx, s, plan->groups);
   if (!rc) {
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaStreamBeginCapture");
@@ -1169,6 +1244,7 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
     delete plan;
     return rc;
   }
+  ctx->plans.push_back(plan);
   *out = plan;
   return UGU_GPU_OK;
 }
@@ -1188,6 +1264,7 @@ int ugu_gpu_plan_destroy(ugu_gpu_plan* plan) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->pending_plan == plan) ctx->pending_plan = nullptr;
+  ctx->plans.erase(std::remove(ctx->plans.begin(), ctx->plans.end(), plan), ctx->plans.end());
   cudaGraphExecDestroy(plan->exec);
   cudaGraphDestroy(plan->graph);
   free_scratch(plan->scratch);
@@ -1201,6 +1278,7 @@ int ugu_gpu_synchronize(ugu_gpu_context* ctx) {
   if (ctx->pending_plan) {
     ugu_gpu_plan* p = ctx->pending_plan;
     ctx->pending_plan = nullptr;
+    if (p->raytrace) return UGU_GPU_OK;
     return check_counters(ctx, p->scratch, p->groups.size());
   }
   return UGU_GPU_OK;

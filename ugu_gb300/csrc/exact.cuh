@@ -59,6 +59,7 @@ struct Cam {
   float R[9];  // w2c rotation, row-major (float cast of w2c().rotation())
   float t[3];  // w2c translation
   float C[9];  // c2w rotation, row-major (PinholeCamera::c2w_R_f_)
+  float T[3];  // c2w translation (PinholeCamera::c2w_t_f_), the raytracer's ray origin
 };
 
 // Loop A (rasterizer.cc:131-136) and PinholeCamera::Project

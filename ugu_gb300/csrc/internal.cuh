@@ -13,6 +13,8 @@
 // pointers.  Z-buffer: one 64-bit key per pixel of the current view group.
 #pragma once
 
+#include <vector>
+
 #include <cstdint>
 
 #include "exact.cuh"
@@ -47,6 +49,14 @@ struct DevMesh {
   const int4* vidx_ranked;
   const int4* vidx_morton;
   const float4* fnormals_morton;
+  // Raytracer only (built on first use): the naive BVH flattened in
+  // depth-first order, 2 float4 per node, and its leaf entries in that
+  // order, 3 float4 per entry (an entry's index is its rank in the
+  // reference's traversal order).  NULL until built.
+  const float4* bvh_nodes;
+  const float4* bvh_tris;
+  int32_t bvh_depth;    // deepest node (root = 0)
+  int32_t bvh_entries;
 };
 
 struct DevView {
@@ -160,6 +170,32 @@ struct BackwardParams {
   void* proj64;                 // per view (DevView::proj_offset), 32 bytes per vertex: screen
                                 // x, y projected in double as hi + lo floats, and 1/z
 };
+
+// Raytracer (ray.cu): the views of one group, one thread per pixel.
+struct RayParams {
+  const DevMesh* meshes;
+  const DevView* views;
+  int32_t num_views;
+  ShadeOpts shade;
+  int32_t backface_culling;
+  float depth_scale;
+};
+
+// Deepest BVH node the traversal stack holds (a median split of 2^60 faces).
+constexpr int kMaxBvhDepth = 60;
+
+// Host copy of a mesh's BVH (bvh.cu): 2 float4 per node, 3 per leaf entry.
+struct HostBvh {
+  std::vector<float4> nodes, tris;
+  int depth = 0;
+};
+// Builds ugu::BvhNaive's tree for the mesh; false when it is deeper than
+// kMaxBvhDepth or the mesh has no face.
+bool build_bvh(const float* vertices, const int32_t* faces, int num_faces, HostBvh& out);
+// One block per kRayTileW x kRayTileH pixels; max_tiles = the most tiles of
+// any view of the group.
+constexpr int kRayTileW = 16, kRayTileH = 8;
+void launch_ray(const RayParams& p, int64_t max_tiles, cudaStream_t s);
 
 // Host-side launcher (backward.cu): the hi + lo projection table (when
 // position gradients are asked for), then the per-pixel backward.

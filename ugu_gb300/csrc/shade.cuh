@@ -1,6 +1,7 @@
 // shade.cuh -- Loop C of ugu's rasterizer for one pixel (rasterizer.cc:254-299)
 // and the pixel shaders (pixel_shader.h:215-422), in the reference's FP32
-// operation order.  Shared by the global-z-buffer path and the tiled path.
+// operation order.  Shared by the global-z-buffer path, the tiled path and
+// the raytracer.
 #pragma once
 
 #include "internal.cuh"
@@ -31,36 +32,18 @@ __device__ __forceinline__ void fetch_texel(const DevTexture& t, int64_t i, floa
 }
 
 
-// Loop C body for a pixel whose final face id is > 0 (rasterizer.cc:254-299),
-// given the winning face's projected vertices and area.
-__device__ __forceinline__ void shade_face_pixel(const ShadeOpts& p, const DevMesh& m,
-                                                 const Cam& c, int fid, const FaceSetup& s,
-                                                 int x, int y, Shaded& out) {
-  Bary w = edges_at(s, x, y);
-  perspective(s, w);
-
-  // shading normal (:268-279) and its camera-frame copy (:282-289)
-  float sn[3] = {0.0f, 0.0f, 0.0f};
-  if (p.shading_normal == 0) {
-    float4 fn = __ldg(&m.fnormals[fid]);
-    sn[0] = fn.x;
-    sn[1] = fn.y;
-    sn[2] = fn.z;
-  } else {
-    int4 ni = __ldg(&m.nidx[fid]);
-    float4 n0 = __ldg(&m.normals[ni.x]);
-    float4 n1 = __ldg(&m.normals[ni.y]);
-    float4 n2 = __ldg(&m.normals[ni.z]);
-    sn[0] = fadd(fadd(fmul(w.w0, n0.x), fmul(w.w1, n1.x)), fmul(w.w2, n2.x));
-    sn[1] = fadd(fadd(fmul(w.w0, n0.y), fmul(w.w1, n1.y)), fmul(w.w2, n2.y));
-    sn[2] = fadd(fadd(fmul(w.w0, n0.z), fmul(w.w1, n1.z)), fmul(w.w2, n2.z));
-  }
+// The pixel shader of one pixel (pixel_shader.h:215-422) given the face,
+// the colorizer's (u, v), the world-frame shading normal sn and the pixel;
+// also the camera-frame normal w2c_R * sn (rasterizer.cc:282-289,
+// raytracer.cc:192-199).
+__device__ __forceinline__ void shade_uv(const ShadeOpts& p, const DevMesh& m, const Cam& c,
+                                         int fid, float u, float v, const float sn[3], int x,
+                                         int y, Shaded& out) {
   out.n[0] = dot3(c.R[0], c.R[1], c.R[2], sn[0], sn[1], sn[2]);
   out.n[1] = dot3(c.R[3], c.R[4], c.R[5], sn[0], sn[1], sn[2]);
   out.n[2] = dot3(c.R[6], c.R[7], c.R[8], sn[0], sn[1], sn[2]);
 
-  // colorizer: u = w1, v = w2, weights (1 - u - v), u, v
-  const float u = w.w1, v = w.w2;
+  // colorizer: weights (1 - u - v), u, v
   const float s0 = fsub(fsub(1.0f, u), v);
   float col[3] = {255.0f, 255.0f, 255.0f};
   if (p.diffuse_color == 2) {  // pixel_shader.h:234-256
@@ -140,6 +123,34 @@ __device__ __forceinline__ void shade_face_pixel(const ShadeOpts& p, const DevMe
       for (int k = 0; k < 3; ++k) out.c[k] = f2u8(fmul(coeff, (float)out.c[k]));
     }
   }
+}
+
+// Loop C body for a pixel whose final face id is > 0 (rasterizer.cc:254-299),
+// given the winning face's projected vertices and area.
+__device__ __forceinline__ void shade_face_pixel(const ShadeOpts& p, const DevMesh& m,
+                                                 const Cam& c, int fid, const FaceSetup& s,
+                                                 int x, int y, Shaded& out) {
+  Bary w = edges_at(s, x, y);
+  perspective(s, w);
+
+  // shading normal (:268-279) from the stored weights
+  float sn[3] = {0.0f, 0.0f, 0.0f};
+  if (p.shading_normal == 0) {
+    float4 fn = __ldg(&m.fnormals[fid]);
+    sn[0] = fn.x;
+    sn[1] = fn.y;
+    sn[2] = fn.z;
+  } else {
+    int4 ni = __ldg(&m.nidx[fid]);
+    float4 n0 = __ldg(&m.normals[ni.x]);
+    float4 n1 = __ldg(&m.normals[ni.y]);
+    float4 n2 = __ldg(&m.normals[ni.z]);
+    sn[0] = fadd(fadd(fmul(w.w0, n0.x), fmul(w.w1, n1.x)), fmul(w.w2, n2.x));
+    sn[1] = fadd(fadd(fmul(w.w0, n0.y), fmul(w.w1, n1.y)), fmul(w.w2, n2.y));
+    sn[2] = fadd(fadd(fmul(w.w0, n0.z), fmul(w.w1, n1.z)), fmul(w.w2, n2.z));
+  }
+  // the colorizer's u = w1, v = w2
+  shade_uv(p, m, c, fid, w.w1, w.w2, sn, x, y, out);
 }
 
 

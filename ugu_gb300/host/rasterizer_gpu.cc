@@ -30,12 +30,14 @@ bool FillCamera(const Camera& cam, ugu_gpu_camera* out) {
   const Eigen::Matrix3f w2c_R = cam.w2c().rotation().cast<float>();
   const Eigen::Vector3f w2c_t = cam.w2c().translation().cast<float>();
   const Eigen::Matrix3f c2w_R = cam.c2w().matrix().block<3, 3>(0, 0).cast<float>();
+  const Eigen::Vector3f c2w_t = cam.c2w().matrix().block<3, 1>(0, 3).cast<float>();
   for (int r = 0; r < 3; ++r) {
     for (int c = 0; c < 3; ++c) {
       out->w2c_R[3 * r + c] = w2c_R(r, c);
       out->c2w_R[3 * r + c] = c2w_R(r, c);
     }
     out->w2c_t[r] = w2c_t[r];
+    out->c2w_t[r] = c2w_t[r];
   }
   return true;
 }
@@ -55,6 +57,7 @@ class RasterizerGpu::Impl {
   RendererCpuOption option_;
   ugu_gpu_context* ctx_{nullptr};
   int device_{0};
+  uint32_t flags_{0};  // UGU_GPU_RAYTRACE for RaytracerGpu
 
   explicit Impl(int device) : device_(device) {}
   ~Impl() { ugu_gpu_destroy(ctx_); }
@@ -163,7 +166,11 @@ class RasterizerGpu::Impl {
     im.mask = mask ? mask->data : nullptr;
     im.face_id = face_id ? reinterpret_cast<int32_t*>(face_id->data) : nullptr;
     im.color_f32 = nullptr;
-    const int rc = ugu_gpu_render(ctx_, 0, &cam, &im);
+    ugu_gpu_view v;
+    v.mesh = 0;
+    v.camera = cam;
+    v.images = im;
+    const int rc = ugu_gpu_render_views(ctx_, 1, &v, flags_);
     if (rc != UGU_GPU_OK) {
       LOGE("%s\n", ugu_gpu_last_error(ctx_));
       return false;
@@ -173,6 +180,15 @@ class RasterizerGpu::Impl {
 };
 
 RasterizerGpu::RasterizerGpu() : pimpl_(new Impl(0)) {}
+
+void RasterizerGpu::set_render_flags(uint32_t flags) { pimpl_->flags_ = flags; }
+
+bool RasterizerGpu::has_mesh() const { return pimpl_->mesh_ != nullptr; }
+
+bool RasterizerGpu::has_mesh_data() const {
+  return pimpl_->mesh_ != nullptr && !pimpl_->mesh_->vertices().empty() &&
+         !pimpl_->mesh_->vertex_indices().empty();
+}
 RasterizerGpu::~RasterizerGpu() {}
 RasterizerGpu::RasterizerGpu(const RendererCpuOption& option, int device)
     : pimpl_(new Impl(device)) {
@@ -283,12 +299,30 @@ bool RasterizerGpu::RenderViews(const std::vector<std::shared_ptr<const Camera>>
       Resize(&(*face_ids)[i], w, h),
           im.face_id = reinterpret_cast<int32_t*>((*face_ids)[i].data);
   }
-  const int rc = ugu_gpu_render_views(p.ctx_, static_cast<int32_t>(n), views.data(), 0);
+  const int rc = ugu_gpu_render_views(p.ctx_, static_cast<int32_t>(n), views.data(), p.flags_);
   if (rc != UGU_GPU_OK) {
     LOGE("%s\n", ugu_gpu_last_error(p.ctx_));
     return false;
   }
   return true;
+}
+
+RaytracerGpu::RaytracerGpu() : RasterizerGpu() { set_render_flags(UGU_GPU_RAYTRACE); }
+
+RaytracerGpu::RaytracerGpu(const RendererCpuOption& option, int device)
+    : RasterizerGpu(option, device) {
+  set_render_flags(UGU_GPU_RAYTRACE);
+}
+
+// raytracer.cc:90-110: "mesh has not been set" (reported by the base), then
+// "mesh is empty"; the BVH itself is built on the device side at the first
+// render.
+bool RaytracerGpu::PrepareMesh() {
+  if (has_mesh() && !has_mesh_data()) {
+    LOGE("mesh is empty\n");
+    return false;
+  }
+  return RasterizerGpu::PrepareMesh();
 }
 
 }  // namespace ugu

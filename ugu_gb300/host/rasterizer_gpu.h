@@ -11,9 +11,14 @@
  * GPU by the kernels behind include/ugu_gpu.h and copied back before Render
  * returns.  Only PinholeCamera is supported (OpenCvCamera's distortion and
  * OrthoCamera are rejected with an error).
+ *
+ * ugu::RaytracerGpu is the same drop-in for ugu::Raytracer
+ * (include/ugu/renderer/cpu/raytracer.h:14-53): its renders cast one ray per
+ * pixel through the reference's naive BVH (UGU_GPU_RAYTRACE).
  */
 #pragma once
 
+#include <cstdint>
 #include <memory>
 #include <vector>
 
@@ -59,6 +64,21 @@ class RasterizerGpu : public RendererCpu {
                    std::vector<Image3b>* colors, std::vector<Image1f>* depths,
                    std::vector<Image3f>* normals, std::vector<Image1b>* masks,
                    std::vector<Image1i>* face_ids) const;
+
+ protected:
+  // UGU_GPU_* flags added to every render (RaytracerGpu: UGU_GPU_RAYTRACE).
+  void set_render_flags(uint32_t flags);
+  bool has_mesh() const;       // a mesh was set
+  bool has_mesh_data() const;  // ... with vertices and faces
+};
+
+class RaytracerGpu : public RasterizerGpu {
+ public:
+  RaytracerGpu();
+  explicit RaytracerGpu(const RendererCpuOption& option, int device = 0);
+
+  // raytracer.cc:90-110: fails on a missing or empty mesh.
+  bool PrepareMesh() override;
 };
 
 }  // namespace ugu

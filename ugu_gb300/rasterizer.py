@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import sys
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -83,9 +84,12 @@ class Context:
             raise capi.GpuError(rc, self.lib.ugu_gpu_last_error(None).decode())
         self.h = h
         self._uploads = {}
+        self._plans = weakref.WeakSet()
 
     def close(self):
         if getattr(self, "h", None):
+            for p in list(getattr(self, "_plans", ())):  # the library frees them with ctx
+                p.h = None
             self.lib.ugu_gpu_destroy(self.h)
             self.h = None
 
@@ -128,7 +132,9 @@ class Context:
         h = C.c_void_p()
         self.check(self.lib.ugu_gpu_plan_create(self.h, len(views), C.addressof(arr), int(flags),
                                                 C.byref(h)))
-        return Plan(self, h)
+        plan = Plan(self, h)
+        self._plans.add(plan)
+        return plan
 
     def synchronize(self) -> int:
         return self.lib.ugu_gpu_synchronize(self.h)
@@ -188,7 +194,7 @@ class Plan:
         return self.ctx.lib.ugu_gpu_plan_launch(self.h)
 
     def close(self):
-        if self.h:
+        if self.h:  # None once closed here or with its context
             self.ctx.lib.ugu_gpu_plan_destroy(self.h)
             self.h = None
 
@@ -272,11 +278,14 @@ class Rasterizer:
         im = capi.Images()
         for k, v in outs.items():
             setattr(im, k, None if v is None else v.ctypes.data)
-        rc = self._ctx.render(0, self._camera, im)
+        rc = self._render(im)
         if rc != capi.OK:
             LOGE(self._ctx.last_error())
             return False, {}
         return True, {k: v for k, v in outs.items() if v is not None}
+
+    def _render(self, im: capi.Images) -> int:
+        return self._ctx.render(0, self._camera, im)
 
     def RenderColor(self):
         return self.Render(color=True)
@@ -294,7 +303,7 @@ class Rasterizer:
         return self.Render(face_id=True)
 
     def RenderW(self, color=None, depth=True, normal=None, mask=None, face_id=None):
-        """rasterizer.cc:329-344: float depth converted by ConvertTo
+        """rasterizer.cc:329-344 (raytracer.cc:241-256): float depth converted by ConvertTo
         (image_proc.h:454-...) with scale 1: static_cast<uint16_t>(double)."""
         if depth is None:
             LOGE("depth is nullptr")
@@ -306,6 +315,29 @@ class Rasterizer:
 
     def RenderDepthW(self):
         return self.RenderW(depth=True)
+
+
+class Raytracer(Rasterizer):
+    """ugu::Raytracer's interface over the GPU (raytracer.h:14-53,
+    src/renderer/cpu/raytracer.cc): the same RendererCpu methods; Render
+    casts one ray per pixel through the naive BVH (built on the device side
+    at the first Render after PrepareMesh) instead of rasterising."""
+
+    def PrepareMesh(self) -> bool:  # raytracer.cc:90-110
+        if self._mesh is None:
+            LOGE("mesh has not been set\n")
+            return False
+        if len(self._mesh.vertices) == 0 or len(self._mesh.vertex_indices) == 0:
+            LOGE("mesh is empty\n")
+            return False
+        return super().PrepareMesh()
+
+    def _render(self, im: capi.Images) -> int:
+        v = capi.View()
+        v.mesh = 0
+        v.camera = capi.camera_struct(self._camera)
+        v.images = im
+        return self._ctx.render_views([v], capi.RAYTRACE)
 
 
 def depth_to_u16(depth: np.ndarray) -> np.ndarray:
