@@ -154,16 +154,6 @@ __device__ __forceinline__ int mt_decide(const MtFloat& q) {
   return 0;
 }
 
-// Leaf triangles: false only when the double test certainly misses, or
-// certainly hits at a float t greater than best_t.
-__device__ __forceinline__ bool maybe_hit(float3 o, float3 d, float3 a, float3 b, float3 c,
-                                          float best_t) {
-  const MtFloat q = mt_float(o, d, a, b, c);
-  if (mt_decide(q) < 0) return false;
-  if (q.lo > 0.0f && q.tn - q.et > q.hi * best_t * (1.0f + 4e-6f)) return false;
-  return true;
-}
-
 // The reference's box test (bvh_naive.h:232-238): the ray against the 12
 // triangles of the box mesh (bvh_base.h:23-80) with the double test; the
 // box counts as hit when any triangle is.  Corners: bit 0/1/2 set = max
@@ -180,9 +170,16 @@ __device__ __forceinline__ float3 box_corner(float4 lo, float4 hi, int k) {
   return make_float3(c & 1 ? hi.x : lo.x, c & 2 ? hi.y : lo.y, c & 4 ? hi.z : lo.z);
 }
 
-__device__ __noinline__ bool reference_box_hit(float4 lo, float4 hi, float3 o, float3 d) {
-  unsigned undecided = 0;
+// Triangles of the box mesh per face: x min, x max, y min, y max, z min,
+// z max (bvh_base.h:23-80 lists y max, y min, x max, x min, z min, z max).
+__constant__ unsigned char kFaceTri[6] = {6, 4, 2, 0, 8, 10};
+
+// The rest of the reference box test: the triangles not in `done`
+// classified in float, then the double test for every undecided one.
+__device__ __noinline__ bool reference_box_rest(float4 lo, float4 hi, float3 o, float3 d,
+                                                unsigned done, unsigned undecided) {
   for (int i = 0; i < 12; ++i) {
+    if (done >> i & 1u) continue;
     const float3 a = box_corner(lo, hi, kBoxTri[i][0]);
     const float3 b = box_corner(lo, hi, kBoxTri[i][1]);
     const float3 c = box_corner(lo, hi, kBoxTri[i][2]);
@@ -202,6 +199,26 @@ __device__ __noinline__ bool reference_box_hit(float4 lo, float4 hi, float3 o, f
   return false;
 }
 
+// face = 2 * axis + (1 for the max side): the face the slab test says the
+// ray enters through (or leaves through, from inside).  Its two triangles
+// decide almost every box; the other ten only run when neither of them is
+// certainly hit.
+__device__ __forceinline__ bool reference_box_hit(float4 lo, float4 hi, float3 o, float3 d,
+                                                  int face) {
+  const int t0 = kFaceTri[face];
+  unsigned undecided = 0;
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int i = t0 + j;
+    const int r = mt_decide(mt_float(o, d, box_corner(lo, hi, kBoxTri[i][0]),
+                                     box_corner(lo, hi, kBoxTri[i][1]),
+                                     box_corner(lo, hi, kBoxTri[i][2])));
+    if (r > 0) return true;
+    if (r == 0) undecided |= 1u << i;
+  }
+  return reference_box_rest(lo, hi, o, d, 3u << t0, undecided);
+}
+
 // One axis of the slab test: the ray's parameters at the two planes.  A
 // ray parallel to the axis (|d| < 1e-30: it moves less than 1e-23 over any
 // distance a hit can have) is inside the slab for every t when lo <= o <=
@@ -218,22 +235,61 @@ __device__ __forceinline__ void slab(float lo, float hi, float o, float d, float
   }
 }
 
-// Conservative slab test: false only when the ray certainly misses the box
-// at t >= 0 or certainly enters it beyond best_t (strictly, in float).
-// Each finite t is within 2e-7 of the exact plane crossing; the margins
-// below take 1e-6.  An infinite tn (a miss) turns into NaN and fails the
-// comparisons, as it should.
-__device__ __forceinline__ bool box_hit(float4 lo, float4 hi, float3 o, float3 d, float3 inv,
-                                        float best_t) {
-  float tx0, tx1, ty0, ty1, tz0, tz1;
-  slab(lo.x, hi.x, o.x, d.x, inv.x, tx0, tx1);
-  slab(lo.y, hi.y, o.y, d.y, inv.y, ty0, ty1);
-  slab(lo.z, hi.z, o.z, d.z, inv.z, tz0, tz1);
-  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-  tn -= 1e-6f * fabsf(tn);
-  tf += 1e-6f * fabsf(tf);
-  return tn <= tf && tf >= 0.0f && !(tn > best_t * (1.0f + 4e-6f));
+// Conservative slab test: -1 when the ray certainly misses the box at
+// t >= 0 or certainly enters it beyond best_t (strictly, in float); else
+// the face it enters through (leaves through, when tn < 0), as
+// 2 * axis + (1 for the max side).  Each finite t is within 2e-7 of the
+// exact plane crossing; the margins below take 1e-6.  An infinite tn (a
+// miss) turns into NaN and fails the comparisons, as it should.
+__device__ __forceinline__ int box_hit(float4 lo, float4 hi, float3 o, float3 d, float3 inv,
+                                       float best_t, float& t_enter) {
+  float t0[3], t1[3];
+  slab(lo.x, hi.x, o.x, d.x, inv.x, t0[0], t1[0]);
+  slab(lo.y, hi.y, o.y, d.y, inv.y, t0[1], t1[1]);
+  slab(lo.z, hi.z, o.z, d.z, inv.z, t0[2], t1[2]);
+  const float D[3] = {d.x, d.y, d.z};
+  float tn = -INFINITY, tf = INFINITY;
+  int an = 0, af = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float mn = fminf(t0[k], t1[k]), mx = fmaxf(t0[k], t1[k]);
+    if (mn > tn) tn = mn, an = k;
+    if (mx < tf) tf = mx, af = k;
+  }
+  const float tnc = tn - 1e-6f * fabsf(tn);
+  const float tfc = tf + 1e-6f * fabsf(tf);
+  if (!(tnc <= tfc && tfc >= 0.0f && !(tnc > best_t * (1.0f + 4e-6f)))) return -1;
+  t_enter = tnc;
+  return tn >= 0.0f ? 2 * an + (D[an] > 0.0f ? 0 : 1) : 2 * af + (D[af] > 0.0f ? 1 : 0);
+}
+
+// True when the reference's box test certainly hits: the ray crosses the
+// plane of `face` at t > 0 at a point well inside the face, clear of its
+// edges and of the diagonal that splits it into the box mesh's two
+// triangles, and the face's determinant |d_k| * (its two side lengths) is
+// above the test's epsilon.  The double test's own rounding (~1e-16 of the
+// magnitudes) is far inside the float margins used here.  Diagonals
+// (bvh_base.h:23-80, in face coordinates s, u of the two other axes in
+// x, y, z order): y faces s = u, x and z faces s + u = 1.
+__device__ __forceinline__ bool face_certain(float4 lo, float4 hi, float3 o, float3 d, float3 inv,
+                                             int face) {
+  const int k = face >> 1;
+  const float L[3] = {lo.x, lo.y, lo.z}, H[3] = {hi.x, hi.y, hi.z};
+  const float O[3] = {o.x, o.y, o.z}, D[3] = {d.x, d.y, d.z}, I[3] = {inv.x, inv.y, inv.z};
+  if (fabsf(D[k]) < 1e-30f) return false;
+  const float t = ((face & 1 ? H[k] : L[k]) - O[k]) * I[k];
+  if (!(t > 0.0f)) return false;
+  const int i = k == 0 ? 1 : 0, j = k == 2 ? 1 : 2;  // the face's axes, in order
+  const float di = H[i] - L[i], dj = H[j] - L[j];
+  if (!(di > 0.0f && dj > 0.0f) || di * dj * fabsf(D[k]) * (1.0f - 1e-5f) < 1.01f * (float)kDetEps)
+    return false;
+  const float pi = O[i] + t * D[i], pj = O[j] + t * D[j];
+  const float ms = 2e-6f * (fabsf(O[i]) + fabsf(t * D[i]) + fabsf(L[i]) + fabsf(H[i])) / di + 1e-6f;
+  const float mu = 2e-6f * (fabsf(O[j]) + fabsf(t * D[j]) + fabsf(L[j]) + fabsf(H[j])) / dj + 1e-6f;
+  const float sc = (pi - L[i]) / di, uc = (pj - L[j]) / dj;
+  if (!(sc > ms && sc < 1.0f - ms && uc > mu && uc < 1.0f - mu)) return false;
+  const float diag = k == 1 ? sc - uc : sc + uc - 1.0f;
+  return fabsf(diag) > ms + mu;
 }
 
 struct RayHit {
@@ -243,51 +299,136 @@ struct RayHit {
 
 __device__ __forceinline__ float3 ld3(const float4& q) { return make_float3(q.x, q.y, q.z); }
 
+// Bounds [t_lo, t_hi] on the double test's t for a triangle the float test
+// did not reject (t_hi = inf when the sign of det is undecided).
+__device__ __forceinline__ void t_bounds(const MtFloat& q, float& t_lo, float& t_hi) {
+  if (q.lo > 0.0f) {
+    t_lo = fmaxf(0.0f, (q.tn - q.et) / q.hi) * (1.0f - 1e-6f);
+    t_hi = (q.tn + q.et) / q.lo * (1.0f + 1e-6f);
+  } else {
+    t_lo = 0.0f;
+    t_hi = INFINITY;
+  }
+}
+
+// A triangle whose t is certainly above bound (1 + 4e-6) has a float t
+// strictly above every float t <= bound: it can neither win nor tie.
+__device__ __forceinline__ bool beyond(float t_lo, float bound) {
+  return t_lo > bound * (1.0f + 4e-6f);
+}
+
+constexpr int kCand = 8;
+
+// The double test on the pending candidates, nearest lower bound first,
+// while one can still win or tie; updates the hit and the bound.
+__device__ __forceinline__ void resolve(const DevMesh& m, float3 o, float3 d, int* ce, float* cl,
+                                        int& n, RayHit& h, float& bound) {
+  while (n > 0) {
+    int j = 0;
+    for (int k = 1; k < n; ++k)
+      if (cl[k] < cl[j]) j = k;
+    if (beyond(cl[j], bound)) break;  // so is every other candidate
+    const int e = ce[j];
+    ce[j] = ce[n - 1];
+    cl[j] = cl[n - 1];
+    --n;
+    const float4 q0 = __ldg(&m.bvh_tris[3 * e]);
+    float t, u, v;
+    if (!moller_trumbore_f64(o, d, ld3(q0), ld3(__ldg(&m.bvh_tris[3 * e + 1])),
+                             ld3(__ldg(&m.bvh_tris[3 * e + 2])), t, u, v))
+      continue;
+    if (t < h.t || (t == h.t && e < h.rank)) {
+      h.t = t;
+      h.u = u;
+      h.v = v;
+      h.rank = e;
+      h.fid = __float_as_int(q0.w);
+      bound = fminf(bound, t);
+    }
+  }
+  n = 0;
+}
+
 // Nearest hit of the ray in the mesh's BVH: the smallest float t, ties to
-// the lowest rank (the reference's depth-first collection order).
+// the lowest rank (the reference's depth-first collection order).  The
+// traversal classifies triangles in float only; a certain hit bounds the
+// nearest t (and prunes boxes), and the triangles that could still win or
+// tie wait in a short list for the double test, run once per ray after the
+// traversal (a full list is resolved on the spot).
 __device__ RayHit trace(const DevMesh& m, float3 o, float3 d) {
   RayHit h;
   h.t = INFINITY;
   h.u = h.v = 0.0f;
   h.rank = INT_MAX;
   h.fid = -1;
+  float bound = INFINITY;  // >= the smallest double-test t among the hits seen
+  int ce[kCand];
+  float cl[kCand];
+  int nc = 0;
   const float3 inv = make_float3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);  // used where |d| >= 1e-30
+  // stack entries: node << 3 | face (the face the slab test picked), and the
+  // node's entry t, the pruning key once a closer hit is known
   int stack[kStack];
+  float stack_t[kStack];
   int sp = 0;
-  stack[sp++] = 0;
+  {
+    float t0;
+    const int f = box_hit(__ldg(&m.bvh_nodes[0]), __ldg(&m.bvh_nodes[1]), o, d, inv, bound, t0);
+    if (f >= 0) {
+      stack[0] = f;
+      stack_t[0] = t0;
+      sp = 1;
+    }
+  }
   while (sp > 0) {
-    const int n = stack[--sp];
+    --sp;
+    if (beyond(stack_t[sp], bound)) continue;
+    const int n = stack[sp] >> 3, face = stack[sp] & 7;
     const float4 lo = __ldg(&m.bvh_nodes[2 * n]);
     const float4 hi = __ldg(&m.bvh_nodes[2 * n + 1]);
-    if (!box_hit(lo, hi, o, d, inv, h.t)) continue;
     const int a = __float_as_int(lo.w), b = __float_as_int(hi.w);
-    if (a >= 0) {  // internal: the left child is traversed first
+    if (a >= 0) {
       // the reference descends only when its own box test hits; the slab
-      // test above passed every box it can hit, not only those
-      if (!reference_box_hit(lo, hi, o, d)) continue;
+      // test passed every box it can hit, not only those
+      if (!face_certain(lo, hi, o, d, inv, face) && !reference_box_hit(lo, hi, o, d, face))
+        continue;
+      // children slab-tested here and pushed far first; the reference's
+      // left-first order only matters through the ranks
+      float ta, tb;
+      const int fa = box_hit(__ldg(&m.bvh_nodes[2 * a]), __ldg(&m.bvh_nodes[2 * a + 1]), o, d,
+                             inv, bound, ta);
+      const int fb = box_hit(__ldg(&m.bvh_nodes[2 * b]), __ldg(&m.bvh_nodes[2 * b + 1]), o, d,
+                             inv, bound, tb);
       if (sp + 2 > kStack) break;  // deeper than built trees go
-      stack[sp++] = b;
-      stack[sp++] = a;
+      const bool a_first = fa >= 0 && (fb < 0 || ta <= tb);
+      if (a_first) {
+        if (fb >= 0) stack[sp] = b << 3 | fb, stack_t[sp++] = tb;
+        stack[sp] = a << 3 | fa, stack_t[sp++] = ta;
+      } else {
+        if (fa >= 0) stack[sp] = a << 3 | fa, stack_t[sp++] = ta;
+        if (fb >= 0) stack[sp] = b << 3 | fb, stack_t[sp++] = tb;
+      }
       continue;
     }
     const int first = -1 - a;
     for (int e = first; e < first + b; ++e) {
-      const float4 q0 = __ldg(&m.bvh_tris[3 * e]);
-      const float3 v0 = ld3(q0);
+      const float3 v0 = ld3(__ldg(&m.bvh_tris[3 * e]));
       const float3 v1 = ld3(__ldg(&m.bvh_tris[3 * e + 1]));
       const float3 v2 = ld3(__ldg(&m.bvh_tris[3 * e + 2]));
-      if (!maybe_hit(o, d, v0, v1, v2, h.t)) continue;
-      float t, u, v;
-      if (!moller_trumbore_f64(o, d, v0, v1, v2, t, u, v)) continue;
-      if (t < h.t || (t == h.t && e < h.rank)) {
-        h.t = t;
-        h.u = u;
-        h.v = v;
-        h.rank = e;
-        h.fid = __float_as_int(q0.w);
-      }
+      const MtFloat q = mt_float(o, d, v0, v1, v2);
+      const int r = mt_decide(q);
+      if (r < 0) continue;
+      float tl, th;
+      t_bounds(q, tl, th);
+      if (beyond(tl, bound)) continue;
+      if (r > 0) bound = fminf(bound, th);
+      if (nc == kCand) resolve(m, o, d, ce, cl, nc, h, bound);
+      ce[nc] = e;
+      cl[nc] = tl;
+      ++nc;
     }
   }
+  resolve(m, o, d, ce, cl, nc, h, bound);
   return h;
 }
 
