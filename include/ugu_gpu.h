@@ -147,6 +147,52 @@ enum {
                                         ugu::Rasterizer's */
 };
 
+/* The image helpers ugu's examples apply to a render
+ * (examples/ex02_renderer.cc:146-154), in one device pass per item:
+ *   vis_depth   = Depth2Gray(depth, min_d, max_d)   src/util/image_util.cc:392-411
+ *   vis_normal  = Normal2Color(normal, gl_coord)    image_util.cc:413-446 (RGB order)
+ *   vis_face_id = FaceId2RandomColor(face_id)       image_util.cc:448-487 (RGB order)
+ *   depth_u16   = ConvertTo<uint16_t>(depth)        include/ugu/image_proc.h:453-...
+ * An output is written when it and its input are non-NULL.  Depth2Gray's
+ * defaults are min_d = 200, max_d = 1500. */
+typedef struct {
+  int32_t width, height;
+  const float* depth;      /* H*W */
+  const float* normal;     /* H*W*3 */
+  const int32_t* face_id;  /* H*W */
+  uint8_t* vis_depth;      /* H*W */
+  uint16_t* depth_u16;     /* H*W */
+  uint8_t* vis_normal;     /* H*W*3 */
+  uint8_t* vis_face_id;    /* H*W*3 */
+  float min_d, max_d;
+  int32_t gl_coord;
+} ugu_gpu_vis;
+
+/* G-buffer channels of a render, the layout of ugu::GBuffer
+ * (include/ugu/renderer/base.h:34-77) as RendererGl reads it back
+ * (src/renderer/gl/renderer.cc:541-646), computed from the rasterizer's own
+ * interpolation at each pixel of the face a render reported (face_id, an
+ * input).  With w the pixel's perspective-correct weights (rasterizer.cc:
+ * 208-224) and (u, v) = (w1, w2):
+ *   pos_wld    = w0 P0 + w1 P1 + w2 P2           pos_cam    = w2c_t + w2c_R pos_wld
+ *   normal_wld = normalize(shading normal)       normal_cam = w2c_R normal_wld
+ *   bary       = (u, v, 1 - u - v)               uv = (t, s, 1 - t - s), the
+ *                                                  texture coordinate (zeros without uv)
+ *   stencil    = 255 where face_id >= 0.
+ * Pixels with face_id < 0 get zeros.  Any output may be NULL. */
+typedef struct {
+  int32_t mesh;
+  ugu_gpu_camera camera;
+  const int32_t* face_id;  /* H*W, input */
+  float* pos_wld;          /* H*W*3 */
+  float* pos_cam;          /* H*W*3 */
+  float* normal_wld;       /* H*W*3 */
+  float* normal_cam;       /* H*W*3 */
+  float* bary;             /* H*W*3 */
+  float* uv;               /* H*W*3 */
+  uint8_t* stencil;        /* H*W */
+} ugu_gpu_gbuffer;
+
 /* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
 typedef struct {
   int32_t path;             /* UGU_GPU_PATH_TILED (default) or UGU_GPU_PATH_GLOBAL */
@@ -225,6 +271,18 @@ UGU_GPU_API int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_
                      ugu_gpu_tuning* chosen);
 
 UGU_GPU_API int ugu_gpu_get_stats(const ugu_gpu_context* ctx, ugu_gpu_stats* stats);
+
+/* The helpers of ugu_gpu_vis for n items; UGU_GPU_DEVICE_POINTERS for device
+ * buffers (else host buffers, staged through the device); synchronous. */
+UGU_GPU_API int ugu_gpu_visualize(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_vis* items,
+                                  uint32_t flags);
+
+/* The G-buffer channels of n views (ugu_gpu_gbuffer) with the context's
+ * option (shading normal); UGU_GPU_DEVICE_POINTERS for device buffers (else
+ * host, staged); synchronous.  A face id outside [-1, num_faces) is an
+ * error (UGU_GPU_ERR_INDEX_OUT_OF_RANGE), its pixel left at zeros. */
+UGU_GPU_API int ugu_gpu_render_gbuffer(ugu_gpu_context* ctx, int32_t n,
+                                       const ugu_gpu_gbuffer* views, uint32_t flags);
 UGU_GPU_API int ugu_gpu_synchronize(ugu_gpu_context* ctx);
 /* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
 UGU_GPU_API int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream);

@@ -13,6 +13,7 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "liboracle.so")
 SRC = os.path.join(HERE, "raster_oracle.c")
 SRC_CC = os.path.join(HERE, "ray_oracle.cc")  # the raytracer's BVH (std::sort order)
+SRC_VIS = os.path.join(HERE, "vis_oracle.cc")  # image helpers (std::mt19937, std::round)
 
 # -ffp-contract=off: every float operation rounds once, in source order, on
 # x86-64 and on aarch64 alike (GCC contracts to FMA by default on aarch64).
@@ -23,17 +24,18 @@ CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
 def build(force: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     hdr = os.path.join(HERE, "raster_oracle.h")
-    srcs = (SRC, SRC_CC, hdr)
+    srcs = (SRC, SRC_CC, SRC_VIS, hdr)
     if (not force and os.path.exists(LIB_PATH)
             and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(f) for f in srcs)):
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    oc, occ = tmp + ".c.o", tmp + ".cc.o"
+    oc, occ, ovis = tmp + ".c.o", tmp + ".cc.o", tmp + ".vis.o"
     subprocess.check_call(["gcc", *CFLAGS, "-c", SRC, "-o", oc])
     subprocess.check_call(["g++", *CXXFLAGS, "-c", SRC_CC, "-o", occ])
-    subprocess.check_call(["g++", "-shared", oc, occ, "-o", tmp, "-lm"])
-    os.remove(oc)
-    os.remove(occ)
+    subprocess.check_call(["g++", *CXXFLAGS, "-c", SRC_VIS, "-o", ovis])
+    subprocess.check_call(["g++", "-shared", oc, occ, ovis, "-o", tmp, "-lm"])
+    for f in (oc, occ, ovis):
+        os.remove(f)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -110,6 +112,11 @@ def load():
         lib.oracle_calc_normals.argtypes = [C.c_int32, P, C.c_int32, P, P, P]
         lib.oracle_raytrace.argtypes = [P, P, P, C.c_float, P, P, P, P, P, P, P]
         lib.oracle_raytrace.restype = C.c_int
+        lib.oracle_visualize.argtypes = [C.c_int32, C.c_int32, P, P, P, P, P, P, P, C.c_float,
+                                         C.c_float, C.c_int32]
+        lib.oracle_visualize.restype = None
+        lib.oracle_gbuffer.argtypes = [P] * 11
+        lib.oracle_gbuffer.restype = C.c_int64
         _lib = lib
     return _lib
 
@@ -257,6 +264,51 @@ def raytrace(mesh, cam, opt, outputs=("color", "depth", "normal", "mask", "face_
                              _ptr(out.get("face_id")), _ptr(out.get("color_f32")),
                              _ptr(out.get("sort_dependent")))
     return rc, out
+
+
+def visualize(depth=None, normal=None, face_id=None, min_d=200.0, max_d=1500.0,
+              gl_coord=False):
+    """Depth2Gray, ConvertTo<uint16_t>, Normal2Color and FaceId2RandomColor
+    of ugu's image_util for the given images; returns a dict."""
+    lib = load()
+    shp = next(a for a in (depth, normal, face_id) if a is not None).shape
+    H, W = shp[0], shp[1]
+    d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+    n = None if normal is None else np.ascontiguousarray(normal, np.float32)
+    f = None if face_id is None else np.ascontiguousarray(face_id, np.int32)
+    out = {}
+    if d is not None:
+        out["vis_depth"] = np.zeros((H, W), np.uint8)
+        out["depth_u16"] = np.zeros((H, W), np.uint16)
+    if n is not None:
+        out["vis_normal"] = np.zeros((H, W, 3), np.uint8)
+    if f is not None:
+        out["vis_face_id"] = np.zeros((H, W, 3), np.uint8)
+    lib.oracle_visualize(W, H, _ptr(d), _ptr(n), _ptr(f), _ptr(out.get("vis_depth")),
+                         _ptr(out.get("depth_u16")), _ptr(out.get("vis_normal")),
+                         _ptr(out.get("vis_face_id")), float(min_d), float(max_d),
+                         1 if gl_coord else 0)
+    return out
+
+
+GBUFFER = ("pos_wld", "pos_cam", "normal_wld", "normal_cam", "bary", "uv")
+
+
+def gbuffer(mesh, cam, opt, face_id):
+    """The G-buffer channels of the faces a render reported; returns
+    (number of face ids out of range, dict of images)."""
+    lib = load()
+    H, W = cam.height, cam.width
+    out = {k: np.zeros((H, W, 3), np.float32) for k in GBUFFER}
+    out["stencil"] = np.zeros((H, W), np.uint8)
+    fid = np.ascontiguousarray(face_id, np.int32)
+    mh = _MeshHandle(mesh)
+    cs = camera_struct(cam)
+    os_ = option_struct(opt)
+    bad = lib.oracle_gbuffer(C.addressof(mh.s), C.addressof(cs), C.addressof(os_),
+                             fid.ctypes.data, *[out[k].ctypes.data for k in GBUFFER],
+                             out["stencil"].ctypes.data)
+    return int(bad), out
 
 
 def ray_w(cam, x: int, y: int) -> np.ndarray:

@@ -412,6 +412,96 @@ int oracle_render(const oracle_mesh* m, const oracle_camera* cam,
 
 /* ------------------------------------------------------------------------ */
 /* FP64 recomputation (no reference counterpart: the error yardstick).       */
+int64_t oracle_gbuffer(const oracle_mesh* m, const oracle_camera* cam,
+                       const oracle_option* o, const int32_t* face_id, float* pos_wld,
+                       float* pos_cam, float* normal_wld, float* normal_cam, float* bary,
+                       float* uv, uint8_t* stencil) {
+  const int W = cam->width, H = cam->height;
+  int64_t bad = 0;
+  for (int y = 0; y < H; y++) {
+    for (int x = 0; x < W; x++) {
+      const size_t p = (size_t)y * (size_t)W + (size_t)x;
+      const int fid = face_id[p];
+      float pw[3] = {0, 0, 0}, pc[3] = {0, 0, 0}, nw[3] = {0, 0, 0}, nc[3] = {0, 0, 0};
+      float b3[3] = {0, 0, 0}, t3[3] = {0, 0, 0};
+      uint8_t st = 0;
+      if (fid < -1 || fid >= m->num_faces) {
+        bad++;
+      } else if (fid >= 0) {
+        st = 255;
+        const int32_t* f = &m->vertex_indices[3 * fid];
+        float v0[3], v1[3], v2[3];
+        project_vertex(cam, &m->vertices[3 * f[0]], v0);
+        project_vertex(cam, &m->vertices[3 * f[1]], v1);
+        project_vertex(cam, &m->vertices[3 * f[2]], v2);
+        const float area = edge_fn(v0[0], v0[1], v1[0], v1[1], v2[0], v2[1]);
+        const float px = (float)x, py = (float)y;
+        float w0 = edge_fn(v1[0], v1[1], v2[0], v2[1], px, py);
+        float w1 = edge_fn(v2[0], v2[1], v0[0], v0[1], px, py);
+        float w2 = edge_fn(v0[0], v0[1], v1[0], v1[1], px, py);
+        w0 = w0 / area;
+        w1 = w1 / area;
+        w2 = w2 / area;
+        w0 = w0 / v0[2];
+        w1 = w1 / v1[2];
+        w2 = w2 / v2[2];
+        const float z = 1.0f / (w0 + w1 + w2);
+        w0 = w0 * z;
+        w1 = w1 * z;
+        w2 = w2 * z;
+        b3[0] = w1;
+        b3[1] = w2;
+        b3[2] = 1.f - w1 - w2;
+        const float* P0 = &m->vertices[3 * f[0]];
+        const float* P1 = &m->vertices[3 * f[1]];
+        const float* P2 = &m->vertices[3 * f[2]];
+        for (int k = 0; k < 3; k++) pw[k] = (w0 * P0[k] + w1 * P1[k]) + w2 * P2[k];
+        /* w2c_t + (w2c_R * wld) */
+        matvec3(cam->w2c_R, pw, pc);
+        for (int k = 0; k < 3; k++) pc[k] = cam->w2c_t[k] + pc[k];
+        float sn[3];
+        if (o->shading_normal == 0) {
+          for (int k = 0; k < 3; k++) sn[k] = m->face_normals[3 * fid + k];
+        } else {
+          const int32_t* ni = &m->normal_indices[3 * fid];
+          const float* n0 = &m->normals[3 * ni[0]];
+          const float* n1 = &m->normals[3 * ni[1]];
+          const float* n2 = &m->normals[3 * ni[2]];
+          for (int k = 0; k < 3; k++) sn[k] = (w0 * n0[k] + w1 * n1[k]) + w2 * n2[k];
+        }
+        const float n2s = dot3(sn, sn);
+        if (n2s > 0.0f) {
+          const float r = sqrtf(n2s);
+          for (int k = 0; k < 3; k++) nw[k] = sn[k] / r;
+        } else {
+          for (int k = 0; k < 3; k++) nw[k] = sn[k];
+        }
+        matvec3(cam->w2c_R, nw, nc);
+        if (m->num_uv > 0 && m->num_uv_indices > 0) {
+          const float s0 = 1.0f - w1 - w2;
+          const int32_t* ti = &m->uv_indices[3 * fid];
+          const float* a = &m->uv[2 * ti[0]];
+          const float* b = &m->uv[2 * ti[1]];
+          const float* d = &m->uv[2 * ti[2]];
+          t3[0] = (s0 * a[0] + w1 * b[0]) + w2 * d[0];
+          t3[1] = (s0 * a[1] + w1 * b[1]) + w2 * d[1];
+          t3[2] = 1.f - t3[0] - t3[1];
+        }
+      }
+      for (int k = 0; k < 3; k++) {
+        if (pos_wld) pos_wld[3 * p + k] = pw[k];
+        if (pos_cam) pos_cam[3 * p + k] = pc[k];
+        if (normal_wld) normal_wld[3 * p + k] = nw[k];
+        if (normal_cam) normal_cam[3 * p + k] = nc[k];
+        if (bary) bary[3 * p + k] = b3[k];
+        if (uv) uv[3 * p + k] = t3[k];
+      }
+      if (stencil) stencil[p] = st;
+    }
+  }
+  return bad;
+}
+
 /* ugu::Raytracer::Impl::Render (raytracer.cc:127-224), same validation and
  * output initialisation as the rasterizer (util_private.cc:12-90). */
 int oracle_raytrace(const oracle_mesh* m, const oracle_camera* cam,

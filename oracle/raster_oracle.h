@@ -114,6 +114,17 @@ int oracle_raytrace(const oracle_mesh* mesh, const oracle_camera* cam,
                     float* depth, float* normal, uint8_t* mask, int32_t* face_id,
                     float* color_f32, uint8_t* sort_dependent);
 
+/* The G-buffer channels (include/ugu_gpu.h, ugu_gpu_gbuffer) of the faces a
+ * render reported: the rasterizer's perspective-correct weights at each
+ * pixel (rasterizer.cc:201-224) applied to positions, the shading normal
+ * (normalised) and the texture coordinates; the layout of ugu::GBuffer
+ * (include/ugu/renderer/base.h:34-77) as src/renderer/gl/renderer.cc:541-646
+ * fills it.  Returns the number of face ids outside [-1, F). */
+int64_t oracle_gbuffer(const oracle_mesh* mesh, const oracle_camera* cam,
+                       const oracle_option* opt, const int32_t* face_id, float* pos_wld,
+                       float* pos_cam, float* normal_wld, float* normal_cam, float* bary,
+                       float* uv, uint8_t* stencil);
+
 /* ray_oracle.cc: ugu::BvhNaive over the mesh (NULL when it has no face) and
  * its nearest hit along a ray (1 and t, u, v, face, or 0). */
 void* oracle_bvh_build(const float* vertices, int32_t num_faces, const int32_t* faces);

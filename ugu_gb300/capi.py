@@ -96,7 +96,7 @@ EXPORTS = [
     "ugu_gpu_plan_create", "ugu_gpu_plan_launch", "ugu_gpu_plan_destroy", "ugu_gpu_backward",
     "ugu_gpu_set_tuning", "ugu_gpu_get_tuning", "ugu_gpu_autotune", "ugu_gpu_get_stats",
     "ugu_gpu_synchronize", "ugu_gpu_set_stream", "ugu_gpu_render_noalloc",
-    "ugu_gpu_get_device_mesh",
+    "ugu_gpu_get_device_mesh", "ugu_gpu_visualize", "ugu_gpu_render_gbuffer",
 ]
 
 NOALLOC_MAX_PIXELS = 2097152
@@ -149,6 +149,8 @@ def load(path: str | None = None):
     lib.ugu_gpu_render_noalloc.argtypes = [C.POINTER(DeviceMesh), C.POINTER(Option),
                                            C.POINTER(CameraDesc), C.POINTER(Images), P]
     lib.ugu_gpu_get_device_mesh.argtypes = [P, C.c_int32, C.POINTER(DeviceMesh)]
+    lib.ugu_gpu_visualize.argtypes = [P, C.c_int32, P, C.c_uint32]
+    lib.ugu_gpu_render_gbuffer.argtypes = [P, C.c_int32, P, C.c_uint32]
     for name in EXPORTS:
         if name != "ugu_gpu_last_error":
             getattr(lib, name).restype = C.c_int
@@ -160,6 +162,23 @@ class GpuError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"ugu_gpu error {code}: {msg}")
         self.code = code
+
+
+class Vis(C.Structure):
+    """ugu_gpu_vis: the image helpers of one render (include/ugu_gpu.h)."""
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32),
+                ("depth", P), ("normal", P), ("face_id", P),
+                ("vis_depth", P), ("depth_u16", P), ("vis_normal", P), ("vis_face_id", P),
+                ("min_d", C.c_float), ("max_d", C.c_float), ("gl_coord", C.c_int32)]
+
+
+GBUFFER = ("pos_wld", "pos_cam", "normal_wld", "normal_cam", "bary", "uv")
+
+
+class GBufferView(C.Structure):
+    """ugu_gpu_gbuffer: G-buffer channels of one rendered view."""
+    _fields_ = [("mesh", C.c_int32), ("camera", CameraDesc), ("face_id", P)]
+    _fields_ += [(k, P) for k in GBUFFER] + [("stencil", P)]
 
 
 def camera_struct(cam) -> CameraDesc:

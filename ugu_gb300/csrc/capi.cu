@@ -130,6 +130,12 @@ struct ugu_gpu_context {
   bool raytrace = false;
   // plans created on this context and not destroyed yet (destroyed with it)
   std::vector<ugu_gpu_plan*> plans;
+  // device staging of ugu_gpu_visualize / ugu_gpu_render_gbuffer with host
+  // buffers, and the G-buffer pass's bad-id counter (device, then pinned)
+  uint8_t* vis_buf = nullptr;
+  size_t vis_cap = 0;
+  unsigned long long* gbuf_bad = nullptr;
+  unsigned long long* h_gbuf_bad = nullptr;
 };
 
 struct ugu_gpu_plan {
@@ -1016,6 +1022,9 @@ int ugu_gpu_destroy(ugu_gpu_context* ctx) {
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->tile_events) cudaEventDestroy(e);
+  cudaFree(ctx->vis_buf);
+  cudaFree(ctx->gbuf_bad);
+  cudaFreeHost(ctx->h_gbuf_bad);
   delete ctx;
   return UGU_GPU_OK;
 }
@@ -1505,6 +1514,176 @@ int ugu_gpu_get_device_mesh(ugu_gpu_context* ctx, int32_t slot, ugu_gpu_device_m
   out->uv_indices4 = reinterpret_cast<const int32_t*>(d.uvidx);
   out->material_ids = d.mat_ids;
   out->materials = m.dev_tex.empty() ? nullptr : m.dev_tex.data();
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_visualize(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_vis* items,
+                      uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  if (n < 0 || (n > 0 && !items))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad item list");
+  cudaSetDevice(ctx->device);
+  const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
+  for (int k = 0; k < n; ++k) {
+    ugu_gpu_vis it = items[k];
+    if (it.width < 0 || it.height < 0)
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "item %d: negative size", k);
+    const size_t px = (size_t)it.width * (size_t)it.height;
+    if (px == 0) continue;
+    if (!dev) {
+      // inputs and outputs staged in one device buffer, 256-byte aligned parts
+      struct Part {
+        const void* in;
+        void* out;
+        size_t bytes;
+      };
+      const Part parts[7] = {{it.depth, nullptr, 4 * px},
+                             {it.normal, nullptr, 12 * px},
+                             {it.face_id, nullptr, 4 * px},
+                             {nullptr, it.vis_depth, px},
+                             {nullptr, it.depth_u16, 2 * px},
+                             {nullptr, it.vis_normal, 3 * px},
+                             {nullptr, it.vis_face_id, 3 * px}};
+      size_t total = 0;
+      for (const Part& q : parts)
+        if (q.in || q.out) total += align256(q.bytes);
+      if (total > ctx->vis_cap) {
+        cudaFree(ctx->vis_buf);
+        ctx->vis_buf = nullptr;
+        ctx->vis_cap = 0;
+        CK(ctx, cudaMalloc(&ctx->vis_buf, total), "cudaMalloc(visualize staging)");
+        ctx->vis_cap = total;
+      }
+      void* dptr[7] = {};
+      size_t off = 0;
+      for (int j = 0; j < 7; ++j) {
+        if (!parts[j].in && !parts[j].out) continue;
+        dptr[j] = ctx->vis_buf + off;
+        off += align256(parts[j].bytes);
+        if (parts[j].in)
+          CK(ctx, cudaMemcpyAsync(dptr[j], parts[j].in, parts[j].bytes, cudaMemcpyHostToDevice,
+                                  ctx->stream),
+             "cudaMemcpyAsync(visualize input)");
+      }
+      it.depth = static_cast<const float*>(dptr[0]);
+      it.normal = static_cast<const float*>(dptr[1]);
+      it.face_id = static_cast<const int32_t*>(dptr[2]);
+      it.vis_depth = static_cast<uint8_t*>(dptr[3]);
+      it.depth_u16 = static_cast<uint16_t*>(dptr[4]);
+      it.vis_normal = static_cast<uint8_t*>(dptr[5]);
+      it.vis_face_id = static_cast<uint8_t*>(dptr[6]);
+      launch_vis(it, ctx->stream);
+      CK(ctx, cudaGetLastError(), "visualize launch");
+      for (int j = 3; j < 7; ++j)
+        if (parts[j].out)
+          CK(ctx, cudaMemcpyAsync(parts[j].out, dptr[j], parts[j].bytes, cudaMemcpyDeviceToHost,
+                                  ctx->stream),
+             "cudaMemcpyAsync(visualize output)");
+      // the staging buffer is reused by the next item
+      CK(ctx, cudaStreamSynchronize(ctx->stream), "visualize");
+    } else {
+      launch_vis(it, ctx->stream);
+      CK(ctx, cudaGetLastError(), "visualize launch");
+    }
+    ++ctx->launches;
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "visualize");
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_render_gbuffer(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_gbuffer* views,
+                           uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  if (n < 0 || (n > 0 && !views))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view list");
+  cudaSetDevice(ctx->device);
+  int rc = check_option(ctx, ctx->opt);
+  if (rc) return rc;
+  for (int k = 0; k < n; ++k) {
+    const ugu_gpu_gbuffer& v = views[k];
+    if (v.mesh < 0 || v.mesh >= kMaxMeshes || !ctx->meshes[v.mesh].present)
+      return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh has not been initialized");
+    const MeshSlot& m = ctx->meshes[v.mesh];
+    if (ctx->opt.shading_normal == 0 && !m.has_fnormals)
+      return set_error(ctx, UGU_GPU_ERR_NO_FACE_NORMALS_FOR_SHADING,
+                       "specified face normal as shading normal but face normal is empty.");
+    if (ctx->opt.shading_normal == 1 && !m.has_normals)
+      return set_error(ctx, UGU_GPU_ERR_NO_VERTEX_NORMALS,
+                       "specified vertex normal as shading normal but vertex normal is empty.");
+    if (!v.face_id || v.camera.width < 0 || v.camera.height < 0)
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "view %d: no face_id or bad size", k);
+  }
+  if (!ctx->gbuf_bad) {
+    CK(ctx, cudaMalloc(&ctx->gbuf_bad, sizeof(unsigned long long)), "cudaMalloc(counter)");
+    CK(ctx, cudaMallocHost(&ctx->h_gbuf_bad, sizeof(unsigned long long)),
+       "cudaMallocHost(counter)");
+  }
+  CK(ctx, cudaMemsetAsync(ctx->gbuf_bad, 0, sizeof(unsigned long long), ctx->stream),
+     "cudaMemsetAsync(counter)");
+  const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
+  for (int k = 0; k < n; ++k) {
+    const ugu_gpu_gbuffer& v = views[k];
+    const size_t px = (size_t)v.camera.width * (size_t)v.camera.height;
+    if (px == 0) continue;
+    GbufParams p{};
+    fill_cam(p.cam, v.camera);
+    p.mesh = ctx->d_meshes + v.mesh;
+    p.shading_normal = ctx->opt.shading_normal;
+    p.bad_ids = ctx->gbuf_bad;
+    float* const outs[6] = {v.pos_wld, v.pos_cam, v.normal_wld, v.normal_cam, v.bary, v.uv};
+    float** dst[6] = {&p.pos_wld, &p.pos_cam, &p.normal_wld, &p.normal_cam, &p.bary, &p.uv};
+    if (dev) {
+      p.face_id = v.face_id;
+      for (int j = 0; j < 6; ++j) *dst[j] = outs[j];
+      p.stencil = v.stencil;
+      launch_gbuffer(p, ctx->stream);
+      CK(ctx, cudaGetLastError(), "G-buffer launch");
+    } else {
+      size_t total = align256(4 * px) + align256(px);
+      for (int j = 0; j < 6; ++j)
+        if (outs[j]) total += align256(12 * px);
+      if (total > ctx->vis_cap) {
+        CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        cudaFree(ctx->vis_buf);
+        ctx->vis_buf = nullptr;
+        ctx->vis_cap = 0;
+        CK(ctx, cudaMalloc(&ctx->vis_buf, total), "cudaMalloc(G-buffer staging)");
+        ctx->vis_cap = total;
+      }
+      uint8_t* q = ctx->vis_buf;
+      p.face_id = reinterpret_cast<const int32_t*>(q);
+      CK(ctx, cudaMemcpyAsync(q, v.face_id, 4 * px, cudaMemcpyHostToDevice, ctx->stream),
+         "cudaMemcpyAsync(face_id)");
+      q += align256(4 * px);
+      p.stencil = v.stencil ? q : nullptr;
+      q += align256(px);
+      for (int j = 0; j < 6; ++j) {
+        *dst[j] = nullptr;
+        if (!outs[j]) continue;
+        *dst[j] = reinterpret_cast<float*>(q);
+        q += align256(12 * px);
+      }
+      launch_gbuffer(p, ctx->stream);
+      CK(ctx, cudaGetLastError(), "G-buffer launch");
+      for (int j = 0; j < 6; ++j)
+        if (outs[j])
+          CK(ctx, cudaMemcpyAsync(outs[j], *dst[j], 12 * px, cudaMemcpyDeviceToHost, ctx->stream),
+             "cudaMemcpyAsync(G-buffer)");
+      if (v.stencil)
+        CK(ctx, cudaMemcpyAsync(v.stencil, p.stencil, px, cudaMemcpyDeviceToHost, ctx->stream),
+           "cudaMemcpyAsync(stencil)");
+      // the staging buffer is reused by the next view
+      CK(ctx, cudaStreamSynchronize(ctx->stream), "G-buffer");
+    }
+    ++ctx->launches;
+  }
+  CK(ctx, cudaMemcpyAsync(ctx->h_gbuf_bad, ctx->gbuf_bad, sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, ctx->stream),
+     "cudaMemcpyAsync(counter)");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "G-buffer");
+  if (*ctx->h_gbuf_bad)
+    return set_error(ctx, UGU_GPU_ERR_INDEX_OUT_OF_RANGE,
+                     "%llu face ids outside [-1, num_faces)", *ctx->h_gbuf_bad);
   return UGU_GPU_OK;
 }
 

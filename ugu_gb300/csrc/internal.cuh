@@ -18,6 +18,7 @@
 #include <cstdint>
 
 #include "exact.cuh"
+#include "ugu_gpu.h"
 
 namespace ugu_gpu {
 
@@ -170,6 +171,21 @@ struct BackwardParams {
   void* proj64;                 // per view (DevView::proj_offset), 32 bytes per vertex: screen
                                 // x, y projected in double as hi + lo floats, and 1/z
 };
+
+// Image helpers of ugu_gpu_visualize (vis.cu): one item, device pointers.
+void launch_vis(const ugu_gpu_vis& item, cudaStream_t s);
+
+// G-buffer pass (vis.cu): one view, device pointers.
+struct GbufParams {
+  Cam cam;
+  const DevMesh* mesh;  // device copy of the view's mesh slot
+  int32_t shading_normal;
+  const int32_t* face_id;
+  float *pos_wld, *pos_cam, *normal_wld, *normal_cam, *bary, *uv;
+  uint8_t* stencil;
+  unsigned long long* bad_ids;  // face ids outside [-1, num_faces)
+};
+void launch_gbuffer(const GbufParams& p, cudaStream_t s);
 
 // Raytracer (ray.cu): the views of one group, one thread per pixel.
 struct RayParams {

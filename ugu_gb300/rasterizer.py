@@ -180,6 +180,14 @@ class Context:
         d.textures = tex
         return d
 
+    def render_gbuffer(self, views, flags: int = 0) -> int:
+        arr = (capi.GBufferView * len(views))(*views)
+        return self.lib.ugu_gpu_render_gbuffer(self.h, len(views), C.addressof(arr), int(flags))
+
+    def visualize(self, items, flags: int = 0) -> int:
+        arr = (capi.Vis * len(items))(*items)
+        return self.lib.ugu_gpu_visualize(self.h, len(items), C.addressof(arr), int(flags))
+
     def stats(self) -> capi.Stats:
         s = capi.Stats()
         self.check(self.lib.ugu_gpu_get_stats(self.h, C.byref(s)))
@@ -316,6 +324,30 @@ class Rasterizer:
     def RenderDepthW(self):
         return self.RenderW(depth=True)
 
+    def RenderGBuffer(self):
+        """Extension: ugu::GBuffer's channels (include/ugu/renderer/base.h:
+        34-77) for the current camera -- face_id from a render, then the
+        G-buffer pass (include/ugu_gpu.h, ugu_gpu_render_gbuffer).  Returns
+        (ok, {name: image})."""
+        ok, out = self.Render(face_id=True)
+        if not ok:
+            return False, {}
+        H, W = self._camera.height, self._camera.width
+        g = {k: np.zeros((H, W, 3), np.float32) for k in capi.GBUFFER}
+        g["stencil"] = np.zeros((H, W), np.uint8)
+        v = capi.GBufferView()
+        v.mesh = 0
+        v.camera = capi.camera_struct(self._camera)
+        v.face_id = out["face_id"].ctypes.data
+        for k, a in g.items():
+            setattr(v, k, a.ctypes.data)
+        rc = self._ctx.render_gbuffer([v])
+        if rc != capi.OK:
+            LOGE(self._ctx.last_error())
+            return False, {}
+        g["face_id"] = out["face_id"]
+        return True, g
+
 
 class Raytracer(Rasterizer):
     """ugu::Raytracer's interface over the GPU (raytracer.h:14-53,
@@ -338,6 +370,55 @@ class Raytracer(Rasterizer):
         v.camera = capi.camera_struct(self._camera)
         v.images = im
         return self._ctx.render_views([v], capi.RAYTRACE)
+
+
+def _visualize(ctx: Context | None, depth=None, normal=None, face_id=None, min_d=200.0,
+               max_d=1500.0, gl_coord=False) -> dict:
+    """One ugu_gpu_visualize call on host arrays; returns the outputs."""
+    own = ctx is None
+    ctx = Context(0) if own else ctx
+    try:
+        src = next(a for a in (depth, normal, face_id) if a is not None)
+        H, W = src.shape[0], src.shape[1]
+        keep, out = [], {}
+        it = capi.Vis()
+        it.width, it.height = W, H
+        it.min_d, it.max_d, it.gl_coord = float(min_d), float(max_d), 1 if gl_coord else 0
+        for name, a, dt in (("depth", depth, np.float32), ("normal", normal, np.float32),
+                            ("face_id", face_id, np.int32)):
+            if a is not None:
+                a = np.ascontiguousarray(a, dt)
+                keep.append(a)
+                setattr(it, name, a.ctypes.data)
+        if depth is not None:
+            out["vis_depth"] = np.zeros((H, W), np.uint8)
+            out["depth_u16"] = np.zeros((H, W), np.uint16)
+        if normal is not None:
+            out["vis_normal"] = np.zeros((H, W, 3), np.uint8)
+        if face_id is not None:
+            out["vis_face_id"] = np.zeros((H, W, 3), np.uint8)
+        for k, v in out.items():
+            setattr(it, k, v.ctypes.data)
+        ctx.check(ctx.visualize([it]))
+        return out
+    finally:
+        if own:
+            ctx.close()
+
+
+def Depth2Gray(depth, min_d: float = 200.0, max_d: float = 1500.0, ctx=None) -> np.ndarray:
+    """src/util/image_util.cc:392-411 on the GPU."""
+    return _visualize(ctx, depth=depth, min_d=min_d, max_d=max_d)["vis_depth"]
+
+
+def Normal2Color(normal, gl_coord: bool = False, ctx=None) -> np.ndarray:
+    """src/util/image_util.cc:413-446 (RGB order) on the GPU."""
+    return _visualize(ctx, normal=normal, gl_coord=gl_coord)["vis_normal"]
+
+
+def FaceId2RandomColor(face_id, ctx=None) -> np.ndarray:
+    """src/util/image_util.cc:448-487 (RGB order) on the GPU."""
+    return _visualize(ctx, face_id=face_id)["vis_face_id"]
 
 
 def depth_to_u16(depth: np.ndarray) -> np.ndarray:
