@@ -193,6 +193,47 @@ typedef struct {
   uint8_t* stencil;        /* H*W */
 } ugu_gpu_gbuffer;
 
+/* ugu::VisibilityTester (include/ugu/texturing/visibility_tester.h:216-265,
+ * src/texturing/visibility_tester.cc): the per-keyframe vertex test
+ * TestVertex (:416-529) for every (keyframe, vertex), or facewise
+ * (:606-668) for every (keyframe, face corner) with the vertex moved 1e-3 of
+ * the way to its face's centre.  The ray casts go through the tester's own
+ * naive BVH (leaves of up to 5 faces, :285-294) over the mesh slot's
+ * vertices and faces.  Keyframe images are host or device buffers per the
+ * UGU_GPU_DEVICE_POINTERS flag, like the outputs. */
+typedef struct {
+  int32_t id;                 /* Keyframe::id */
+  ugu_gpu_camera camera;      /* pinhole; c2w_R / c2w_t give the rays */
+  float w2c_linear[9];        /* camera->w2c().cast<float>() linear part, row-major
+                                 (TestVertex transforms with it, :422) */
+  const uint8_t* color;       /* H*W*3 RGB8 */
+  const float* depth;         /* H*W, needed with use_depth */
+  const uint8_t* mask;        /* H*W, needed with use_mask */
+} ugu_gpu_keyframe;
+
+/* VisibilityTesterOption (visibility_tester.h:38-58). */
+typedef struct {
+  float backface_culling_angle_rad_th;
+  int32_t use_mask, use_depth;
+  int32_t interp;  /* 0 kNn, 1 kBilinear */
+  float max_viewing_angle;
+  float max_distance_from_camera_to_vertex;
+  float max_depth_difference;
+  float eps;
+} ugu_gpu_visibility_option;
+
+/* Per (keyframe, item) results, keyframe-major: item = vertex, or 3 *
+ * face + corner when facewise.  VertexInfoPerKeyframe's fields
+ * (visibility_tester.h:60-72); meaningful where visible is 1. */
+typedef struct {
+  uint8_t* visible;
+  float* projected_pos;  /* 2 floats */
+  float* viewing_angle;
+  float* distance;       /* along the ray; FLT_MAX when the ray hit nothing */
+  float* color;          /* 3 floats */
+  float* intensity;
+} ugu_gpu_visibility_out;
+
 /* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
 typedef struct {
   int32_t path;             /* UGU_GPU_PATH_TILED (default) or UGU_GPU_PATH_GLOBAL */
@@ -283,6 +324,16 @@ UGU_GPU_API int ugu_gpu_visualize(ugu_gpu_context* ctx, int32_t n, const ugu_gpu
  * error (UGU_GPU_ERR_INDEX_OUT_OF_RANGE), its pixel left at zeros. */
 UGU_GPU_API int ugu_gpu_render_gbuffer(ugu_gpu_context* ctx, int32_t n,
                                        const ugu_gpu_gbuffer* views, uint32_t flags);
+
+/* VisibilityTester::Test (visibility_tester.cc:670-731) for the mesh in
+ * `mesh` with per-vertex `normals` (V*3, the tester's own normals, host
+ * memory) against n keyframes; facewise selects TestFacewiseVertices.  The
+ * statistics (CalcStat) are left to the caller.  Synchronous. */
+UGU_GPU_API int ugu_gpu_test_visibility(ugu_gpu_context* ctx, int32_t mesh, const float* normals,
+                                        int32_t n, const ugu_gpu_keyframe* keyframes,
+                                        const ugu_gpu_visibility_option* option,
+                                        int32_t facewise, const ugu_gpu_visibility_out* out,
+                                        uint32_t flags);
 UGU_GPU_API int ugu_gpu_synchronize(ugu_gpu_context* ctx);
 /* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
 UGU_GPU_API int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream);

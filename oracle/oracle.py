@@ -117,6 +117,9 @@ def load():
         lib.oracle_visualize.restype = None
         lib.oracle_gbuffer.argtypes = [P] * 11
         lib.oracle_gbuffer.restype = C.c_int64
+        lib.oracle_test_visibility.argtypes = [P, C.c_int32, P, C.c_int32, P, C.c_int32, P, P,
+                                               C.c_int32, P, P, P, P, P, P]
+        lib.oracle_test_visibility.restype = None
         _lib = lib
     return _lib
 
@@ -309,6 +312,59 @@ def gbuffer(mesh, cam, opt, face_id):
                              fid.ctypes.data, *[out[k].ctypes.data for k in GBUFFER],
                              out["stencil"].ctypes.data)
     return int(bad), out
+
+
+class KeyframeS(C.Structure):
+    _fields_ = [("id", C.c_int32), ("cam", CameraS), ("L", C.c_float * 9),
+                ("color", C.c_void_p), ("depth", C.c_void_p), ("mask", C.c_void_p)]
+
+
+class VisOptionS(C.Structure):
+    _fields_ = [("backface_th", C.c_float), ("use_mask", C.c_int32), ("use_depth", C.c_int32),
+                ("interp", C.c_int32), ("max_viewing_angle", C.c_float),
+                ("max_distance", C.c_float), ("max_depth_difference", C.c_float),
+                ("eps", C.c_float)]
+
+
+def test_visibility(vertices, faces, normals, keyframes, option, facewise):
+    """VisibilityTester's per-keyframe test (oracle/ray_oracle.cc) for
+    keyframes = [(id, camera, w2c_linear 3x3, color HxWx3 u8, depth or None,
+    mask or None)] and option = VisibilityTesterOption fields; returns a dict
+    of keyframe-major arrays."""
+    lib = load()
+    V = np.ascontiguousarray(vertices, np.float32)
+    F = np.ascontiguousarray(faces, np.int32)
+    N = np.ascontiguousarray(normals, np.float32)
+    keep = []
+    kfs = (KeyframeS * len(keyframes))()
+    for i, (kid, cam, L, color, depth, mask) in enumerate(keyframes):
+        kfs[i].id = int(kid)
+        kfs[i].cam = camera_struct(cam)
+        kfs[i].L[:] = [float(x) for x in np.asarray(L, np.float32).reshape(-1)]
+        for name, a, dt in (("color", color, np.uint8), ("depth", depth, np.float32),
+                            ("mask", mask, np.uint8)):
+            if a is not None:
+                a = np.ascontiguousarray(a, dt)
+                keep.append(a)
+                setattr(kfs[i], name, a.ctypes.data)
+    o = VisOptionS(float(option.backface_culling_angle_rad_th), int(option.use_mask),
+                   int(option.use_depth), int(option.interp), float(option.max_viewing_angle),
+                   float(option.max_distance_from_camera_to_vertex),
+                   float(option.max_depth_difference), float(option.eps))
+    items = 3 * len(F) if facewise else len(V)
+    K = len(keyframes)
+    out = {"visible": np.zeros((K, items), np.uint8),
+           "projected_pos": np.zeros((K, items, 2), np.float32),
+           "viewing_angle": np.zeros((K, items), np.float32),
+           "distance": np.zeros((K, items), np.float32),
+           "color": np.zeros((K, items, 3), np.float32),
+           "intensity": np.zeros((K, items), np.float32)}
+    lib.oracle_test_visibility(V.ctypes.data, len(V), F.ctypes.data, len(F), N.ctypes.data, K,
+                               C.addressof(kfs), C.addressof(o), 1 if facewise else 0,
+                               *[out[k].ctypes.data for k in ("visible", "projected_pos",
+                                                              "viewing_angle", "distance",
+                                                              "color", "intensity")])
+    return out
 
 
 def ray_w(cam, x: int, y: int) -> np.ndarray:

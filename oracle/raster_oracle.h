@@ -125,6 +125,30 @@ int64_t oracle_gbuffer(const oracle_mesh* mesh, const oracle_camera* cam,
                        float* pos_cam, float* normal_wld, float* normal_cam, float* bary,
                        float* uv, uint8_t* stencil);
 
+/* ugu::Keyframe (visibility_tester.h:196-212) and VisibilityTesterOption
+ * (:38-58) as the visibility test reads them; L = w2c().cast<float>()'s
+ * linear part, row-major. */
+typedef struct {
+  int32_t id;
+  oracle_camera cam;
+  float L[9];
+  const uint8_t* color;
+  const float* depth;
+  const uint8_t* mask;
+} oracle_keyframe;
+
+typedef struct {
+  float backface_th;
+  int32_t use_mask, use_depth, interp;
+  float max_viewing_angle, max_distance, max_depth_difference, eps;
+} oracle_vis_option;
+
+void oracle_test_visibility(const float* V, int32_t nv, const int32_t* F, int32_t nf,
+                            const float* N, int32_t n_kf, const oracle_keyframe* kfs,
+                            const oracle_vis_option* o, int32_t facewise, uint8_t* visible,
+                            float* proj, float* angle, float* dist, float* color,
+                            float* intensity);
+
 /* ray_oracle.cc: ugu::BvhNaive over the mesh (NULL when it has no face) and
  * its nearest hit along a ray (1 and t, u, v, face, or 0). */
 void* oracle_bvh_build(const float* vertices, int32_t num_faces, const int32_t* faces);

@@ -21,8 +21,13 @@
  *   of v0 and v1.
  */
 #include <algorithm>
+#include <cfloat>
+#include <cmath>
 #include <cstdint>
+#include <limits>
 #include <vector>
+
+#include "raster_oracle.h"
 
 namespace {
 
@@ -96,13 +101,14 @@ const double kEps = (double)1e-8f;  // BvhNaive::m_epsilon
 struct Bvh {
   const float* V;
   const int32_t* F;
+  size_t leaf_faces = 4;  // BvhNaive::m_min_leaf_primitives
   std::vector<float> centre[3];
   std::vector<Node> nodes;
 
   int build(const std::vector<size_t>& ids, int depth) {
     const int idx = (int)nodes.size();
     nodes.emplace_back();
-    if (ids.size() <= 4 || depth >= 256) {
+    if (ids.size() <= leaf_faces || depth >= 256) {
       nodes[idx].leaf = true;
       nodes[idx].faces = ids;
       return idx;
@@ -162,13 +168,10 @@ struct Bvh {
   }
 };
 
-}  // namespace
-
-extern "C" {
-
-void* oracle_bvh_build(const float* vertices, int32_t num_faces, const int32_t* faces) {
+Bvh* build_bvh(const float* vertices, int32_t num_faces, const int32_t* faces, size_t leaf) {
   if (num_faces <= 0) return nullptr;
   Bvh* b = new Bvh();
+  b->leaf_faces = leaf;
   b->V = vertices;
   b->F = faces;
   for (int k = 0; k < 3; ++k) b->centre[k].resize((size_t)num_faces);
@@ -182,6 +185,141 @@ void* oracle_bvh_build(const float* vertices, int32_t num_faces, const int32_t* 
   for (size_t i = 0; i < ids.size(); ++i) ids[i] = i;
   b->build(ids, 0);
   return b;
+}
+
+// Nearest t along the ray (results[0].t of bvh_naive.h:99-111), or -1.
+float nearest_t(const Bvh* b, const float* org, const float* dir) {
+  std::vector<Hit> hits;
+  b->intersect(0, org, dir, hits);
+  std::sort(hits.begin(), hits.end(), [](const Hit& l, const Hit& r) { return l.t < r.t; });
+  return hits.empty() ? -1.0f : hits[0].t;
+}
+
+float dot3f(const float* a, const float* b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+
+// VisibilityTester::TestVertex (visibility_tester.cc:416-529) for one
+// keyframe and world point wp of vertex vid; false when not visible.
+bool test_vertex(const Bvh* bvh, const float* V, const float* N, int vid, const float* wp,
+                 const oracle_keyframe& K, const oracle_vis_option& o, float* proj, float* angle,
+                 float* dist_out, float* col, float* inten) {
+  const oracle_camera& c = K.cam;
+  float cp[3];
+  for (int k = 0; k < 3; ++k) cp[k] = dot3f(&K.L[3 * k], wp) + c.w2c_t[k];
+  const float x = c.fx / cp[2] * cp[0] + c.cx;  // PinholeCamera::Project
+  const float y = c.fy / cp[2] * cp[1] + c.cy;
+  const float d = cp[2];
+  proj[0] = x;
+  proj[1] = y;
+  if (d < 0 || x < 0 || c.width - 1 < x || y < 0 || c.height - 1 < y) return false;
+  const int nx = static_cast<int>(std::round(x)), ny = static_cast<int>(std::round(y));
+  const size_t nn = (size_t)ny * c.width + nx;
+  if (o.use_mask && K.mask[nn] != 255) return false;
+  if (o.use_depth && K.depth[nn] < std::numeric_limits<float>::epsilon()) return false;
+  // ray_w(float, float) (camera.h:438-448)
+  float r[3] = {(x - c.cx) / c.fx, (y - c.cy) / c.fy, 1.0f};
+  const float n2 = r[0] * r[0] + (r[1] * r[1] + r[2] * r[2]);
+  if (n2 > 0.0f) {
+    const float sq = std::sqrt(n2);
+    for (int k = 0; k < 3; ++k) r[k] = r[k] / sq;
+  }
+  float ray[3];
+  for (int k = 0; k < 3; ++k) ray[k] = dot3f(&c.c2w_R[3 * k], r);
+  const float* org = c.c2w_t;
+  const float dotv = -dot3f(&N[3 * vid], ray);
+  const float va = std::acos(dotv);
+  *angle = va;
+  if (o.backface_th < va) return false;
+  const float t = nearest_t(bvh, org, ray);
+  float distance = std::numeric_limits<float>::max();
+  float hit[3];
+  const float* v = &V[3 * vid];
+  if (t >= 0.0f) {
+    distance = t;
+    for (int k = 0; k < 3; ++k) hit[k] = org[k] + ray[k] * t;
+    const float e[3] = {hit[0] - v[0], hit[1] - v[1], hit[2] - v[2]};
+    const float dd = std::sqrt(dot3f(e, e));
+    if (dd > o.eps) return false;
+  } else {
+    for (int k = 0; k < 3; ++k) hit[k] = v[k];
+  }
+  if (o.use_depth) {
+    const float hz = dot3f(&K.L[6], hit) + c.w2c_t[2];
+    if (o.max_depth_difference < std::abs(hz - K.depth[nn])) return false;
+  }
+  *dist_out = distance;
+  if (distance > o.max_distance || va > o.max_viewing_angle) return false;
+  if (o.interp == 0) {
+    for (int k = 0; k < 3; ++k) col[k] = K.color[3 * nn + k];
+  } else {  // BilinearInterpolation (util/image_util.h:155-195)
+    int x0 = static_cast<int>(std::floor(x)), y0 = static_cast<int>(std::floor(y));
+    int x1 = x0 + 1, y1 = y0 + 1;
+    if (x0 < 0.0f) x0 = 0;
+    if (y0 < 0.0f) y0 = 0;
+    if (c.width <= x1) x1 = c.width - 1;
+    if (c.height <= y1) y1 = c.height - 1;
+    const float lu = x - x0, lv = y - y0;
+    const size_t W = (size_t)c.width;
+    for (int k = 0; k < 3; ++k) {
+      const float cf = (1.0f - lu) * (1.0f - lv) * K.color[3 * (y0 * W + x0) + k] +
+                       lu * (1.0f - lv) * K.color[3 * (y0 * W + x1) + k] +
+                       (1.0f - lu) * lv * K.color[3 * (y1 * W + x0) + k] +
+                       lu * lv * K.color[3 * (y1 * W + x1) + k];
+      col[k] = static_cast<uint8_t>(cf);
+    }
+  }
+  *inten = static_cast<float>(0.2989 * col[0] + 0.5870 * col[1] + 0.1140 * col[2]);
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* oracle_bvh_build(const float* vertices, int32_t num_faces, const int32_t* faces) {
+  return build_bvh(vertices, num_faces, faces, 4);
+}
+
+// VisibilityTester::Test's per-keyframe pass (:670-702): TestVertex for
+// every (keyframe, vertex), or facewise every (keyframe, face corner) with
+// the vertex moved 1e-3 toward the face centre (:606-668).  Outputs
+// keyframe-major; the fields are those of VertexInfoPerKeyframe.
+void oracle_test_visibility(const float* V, int32_t nv, const int32_t* F, int32_t nf,
+                            const float* N, int32_t n_kf, const oracle_keyframe* kfs,
+                            const oracle_vis_option* o, int32_t facewise, uint8_t* visible,
+                            float* proj, float* angle, float* dist, float* color,
+                            float* intensity) {
+  Bvh* bvh = build_bvh(V, nf, F, 5);  // visibility_tester.cc:285-294
+  if (!bvh) return;
+  const int64_t items = facewise ? 3 * (int64_t)nf : (int64_t)nv;
+  for (int32_t k = 0; k < n_kf; ++k)
+    for (int64_t it = 0; it < items; ++it) {
+      const int64_t out = k * items + it;
+      int vid;
+      float wp[3];
+      if (facewise) {
+        const int64_t f = it / 3;
+        const int j = (int)(it % 3);
+        vid = F[3 * f + j];
+        float ctr[3] = {0.0f, 0.0f, 0.0f};
+        for (int i = 0; i < 3; ++i)
+          for (int q = 0; q < 3; ++q) ctr[q] += V[3 * F[3 * f + i] + q];
+        for (int q = 0; q < 3; ++q) ctr[q] /= 3;
+        for (int q = 0; q < 3; ++q) wp[q] = V[3 * vid + q] + (ctr[q] - V[3 * vid + q]) * 1e-3f;
+      } else {
+        vid = (int)it;
+        for (int q = 0; q < 3; ++q) wp[q] = V[3 * vid + q];
+      }
+      float pj[2] = {0, 0}, a = 0, dd = 0, c3[3] = {0, 0, 0}, in = 0;
+      const bool vis = test_vertex(bvh, V, N, vid, wp, kfs[k], *o, pj, &a, &dd, c3, &in);
+      visible[out] = vis ? 1 : 0;
+      proj[2 * out] = pj[0];
+      proj[2 * out + 1] = pj[1];
+      angle[out] = a;
+      dist[out] = dd;
+      for (int q = 0; q < 3; ++q) color[3 * out + q] = c3[q];
+      intensity[out] = in;
+    }
+  delete bvh;
 }
 
 void oracle_bvh_free(void* bvh) { delete static_cast<Bvh*>(bvh); }

@@ -1,0 +1,128 @@
+"""ugu::VisibilityTester's per-keyframe test (TestVertex and the facewise
+variant, src/texturing/visibility_tester.cc:416-668) through
+ugu_gpu_test_visibility, against the oracle's restatement
+(oracle/ray_oracle.cc), which casts through the same pinned naive BVH.
+
+Keyframes are rendered ring views (colour, depth, mask) of the mesh, so
+use_depth / use_mask are exercised on consistent data.  The viewing angle
+is std::acos on the host and acosf on the device: they may differ by an
+ulp, so angles compare within 2 ulp and a visibility decision may differ
+only where the angle is that close to a threshold."""
+import math
+
+import numpy as np
+import pytest
+
+from ugu_gb300 import capi, scenes
+from ugu_gb300.rasterizer import RendererCpuOption
+
+KEYS = ("visible", "projected_pos", "viewing_angle", "distance", "color", "intensity")
+
+
+def keyframes(oracle_lib, m, n=4, size=(96, 72)):
+    opt = RendererCpuOption(diffuse_color=1, interp=1, shading_normal=1, backface_culling=True)
+    out = []
+    for i, cam in enumerate(scenes.ring_cameras(n, 3.0, [size] * n, height=0.4)):
+        rc, im, _ = oracle_lib.render(m, cam, opt, outputs=("color", "depth", "mask"))
+        assert rc == 0
+        out.append((i + 10, cam, im))
+    return out
+
+
+def option(**kw):
+    from ugu_gb300.visibility import VisibilityTesterOption
+    o = VisibilityTesterOption()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def oracle_run(oracle_lib, m, kfs, o, facewise):
+    return oracle_lib.test_visibility(
+        m.vertices, m.vertex_indices, m.normals,
+        [(kid, cam, capi.w2c_linear(cam), im["color"], im["depth"], im["mask"])
+         for kid, cam, im in kfs], o, facewise)
+
+
+@pytest.mark.parametrize("facewise", [False, True])
+def test_oracle_visibility_is_plausible(oracle_lib, facewise):
+    m = scenes.icosphere_textured(3, 64)
+    kfs = keyframes(oracle_lib, m)
+    r = oracle_run(oracle_lib, m, kfs, option(), facewise)
+    vis = r["visible"].astype(bool)
+    frac = vis.mean()
+    assert 0.25 < frac < 0.6, frac  # about the facing half of the sphere
+    assert (r["viewing_angle"][vis] <= math.radians(90.0) + 1e-6).all()
+    # distance along the ray = |vertex - camera centre| for a visible vertex
+    # whose ray hit something (a ray aimed exactly at a vertex may miss every
+    # face around it numerically; the reference keeps the vertex with
+    # distance FLT_MAX, visibility_tester.cc:479-485)
+    nohit = r["distance"] == np.finfo(np.float32).max
+    assert (nohit & vis).sum() <= 0.05 * vis.sum()
+    vis = vis & ~nohit
+    items = np.arange(vis.shape[1])
+    vid = m.vertex_indices.reshape(-1)[items] if facewise else items
+    for k, (_, cam, _) in enumerate(kfs):
+        c = np.asarray(cam.c2w, np.float64)[:3, 3]
+        d = np.linalg.norm(m.vertices[vid].astype(np.float64) - c, axis=1)
+        sel = vis[k]
+        assert np.abs(r["distance"][k][sel] - d[sel]).max() < 0.02
+
+
+def compare(ref, got, name):
+    va_r, va_g = ref["viewing_angle"], got["viewing_angle"]
+    ulp = np.abs(va_r.view(np.int32).astype(np.int64) - va_g.view(np.int32).astype(np.int64))
+    differ = ref["visible"] != got["visible"]
+    th = np.float32(math.radians(90.0))
+    near = np.abs(va_r - th) <= 4 * np.spacing(th)
+    assert not (differ & ~near).any(), f"{name}: visibility differs away from the thresholds"
+    both = (ref["visible"] == 1) & (got["visible"] == 1)
+    assert ulp[both].max(initial=0) <= 2, f"{name}: viewing angle {ulp[both].max()} ulp"
+    for k in ("projected_pos", "distance", "color", "intensity"):
+        a, b = ref[k][both], got[k][both]
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), f"{name}: {k}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("facewise", [False, True])
+@pytest.mark.parametrize("variant", ["default", "nn_no_mask_no_depth", "tight"])
+def test_gpu_visibility_matches_oracle(gpu_lib, oracle_lib, facewise, variant):
+    from ugu_gb300.visibility import Keyframe, VisibilityTester
+    m = scenes.icosphere_textured(4, 64)
+    kfs = keyframes(oracle_lib, m, n=5)
+    o = {"default": option(),
+         "nn_no_mask_no_depth": option(interp=0, use_mask=False, use_depth=False),
+         "tight": option(eps=0.02, max_viewing_angle=float(np.float32(math.radians(60.0))),
+                         max_depth_difference=0.01)}[variant]
+    ref = oracle_run(oracle_lib, m, kfs, o, facewise)
+    vt = VisibilityTester(o)
+    vt.set_data(m.vertices, m.normals, m.vertex_indices)
+    assert vt.PrepareData()
+    got = vt.raw([Keyframe(kid, cam, im["color"], im["depth"], im["mask"])
+                  for kid, cam, im in kfs], facewise)
+    compare(ref, got, f"{variant}/{'facewise' if facewise else 'vertex'}")
+
+
+@pytest.mark.gpu
+def test_gpu_visibility_info_assembly(gpu_lib, oracle_lib):
+    """VisibilityInfo from the device results: per-face keyframes only where
+    all three vertices are visible, statistics filled."""
+    from ugu_gb300.visibility import Keyframe, VisibilityInfo, VisibilityTester
+    m = scenes.icosphere_textured(3, 64)
+    kfs = keyframes(oracle_lib, m, n=4)
+    vt = VisibilityTester(option())
+    vt.set_data(m.vertices, m.normals, m.vertex_indices)
+    assert vt.PrepareData()
+    info = VisibilityInfo(m.num_vertices, m.num_faces)
+    assert vt.Test(info, facewise=False,
+                   keyframes=[Keyframe(kid, cam, im["color"], im["depth"], im["mask"])
+                              for kid, cam, im in kfs])
+    seen = [len(v.visible_keyframes) for v in info.vertex_info_list]
+    assert max(seen) >= 2 and min(seen) >= 0
+    for f, fi in enumerate(info.face_info_list):
+        for rec in fi.visible_keyframes:
+            for j in range(3):
+                assert info.vertex_info_list[m.vertex_indices[f, j]].VisibleFrom(rec.kf_id) >= 0
+            assert rec.area > 0
+    withk = [v for v in info.vertex_info_list if v.visible_keyframes]
+    assert all(v.min_viewing_angle_id >= 10 for v in withk)

@@ -97,6 +97,7 @@ EXPORTS = [
     "ugu_gpu_set_tuning", "ugu_gpu_get_tuning", "ugu_gpu_autotune", "ugu_gpu_get_stats",
     "ugu_gpu_synchronize", "ugu_gpu_set_stream", "ugu_gpu_render_noalloc",
     "ugu_gpu_get_device_mesh", "ugu_gpu_visualize", "ugu_gpu_render_gbuffer",
+    "ugu_gpu_test_visibility",
 ]
 
 NOALLOC_MAX_PIXELS = 2097152
@@ -151,6 +152,8 @@ def load(path: str | None = None):
     lib.ugu_gpu_get_device_mesh.argtypes = [P, C.c_int32, C.POINTER(DeviceMesh)]
     lib.ugu_gpu_visualize.argtypes = [P, C.c_int32, P, C.c_uint32]
     lib.ugu_gpu_render_gbuffer.argtypes = [P, C.c_int32, P, C.c_uint32]
+    lib.ugu_gpu_test_visibility.argtypes = [P, C.c_int32, P, C.c_int32, P, P, C.c_int32, P,
+                                            C.c_uint32]
     for name in EXPORTS:
         if name != "ugu_gpu_last_error":
             getattr(lib, name).restype = C.c_int
@@ -179,6 +182,35 @@ class GBufferView(C.Structure):
     """ugu_gpu_gbuffer: G-buffer channels of one rendered view."""
     _fields_ = [("mesh", C.c_int32), ("camera", CameraDesc), ("face_id", P)]
     _fields_ += [(k, P) for k in GBUFFER] + [("stencil", P)]
+
+
+class KeyframeDesc(C.Structure):
+    """ugu_gpu_keyframe."""
+    _fields_ = [("id", C.c_int32), ("camera", CameraDesc), ("w2c_linear", C.c_float * 9),
+                ("color", P), ("depth", P), ("mask", P)]
+
+
+class VisibilityOption(C.Structure):
+    """ugu_gpu_visibility_option (VisibilityTesterOption)."""
+    _fields_ = [("backface_culling_angle_rad_th", C.c_float), ("use_mask", C.c_int32),
+                ("use_depth", C.c_int32), ("interp", C.c_int32),
+                ("max_viewing_angle", C.c_float),
+                ("max_distance_from_camera_to_vertex", C.c_float),
+                ("max_depth_difference", C.c_float), ("eps", C.c_float)]
+
+
+class VisibilityOut(C.Structure):
+    """ugu_gpu_visibility_out."""
+    _fields_ = [("visible", P), ("projected_pos", P), ("viewing_angle", P), ("distance", P),
+                ("color", P), ("intensity", P)]
+
+
+def w2c_linear(cam) -> np.ndarray:
+    """camera->w2c().cast<float>()'s linear part: the general 3x3 inverse of
+    the c2w rotation block (Affine3d::inverse, camera.h:319), cast."""
+    from . import scenes
+    c2w = np.eye(4) if getattr(cam, "c2w", None) is None else np.asarray(cam.c2w, np.float64)
+    return scenes._inverse3(c2w[:3, :3]).astype(np.float32)
 
 
 def camera_struct(cam) -> CameraDesc:

@@ -7,7 +7,8 @@
 // std::sort orders them by t, and for the handful of hits a ray makes
 // std::sort keeps equal keys in that collection order.  So the tree is built
 // here the same way, with the same std::sort on the same keys:
-//   * a node with <= 4 faces (or at depth 256) is a leaf (bvh_naive.h:137-147);
+//   * a node with <= leaf_faces faces (or at depth 256) is a leaf
+//     (bvh_naive.h:137-147);
 //   * otherwise the faces are sorted by their centroid's coordinate on axis
 //     depth % 3, the centroid summed in float from zero and divided by 3
 //     (bvh_naive.h:164-205); the right child takes sorted[n/2, n) and the
@@ -17,7 +18,8 @@
 // The flattened tree lists the nodes in depth-first order and the leaves'
 // faces in traversal order; a leaf entry's index is therefore its rank in
 // the reference's hit order.  Leaf boxes (the reference tests none) are
-// added for pruning only.
+// added for pruning only.  Leaves hold up to 4 faces for ugu::Raytracer and
+// up to 5 for ugu::VisibilityTester (visibility_tester.cc:285-294).
 #include <algorithm>
 #include <cfloat>
 #include <cstddef>
@@ -30,12 +32,12 @@ namespace ugu_gpu {
 
 namespace {
 
-constexpr unsigned kLeafFaces = 4;  // BvhNaive::m_min_leaf_primitives
 constexpr int kMaxTreeDepth = 256;  // BvhNaive::m_max_tree_depth
 
 struct Builder {
   const float* V;
   const int32_t* F;
+  unsigned leaf_faces;  // BvhNaive::m_min_leaf_primitives
   std::vector<float> centre[3];
   HostBvh* out;
 
@@ -62,7 +64,7 @@ struct Builder {
     float lo[3], hi[3];
     bounds(ids, lo, hi);
     int a, b;
-    if ((unsigned)ids.size() <= kLeafFaces || depth >= kMaxTreeDepth) {
+    if ((unsigned)ids.size() <= leaf_faces || depth >= kMaxTreeDepth) {
       const int first = (int)(out->tris.size() / 3);
       for (size_t f : ids) {
         for (int j = 0; j < 3; ++j) {
@@ -107,7 +109,8 @@ struct Builder {
 
 }  // namespace
 
-bool build_bvh(const float* vertices, const int32_t* faces, int num_faces, HostBvh& out) {
+bool build_bvh(const float* vertices, const int32_t* faces, int num_faces, HostBvh& out,
+               int leaf_faces) {
   out.nodes.clear();
   out.tris.clear();
   out.depth = 0;
@@ -115,6 +118,7 @@ bool build_bvh(const float* vertices, const int32_t* faces, int num_faces, HostB
   Builder b;
   b.V = vertices;
   b.F = faces;
+  b.leaf_faces = (unsigned)leaf_faces;
   b.out = &out;
   for (int k = 0; k < 3; ++k) b.centre[k].resize((size_t)num_faces);
   for (int f = 0; f < num_faces; ++f)

@@ -42,6 +42,7 @@ struct MeshSlot {
   std::vector<float> h_vertices;
   std::vector<int32_t> h_faces;
   bool bvh = false;
+  bool vis_bvh = false;  // the visibility tester's tree (leaves of up to 5 faces)
 };
 
 // Device scratch of one render sequence.  A plan owns its own so that later
@@ -865,6 +866,26 @@ int ensure_bvh(ugu_gpu_context* ctx, int slot) {
   return UGU_GPU_OK;
 }
 
+// VisibilityTester::PrepareData's tree (visibility_tester.cc:319-339) for
+// one slot, on first use.
+int ensure_vis_bvh(ugu_gpu_context* ctx, int slot) {
+  MeshSlot& s = ctx->meshes[slot];
+  if (s.vis_bvh) return UGU_GPU_OK;
+  if (s.h_vertices.empty() || s.h_faces.empty())
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh is empty");
+  HostBvh hb;
+  if (!build_bvh(s.h_vertices.data(), s.h_faces.data(), (int)(s.h_faces.size() / 3), hb, 5))
+    return set_error(ctx, UGU_GPU_ERR_CAPACITY, "BVH deeper than %d levels", kMaxBvhDepth);
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  int rc;
+  if ((rc = upload(ctx, s, hb.nodes, &s.dev.vis_nodes))) return rc;
+  if ((rc = upload(ctx, s, hb.tris, &s.dev.vis_tris))) return rc;
+  CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &s.dev, sizeof(DevMesh), cudaMemcpyHostToDevice),
+     "cudaMemcpy(mesh table)");
+  s.vis_bvh = true;
+  return UGU_GPU_OK;
+}
+
 // The raytracer mode of the context for the lifetime of one call.
 struct RayMode {
   ugu_gpu_context* ctx;
@@ -1684,6 +1705,156 @@ int ugu_gpu_render_gbuffer(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_gbuffe
   if (*ctx->h_gbuf_bad)
     return set_error(ctx, UGU_GPU_ERR_INDEX_OUT_OF_RANGE,
                      "%llu face ids outside [-1, num_faces)", *ctx->h_gbuf_bad);
+  return UGU_GPU_OK;
+}
+
+int ugu_gpu_test_visibility(ugu_gpu_context* ctx, int32_t mesh, const float* normals, int32_t n,
+                            const ugu_gpu_keyframe* keyframes,
+                            const ugu_gpu_visibility_option* option, int32_t facewise,
+                            const ugu_gpu_visibility_out* out, uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  cudaSetDevice(ctx->device);
+  if (n <= 0 || !keyframes || !option || !out)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad keyframe list, option or output");
+  if (mesh < 0 || mesh >= kMaxMeshes || !ctx->meshes[mesh].present)
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh has not been initialized");
+  MeshSlot& ms = ctx->meshes[mesh];
+  const int V = ms.dev.num_vertices, F = ms.dev.num_faces;
+  if (V == 0 || F == 0 || !normals)  // PrepareData (:319-323)
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh is empty");
+  const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
+  for (int k = 0; k < n; ++k) {  // ValidateAndInitBeforeTest (:349-378)
+    const ugu_gpu_keyframe& kf = keyframes[k];
+    if (!kf.color || kf.camera.width <= 0 || kf.camera.height <= 0)
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "keyframe color is empty");
+    if (option->use_mask && !kf.mask)
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                       "use_mask is true but keyframe mask is empty");
+    if (option->use_depth && !kf.depth)
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                       "use_depth is true but keyframe depth is empty");
+  }
+  int rc = ensure_vis_bvh(ctx, mesh);
+  if (rc) return rc;
+  const int64_t items = facewise ? 3 * (int64_t)F : (int64_t)V;
+  // one device buffer: normals, keyframe table, staged images, staged outputs
+  size_t img_bytes = 0;
+  if (!dev)
+    for (int k = 0; k < n; ++k) {
+      const size_t px = (size_t)keyframes[k].camera.width * keyframes[k].camera.height;
+      img_bytes += align256(3 * px) + (keyframes[k].depth ? align256(4 * px) : 0) +
+                   (keyframes[k].mask ? align256(px) : 0);
+    }
+  const size_t ki = (size_t)n * (size_t)items;
+  const size_t out_bytes = dev ? 0 : align256(ki) + align256(8 * ki) + 3 * align256(4 * ki) +
+                                         align256(12 * ki);
+  const size_t total = align256(16 * (size_t)V) + align256(sizeof(DevKeyframe) * n) + img_bytes +
+                       out_bytes;
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (total > ctx->vis_cap) {
+    cudaFree(ctx->vis_buf);
+    ctx->vis_buf = nullptr;
+    ctx->vis_cap = 0;
+    CK(ctx, cudaMalloc(&ctx->vis_buf, total), "cudaMalloc(visibility buffers)");
+    ctx->vis_cap = total;
+  }
+  uint8_t* q = ctx->vis_buf;
+  auto take = [&](size_t bytes) {
+    uint8_t* r = q;
+    q += align256(bytes);
+    return r;
+  };
+  std::vector<float4> n4((size_t)V);
+  for (int i = 0; i < V; ++i)
+    n4[i] = make_float4(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2], 0.0f);
+  float4* d_normals = reinterpret_cast<float4*>(take(16 * (size_t)V));
+  CK(ctx, cudaMemcpyAsync(d_normals, n4.data(), 16 * (size_t)V, cudaMemcpyHostToDevice,
+                          ctx->stream),
+     "cudaMemcpyAsync(normals)");
+  DevKeyframe* d_kfs = reinterpret_cast<DevKeyframe*>(take(sizeof(DevKeyframe) * n));
+  std::vector<DevKeyframe> hk((size_t)n);
+  for (int k = 0; k < n; ++k) {
+    const ugu_gpu_keyframe& kf = keyframes[k];
+    DevKeyframe& d = hk[k];
+    std::memset(&d, 0, sizeof(d));
+    fill_cam(d.cam, kf.camera);
+    std::memcpy(d.L, kf.w2c_linear, sizeof(d.L));
+    d.id = kf.id;
+    const size_t px = (size_t)kf.camera.width * kf.camera.height;
+    if (dev) {
+      d.color = kf.color;
+      d.depth = kf.depth;
+      d.mask = kf.mask;
+      continue;
+    }
+    uint8_t* c = take(3 * px);
+    CK(ctx, cudaMemcpyAsync(c, kf.color, 3 * px, cudaMemcpyHostToDevice, ctx->stream),
+       "cudaMemcpyAsync(keyframe color)");
+    d.color = c;
+    if (kf.depth) {
+      uint8_t* dd = take(4 * px);
+      CK(ctx, cudaMemcpyAsync(dd, kf.depth, 4 * px, cudaMemcpyHostToDevice, ctx->stream),
+         "cudaMemcpyAsync(keyframe depth)");
+      d.depth = reinterpret_cast<const float*>(dd);
+    }
+    if (kf.mask) {
+      uint8_t* mm = take(px);
+      CK(ctx, cudaMemcpyAsync(mm, kf.mask, px, cudaMemcpyHostToDevice, ctx->stream),
+         "cudaMemcpyAsync(keyframe mask)");
+      d.mask = mm;
+    }
+  }
+  CK(ctx, cudaMemcpyAsync(d_kfs, hk.data(), sizeof(DevKeyframe) * n, cudaMemcpyHostToDevice,
+                          ctx->stream),
+     "cudaMemcpyAsync(keyframes)");
+  VisParams p{};
+  p.mesh = ctx->d_meshes + mesh;
+  p.normals = d_normals;
+  p.kfs = d_kfs;
+  p.num_kf = n;
+  p.facewise = facewise ? 1 : 0;
+  p.items = (int32_t)items;
+  p.backface_th = option->backface_culling_angle_rad_th;
+  p.max_viewing_angle = option->max_viewing_angle;
+  p.max_distance = option->max_distance_from_camera_to_vertex;
+  p.max_depth_difference = option->max_depth_difference;
+  p.eps = option->eps;
+  p.use_mask = option->use_mask ? 1 : 0;
+  p.use_depth = option->use_depth ? 1 : 0;
+  p.interp = option->interp;
+  if (dev) {
+    p.visible = out->visible;
+    p.projected = out->projected_pos;
+    p.viewing_angle = out->viewing_angle;
+    p.distance = out->distance;
+    p.color = out->color;
+    p.intensity = out->intensity;
+  } else {
+    p.visible = out->visible ? take(ki) : nullptr;
+    p.projected = out->projected_pos ? reinterpret_cast<float*>(take(8 * ki)) : nullptr;
+    p.viewing_angle = out->viewing_angle ? reinterpret_cast<float*>(take(4 * ki)) : nullptr;
+    p.distance = out->distance ? reinterpret_cast<float*>(take(4 * ki)) : nullptr;
+    p.color = out->color ? reinterpret_cast<float*>(take(12 * ki)) : nullptr;
+    p.intensity = out->intensity ? reinterpret_cast<float*>(take(4 * ki)) : nullptr;
+  }
+  launch_visibility(p, ctx->stream);
+  CK(ctx, cudaGetLastError(), "visibility launch");
+  ++ctx->launches;
+  if (!dev) {
+    auto back = [&](void* dst, const void* src, size_t bytes) -> int {
+      if (!dst) return UGU_GPU_OK;
+      CK(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream),
+         "cudaMemcpyAsync(visibility)");
+      return UGU_GPU_OK;
+    };
+    if ((rc = back(out->visible, p.visible, ki))) return rc;
+    if ((rc = back(out->projected_pos, p.projected, 8 * ki))) return rc;
+    if ((rc = back(out->viewing_angle, p.viewing_angle, 4 * ki))) return rc;
+    if ((rc = back(out->distance, p.distance, 4 * ki))) return rc;
+    if ((rc = back(out->color, p.color, 12 * ki))) return rc;
+    if ((rc = back(out->intensity, p.intensity, 4 * ki))) return rc;
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "visibility");
   return UGU_GPU_OK;
 }
 

@@ -75,10 +75,10 @@ UGU_HD float3 project(const Cam& c, float vx, float vy, float vz) {
   return o;
 }
 
-// PinholeCamera::ray_c + ray_w (camera.h:438-448).
-UGU_HD float3 ray_w(const Cam& c, int x, int y) {
-  float d0 = fdiv(fsub((float)x, c.cx), c.fx);
-  float d1 = fdiv(fsub((float)y, c.cy), c.fy);
+// PinholeCamera::ray_c + ray_w (camera.h:438-448) at an image point.
+UGU_HD float3 ray_w_at(const Cam& c, float x, float y) {
+  float d0 = fdiv(fsub(x, c.cx), c.fx);
+  float d1 = fdiv(fsub(y, c.cy), c.fy);
   float d2 = 1.0f;
   float n2 = sum3(fmul(d0, d0), fmul(d1, d1), fmul(d2, d2));
   if (n2 > 0.0f) {
@@ -93,6 +93,9 @@ UGU_HD float3 ray_w(const Cam& c, int x, int y) {
   r.z = dot3(c.C[6], c.C[7], c.C[8], d0, d1, d2);
   return r;
 }
+
+// The tabulated ray of pixel (x, y) (camera.h:482-513): the same value.
+UGU_HD float3 ray_w(const Cam& c, int x, int y) { return ray_w_at(c, (float)x, (float)y); }
 
 // Screen-space setup of one face for one view (rasterizer.cc:163-193).
 struct FaceSetup {

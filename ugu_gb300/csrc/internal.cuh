@@ -58,6 +58,9 @@ struct DevMesh {
   const float4* bvh_tris;
   int32_t bvh_depth;    // deepest node (root = 0)
   int32_t bvh_entries;
+  // the visibility tester's tree (leaves of up to 5 faces), built on first use
+  const float4* vis_nodes;
+  const float4* vis_tris;
 };
 
 struct DevView {
@@ -187,6 +190,34 @@ struct GbufParams {
 };
 void launch_gbuffer(const GbufParams& p, cudaStream_t s);
 
+// Visibility test (ray.cu): one thread per (keyframe, vertex) or, facewise,
+// per (keyframe, face corner).
+struct DevKeyframe {
+  Cam cam;           // R, t: w2c rotation / translation; C, T: c2w
+  float L[9];        // w2c().linear().cast<float>(), row-major
+  int32_t id;
+  const uint8_t* color;  // H*W*3
+  const float* depth;    // H*W or NULL
+  const uint8_t* mask;   // H*W or NULL
+};
+struct VisParams {
+  const DevMesh* mesh;      // vertices, faces and the visibility tree
+  const float4* normals;    // per vertex (the tester's normals)
+  const DevKeyframe* kfs;
+  int32_t num_kf;
+  int32_t facewise;         // items = faces * 3 corners, else vertices
+  int32_t items;
+  float backface_th, max_viewing_angle, max_distance, max_depth_difference, eps;
+  int32_t use_mask, use_depth, interp;
+  uint8_t* visible;         // [kf][item]
+  float* projected;         // [kf][item][2]
+  float* viewing_angle;     // [kf][item]
+  float* distance;          // [kf][item]
+  float* color;             // [kf][item][3]
+  float* intensity;         // [kf][item]
+};
+void launch_visibility(const VisParams& p, cudaStream_t s);
+
 // Raytracer (ray.cu): the views of one group, one thread per pixel.
 struct RayParams {
   const DevMesh* meshes;
@@ -207,7 +238,8 @@ struct HostBvh {
 };
 // Builds ugu::BvhNaive's tree for the mesh; false when it is deeper than
 // kMaxBvhDepth or the mesh has no face.
-bool build_bvh(const float* vertices, const int32_t* faces, int num_faces, HostBvh& out);
+bool build_bvh(const float* vertices, const int32_t* faces, int num_faces, HostBvh& out,
+               int leaf_faces = 4);
 // One block per kRayTileW x kRayTileH pixels; max_tiles = the most tiles of
 // any view of the group.
 constexpr int kRayTileW = 16, kRayTileH = 8;

@@ -321,7 +321,7 @@ constexpr int kCand = 8;
 
 // The double test on the pending candidates, nearest lower bound first,
 // while one can still win or tie; updates the hit and the bound.
-__device__ __forceinline__ void resolve(const DevMesh& m, float3 o, float3 d, int* ce, float* cl,
+__device__ __forceinline__ void resolve(const float4* tris, float3 o, float3 d, int* ce, float* cl,
                                         int& n, RayHit& h, float& bound) {
   while (n > 0) {
     int j = 0;
@@ -332,10 +332,10 @@ __device__ __forceinline__ void resolve(const DevMesh& m, float3 o, float3 d, in
     ce[j] = ce[n - 1];
     cl[j] = cl[n - 1];
     --n;
-    const float4 q0 = __ldg(&m.bvh_tris[3 * e]);
+    const float4 q0 = __ldg(&tris[3 * e]);
     float t, u, v;
-    if (!moller_trumbore_f64(o, d, ld3(q0), ld3(__ldg(&m.bvh_tris[3 * e + 1])),
-                             ld3(__ldg(&m.bvh_tris[3 * e + 2])), t, u, v))
+    if (!moller_trumbore_f64(o, d, ld3(q0), ld3(__ldg(&tris[3 * e + 1])),
+                             ld3(__ldg(&tris[3 * e + 2])), t, u, v))
       continue;
     if (t < h.t || (t == h.t && e < h.rank)) {
       h.t = t;
@@ -355,7 +355,7 @@ __device__ __forceinline__ void resolve(const DevMesh& m, float3 o, float3 d, in
 // nearest t (and prunes boxes), and the triangles that could still win or
 // tie wait in a short list for the double test, run once per ray after the
 // traversal (a full list is resolved on the spot).
-__device__ RayHit trace(const DevMesh& m, float3 o, float3 d) {
+__device__ RayHit trace(const float4* nodes, const float4* tris, float3 o, float3 d) {
   RayHit h;
   h.t = INFINITY;
   h.u = h.v = 0.0f;
@@ -373,7 +373,7 @@ __device__ RayHit trace(const DevMesh& m, float3 o, float3 d) {
   int sp = 0;
   {
     float t0;
-    const int f = box_hit(__ldg(&m.bvh_nodes[0]), __ldg(&m.bvh_nodes[1]), o, d, inv, bound, t0);
+    const int f = box_hit(__ldg(&nodes[0]), __ldg(&nodes[1]), o, d, inv, bound, t0);
     if (f >= 0) {
       stack[0] = f;
       stack_t[0] = t0;
@@ -384,8 +384,8 @@ __device__ RayHit trace(const DevMesh& m, float3 o, float3 d) {
     --sp;
     if (beyond(stack_t[sp], bound)) continue;
     const int n = stack[sp] >> 3, face = stack[sp] & 7;
-    const float4 lo = __ldg(&m.bvh_nodes[2 * n]);
-    const float4 hi = __ldg(&m.bvh_nodes[2 * n + 1]);
+    const float4 lo = __ldg(&nodes[2 * n]);
+    const float4 hi = __ldg(&nodes[2 * n + 1]);
     const int a = __float_as_int(lo.w), b = __float_as_int(hi.w);
     if (a >= 0) {
       // the reference descends only when its own box test hits; the slab
@@ -395,10 +395,8 @@ __device__ RayHit trace(const DevMesh& m, float3 o, float3 d) {
       // children slab-tested here and pushed far first; the reference's
       // left-first order only matters through the ranks
       float ta, tb;
-      const int fa = box_hit(__ldg(&m.bvh_nodes[2 * a]), __ldg(&m.bvh_nodes[2 * a + 1]), o, d,
-                             inv, bound, ta);
-      const int fb = box_hit(__ldg(&m.bvh_nodes[2 * b]), __ldg(&m.bvh_nodes[2 * b + 1]), o, d,
-                             inv, bound, tb);
+      const int fa = box_hit(__ldg(&nodes[2 * a]), __ldg(&nodes[2 * a + 1]), o, d, inv, bound, ta);
+      const int fb = box_hit(__ldg(&nodes[2 * b]), __ldg(&nodes[2 * b + 1]), o, d, inv, bound, tb);
       if (sp + 2 > kStack) break;  // deeper than built trees go
       const bool a_first = fa >= 0 && (fb < 0 || ta <= tb);
       if (a_first) {
@@ -412,9 +410,9 @@ __device__ RayHit trace(const DevMesh& m, float3 o, float3 d) {
     }
     const int first = -1 - a;
     for (int e = first; e < first + b; ++e) {
-      const float3 v0 = ld3(__ldg(&m.bvh_tris[3 * e]));
-      const float3 v1 = ld3(__ldg(&m.bvh_tris[3 * e + 1]));
-      const float3 v2 = ld3(__ldg(&m.bvh_tris[3 * e + 2]));
+      const float3 v0 = ld3(__ldg(&tris[3 * e]));
+      const float3 v1 = ld3(__ldg(&tris[3 * e + 1]));
+      const float3 v2 = ld3(__ldg(&tris[3 * e + 2]));
       const MtFloat q = mt_float(o, d, v0, v1, v2);
       const int r = mt_decide(q);
       if (r < 0) continue;
@@ -422,13 +420,13 @@ __device__ RayHit trace(const DevMesh& m, float3 o, float3 d) {
       t_bounds(q, tl, th);
       if (beyond(tl, bound)) continue;
       if (r > 0) bound = fminf(bound, th);
-      if (nc == kCand) resolve(m, o, d, ce, cl, nc, h, bound);
+      if (nc == kCand) resolve(tris, o, d, ce, cl, nc, h, bound);
       ce[nc] = e;
       cl[nc] = tl;
       ++nc;
     }
   }
-  resolve(m, o, d, ce, cl, nc, h, bound);
+  resolve(tris, o, d, ce, cl, nc, h, bound);
   return h;
 }
 
@@ -456,7 +454,7 @@ __global__ void __launch_bounds__(kRayThreads) k_ray(RayParams p) {
 
   const float3 o = make_float3(c.T[0], c.T[1], c.T[2]);  // org_ray_w
   const float3 d = ray_w(c, x, y);
-  const RayHit h = trace(sm, o, d);
+  const RayHit h = trace(sm.bvh_nodes, sm.bvh_tris, o, d);
   bool hit = h.fid >= 0;
   if (hit && p.backface_culling) {
     const float4 fn = __ldg(&sm.fnormals[h.fid]);
@@ -517,7 +515,134 @@ __global__ void __launch_bounds__(kRayThreads) k_ray(RayParams p) {
   }
 }
 
+
+// VisibilityTester::TestVertex (src/texturing/visibility_tester.cc:416-529)
+// for one (keyframe, vertex) -- or, facewise (:606-668), one (keyframe,
+// face corner) with the vertex moved 1e-3 of the way to the face centre.
+// Float arithmetic in the reference's order; std::acos is acosf here (the
+// host library's may differ by an ulp).
+__global__ void __launch_bounds__(kRayThreads) k_visibility(VisParams p) {
+  const int64_t item = (int64_t)blockIdx.x * kRayThreads + threadIdx.x;
+  if (item >= p.items) return;
+  const DevKeyframe& K = p.kfs[blockIdx.y];
+  const Cam& c = K.cam;
+  const DevMesh& m = *p.mesh;
+  int vid;
+  float3 wp;
+  if (p.facewise) {
+    const int f = (int)(item / 3), j = (int)(item - 3 * (int64_t)f);
+    const int4 vi = __ldg(&m.vidx[f]);
+    vid = j == 0 ? vi.x : (j == 1 ? vi.y : vi.z);
+    const float4 a = __ldg(&m.vertices[vi.x]), b = __ldg(&m.vertices[vi.y]),
+                 cc = __ldg(&m.vertices[vi.z]);
+    // face_centers_: Zero, += each vertex, /= 3 (:327-333)
+    const float3 ctr = make_float3(fdiv(fadd(fadd(fadd(0.0f, a.x), b.x), cc.x), 3.0f),
+                                   fdiv(fadd(fadd(fadd(0.0f, a.y), b.y), cc.y), 3.0f),
+                                   fdiv(fadd(fadd(fadd(0.0f, a.z), b.z), cc.z), 3.0f));
+    const float4 v = __ldg(&m.vertices[vid]);
+    // v_offset = (center - v) * 1e-3f; world_p = v + v_offset
+    wp = make_float3(fadd(v.x, fmul(fsub(ctr.x, v.x), 1e-3f)),
+                     fadd(v.y, fmul(fsub(ctr.y, v.y), 1e-3f)),
+                     fadd(v.z, fmul(fsub(ctr.z, v.z), 1e-3f)));
+  } else {
+    vid = (int)item;
+    const float4 v = __ldg(&m.vertices[vid]);
+    wp = make_float3(v.x, v.y, v.z);
+  }
+  const float4 v4 = __ldg(&m.vertices[vid]);
+  const int64_t out = (int64_t)blockIdx.y * p.items + item;
+  uint8_t visible = 0;
+  float px = 0.0f, py = 0.0f, angle = 0.0f, distance = 0.0f, intensity = 0.0f;
+  float col[3] = {0.0f, 0.0f, 0.0f};
+  do {
+    // camera_p = w2c().cast<float>() * world_p; Project (camera.h:380-387)
+    const float cx_ = fadd(dot3(K.L[0], K.L[1], K.L[2], wp.x, wp.y, wp.z), c.t[0]);
+    const float cy_ = fadd(dot3(K.L[3], K.L[4], K.L[5], wp.x, wp.y, wp.z), c.t[1]);
+    const float cz_ = fadd(dot3(K.L[6], K.L[7], K.L[8], wp.x, wp.y, wp.z), c.t[2]);
+    px = fadd(fmul(fdiv(c.fx, cz_), cx_), c.cx);
+    py = fadd(fmul(fdiv(c.fy, cz_), cy_), c.cy);
+    if (cz_ < 0.0f || px < 0.0f || (float)(c.width - 1) < px || py < 0.0f ||
+        (float)(c.height - 1) < py)
+      break;
+    const int nx = (int)roundf(px), ny = (int)roundf(py);
+    const int64_t nn = (int64_t)ny * c.width + nx;
+    if (p.use_mask && K.mask[nn] != 255) break;
+    if (p.use_depth && K.depth[nn] < FLT_EPSILON) break;
+    const float3 ray = ray_w_at(c, px, py);
+    const float3 org = make_float3(c.T[0], c.T[1], c.T[2]);
+    const float4 n4 = __ldg(&p.normals[vid]);
+    const float dt = -dot3(n4.x, n4.y, n4.z, ray.x, ray.y, ray.z);
+    angle = acosf(dt);
+    if (p.backface_th < angle) break;
+    const RayHit h = trace(m.vis_nodes, m.vis_tris, org, ray);
+    distance = FLT_MAX;
+    float3 hit;
+    if (h.fid >= 0) {
+      distance = h.t;
+      hit = make_float3(fadd(org.x, fmul(ray.x, h.t)), fadd(org.y, fmul(ray.y, h.t)),
+                        fadd(org.z, fmul(ray.z, h.t)));
+      const float ex = fsub(hit.x, v4.x), ey = fsub(hit.y, v4.y), ez = fsub(hit.z, v4.z);
+      const float dist = __fsqrt_rn(dot3(ex, ey, ez, ex, ey, ez));
+      if (dist > p.eps) break;
+    } else {
+      hit = make_float3(v4.x, v4.y, v4.z);
+    }
+    if (p.use_depth) {
+      const float hz = fadd(dot3(K.L[6], K.L[7], K.L[8], hit.x, hit.y, hit.z), c.t[2]);
+      if (p.max_depth_difference < fabsf(fsub(hz, K.depth[nn]))) break;
+    }
+    if (distance > p.max_distance || angle > p.max_viewing_angle) break;
+    if (p.interp == 0) {
+      col[0] = K.color[3 * nn];
+      col[1] = K.color[3 * nn + 1];
+      col[2] = K.color[3 * nn + 2];
+    } else {  // BilinearInterpolation (util/image_util.h:155-195)
+      int x0 = (int)floorf(px), y0 = (int)floorf(py);
+      int x1 = x0 + 1, y1 = y0 + 1;
+      if (x0 < 0) x0 = 0;
+      if (y0 < 0) y0 = 0;
+      if (c.width <= x1) x1 = c.width - 1;
+      if (c.height <= y1) y1 = c.height - 1;
+      const float lu = fsub(px, (float)x0), lv = fsub(py, (float)y0);
+      const uint8_t* im = K.color;
+      const int64_t W = c.width;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float a00 = fmul(fmul(fsub(1.0f, lu), fsub(1.0f, lv)), (float)im[3 * (y0 * W + x0) + k]);
+        const float a10 = fmul(fmul(lu, fsub(1.0f, lv)), (float)im[3 * (y0 * W + x1) + k]);
+        const float a01 = fmul(fmul(fsub(1.0f, lu), lv), (float)im[3 * (y1 * W + x0) + k]);
+        const float a11 = fmul(fmul(lu, lv), (float)im[3 * (y1 * W + x1) + k]);
+        col[k] = (float)f2u8(fadd(fadd(fadd(a00, a10), a01), a11));
+      }
+    }
+    // Color2Gray: (float)(0.2989 r + 0.5870 g + 0.1140 b) in double
+    intensity = __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(0.2989, (double)col[0]),
+                                                      __dmul_rn(0.5870, (double)col[1])),
+                                            __dmul_rn(0.1140, (double)col[2])));
+    visible = 1;
+  } while (false);
+  if (p.visible) p.visible[out] = visible;
+  if (p.projected) {
+    p.projected[2 * out] = px;
+    p.projected[2 * out + 1] = py;
+  }
+  if (p.viewing_angle) p.viewing_angle[out] = angle;
+  if (p.distance) p.distance[out] = distance;
+  if (p.color) {
+    p.color[3 * out] = col[0];
+    p.color[3 * out + 1] = col[1];
+    p.color[3 * out + 2] = col[2];
+  }
+  if (p.intensity) p.intensity[out] = intensity;
+}
+
 }  // namespace
+
+void launch_visibility(const VisParams& p, cudaStream_t s) {
+  if (p.items <= 0 || p.num_kf <= 0) return;
+  k_visibility<<<dim3((unsigned)((p.items + kRayThreads - 1) / kRayThreads), (unsigned)p.num_kf),
+                 kRayThreads, 0, s>>>(p);
+}
 
 void launch_ray(const RayParams& p, int64_t max_tiles, cudaStream_t s) {
   k_ray<<<dim3((unsigned)max_tiles, (unsigned)p.num_views), kRayThreads, 0, s>>>(p);

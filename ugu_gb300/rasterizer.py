@@ -180,6 +180,14 @@ class Context:
         d.textures = tex
         return d
 
+    def test_visibility(self, slot: int, normals, keyframes, option, facewise: bool, out,
+                        flags: int = 0) -> int:
+        arr = (capi.KeyframeDesc * len(keyframes))(*keyframes)
+        n = np.ascontiguousarray(normals, np.float32)
+        return self.lib.ugu_gpu_test_visibility(self.h, int(slot), n.ctypes.data, len(keyframes),
+                                                C.addressof(arr), C.byref(option),
+                                                1 if facewise else 0, C.byref(out), int(flags))
+
     def render_gbuffer(self, views, flags: int = 0) -> int:
         arr = (capi.GBufferView * len(views))(*views)
         return self.lib.ugu_gpu_render_gbuffer(self.h, len(views), C.addressof(arr), int(flags))
