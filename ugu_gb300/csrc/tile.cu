@@ -13,9 +13,11 @@
 //   k_gather copies every run into its tile's range: faces drawn first from
 //            the front, faces drawn last from the back.
 //   k_tile   persistent blocks pull (view, tile) items from a work queue.
-//            For one tile: set the listed faces up in shared memory, split
-//            each warp's 32 faces into (face, pixel) pairs with a warp prefix
-//            scan of their bbox-in-tile pixel counts, test every pair's
+//            For one tile: set the listed faces up in shared memory with
+//            their candidate pixels (the box-in-tile, or conservative row
+//            spans for small faces, span.cuh), split each warp's 32 faces
+//            into (face, pixel) pairs with a warp prefix scan of their
+//            candidate counts, test every pair's
 //            coverage (Loop B's pixel test), queue the covered ones and run
 //            their z-test 32 at a time into a shared-memory z-buffer of
 //            64-bit (depth bits << 32 | face id << 1 | back-face bit) keys
@@ -30,6 +32,7 @@
 
 #include "internal.cuh"
 #include "shade.cuh"
+#include "span.cuh"
 
 namespace ugu_gpu {
 
@@ -460,6 +463,7 @@ struct Region {
   float4 r2[kChunk];  // v0.z v1.z v2.z fid-bits
   float4 r3[kChunk];  // back-face sign surrogate: sa sb sc tolerance
   float4 r5[kChunk];  // depth pre-test: z1 z2, z0 z2, z0 z1, |area| z0 z1 z2 (1 - 2^-16)
+  uint4 r4[kChunk];   // row spans (FaceSpans: cum_lo cum_hi start_lo start_hi), or 0
   int cnt[kChunk];    // bbox-in-tile pixels, 0 when the face is skipped
 };
 
@@ -536,7 +540,7 @@ __device__ __forceinline__ void depth_test(TileSmem& sm, const Region& R, const 
 // pair per lane: back-face sign, edge functions, coverage.  Covered pairs go
 // to the warp's queue; every 32 of them take the depth test together, one
 // per lane.
-__device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const TileParams& p,
+__device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileParams& p,
                                             const Cam& c, int m, int tx0, int ty0, int tlog) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
@@ -545,7 +549,21 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const
   int qn = 0;
   for (int base = warp * 32; base < m; base += kTileThreads) {
     const int j = base + lane;
-    const int cnt = j < m ? R.cnt[j] : 0;
+    int cnt = j < m ? R.cnt[j] : 0;
+    // the candidate pixels of the lane's face: its row spans when the face is
+    // small enough (span.cuh), else the whole box-in-tile
+    if (cnt > 0) {
+      const float4 a = R.r0[j], b = R.r1[j];
+      const unsigned box = __float_as_uint(b.w);
+      const int bw = (int)((box >> 10) & 31u) + 1, bh = cnt / bw;
+      const int bx0 = tx0 + (int)(box & 31u), by0 = ty0 + (int)((box >> 5) & 31u);
+      FaceSpans sp;
+      if (face_spans(a.x, a.y, a.z, a.w, b.x, b.y, b.z, bx0, bx0 + bw - 1, by0, by0 + bh - 1,
+                     tx0, sp)) {
+        cnt = sp.count;
+        R.r4[j] = make_uint4(sp.cum_lo, sp.cum_hi, sp.start_lo, sp.start_hi);
+      }
+    }
     int incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -569,11 +587,21 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, const Region& R, const
         const float4 r0 = R.r0[jj];
         const float4 r1 = R.r1[jj];
         const float4 r3 = R.r3[jj];
+        const uint4 r4 = R.r4[jj];
         const unsigned box = __float_as_uint(r1.w);
-        const int bw = (int)((box >> 10) & 31u) + 1;
-        const int yy = (local * (int)(box >> 15)) >> 16;
-        const int x = tx0 + (int)(box & 31u) + local - yy * bw;
-        const int y = ty0 + (int)((box >> 5) & 31u) + yy;
+        int x, y;
+        if (r4.w & kSpanFlag) {  // candidate `local` of the face's row spans
+          const FaceSpans sp = {r4.x, r4.y, r4.z, r4.w, 0};
+          int dx, row;
+          span_pixel(sp, local, dx, row);
+          x = tx0 + dx;
+          y = ty0 + (int)((box >> 5) & 31u) + row;
+        } else {  // pixel `local` of the box, row-major
+          const int bw = (int)((box >> 10) & 31u) + 1;
+          const int yy = (local * (int)(box >> 15)) >> 16;
+          x = tx0 + (int)(box & 31u) + local - yy * bw;
+          y = ty0 + (int)((box >> 5) & 31u) + yy;
+        }
         // sign of face_normal . ray_w: the affine surrogate decides unless
         // it is within its error bound of zero; then the reference's ray.
         const float sv = fmaf(r3.x, (float)x, fmaf(r3.y, (float)y, r3.z));
@@ -727,6 +755,7 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           R.r2[j] = make_float4(z0, z1, z2, __int_as_float(f));
           R.r3[j] = make_float4(sa, sb, sc, tol);
           R.r5[j] = make_float4(z1 * z2, z0 * z2, z0 * z1, aP);
+          R.r4[j] = make_uint4(0u, 0u, 0u, 0u);  // the whole box, unless raster_pass narrows it
           R.cnt[j] = bw * bh;
         }
         __syncthreads();
