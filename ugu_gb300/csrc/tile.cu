@@ -13,13 +13,14 @@
 //   k_gather copies every run into its tile's range: faces drawn first from
 //            the front, faces drawn last from the back.
 //   k_tile   persistent blocks pull (view, tile) items from a work queue.
-//            For one tile: set the listed faces up in shared memory with
+//            For one tile, each warp on its own: take the next 32 listed
+//            faces, set them up in the warp's slots of shared memory with
 //            their candidate pixels (the box-in-tile, or conservative row
-//            spans for small faces, span.cuh), split each warp's 32 faces
-//            into (face, pixel) pairs with a warp prefix scan of their
-//            candidate counts, test every pair's
-//            coverage (Loop B's pixel test), queue the covered ones and run
-//            their z-test 32 at a time into a shared-memory z-buffer of
+//            spans for small faces, span.cuh), split them into (face, pixel)
+//            pairs with a warp prefix scan of their candidate counts, test
+//            every pair's coverage (Loop B's pixel test), queue the covered
+//            ones and run their z-test 32 at a time into the block's
+//            shared-memory z-buffer of
 //            64-bit (depth bits << 32 | face id << 1 | back-face bit) keys
 //            with atomicMin, then run Loop C (rasterizer.cc:244-301) for the
 //            tile's pixels: depth, face id, mask and the shading.
@@ -48,10 +49,7 @@ constexpr int kScanThreads = 1024;
 #endif
 constexpr int kTileThreads = UGU_TILE_THREADS;  // one tile per block
 constexpr int kWarps = kTileThreads / 32;
-#ifndef UGU_TILE_CHUNK
-#define UGU_TILE_CHUNK UGU_TILE_THREADS
-#endif
-constexpr int kChunk = UGU_TILE_CHUNK;  // faces set up in shared memory at a time
+constexpr int kChunk = kTileThreads;  // window slots: 32 faces per warp
 static_assert(kChunk <= 256, "queue entries hold an 8-bit face slot");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kBinFaces = 4;     // faces per binning thread
@@ -455,8 +453,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
   }
 }
 
-// Faces of one tile set up in shared memory, one window of kChunk entries
-// at a time.
+// Faces of one tile set up in shared memory: warp w owns slots
+// [32 w, 32 w + 32) and holds up to 32 of its entries there at a time.
 struct Region {
   float4 r0[kChunk];  // v0.x v0.y v1.x v1.y
   float4 r1[kChunk];  // v2.x v2.y area box (pack_box)
@@ -487,6 +485,7 @@ struct TileSmem {
   DevMesh mesh;
   int item;
   unsigned zmax_bits;
+  int cursor[2];  // next entry of each draw class: warps take 32 at a time
 };
 
 // The reference's back-face test fn . ray_w(x, y) > 0 (rasterizer.cc:199),
@@ -535,11 +534,11 @@ __device__ __forceinline__ void depth_test(TileSmem& sm, const Region& R, const 
   if (key < *(volatile unsigned long long*)kp) atomicMin(kp, key);
 }
 
-// Loop B (rasterizer.cc:196-237) over a window's faces.  Each warp takes 32
-// faces, flattens their (face, pixel) pairs with a prefix scan and tests one
-// pair per lane: back-face sign, edge functions, coverage.  Covered pairs go
-// to the warp's queue; every 32 of them take the depth test together, one
-// per lane.
+// Loop B (rasterizer.cc:196-237) over the m <= 32 faces the warp set up in
+// its own slots of the window: flatten their (face, pixel) pairs with a
+// prefix scan and test one pair per lane: back-face sign, edge functions,
+// coverage.  Covered pairs go to the warp's queue; every 32 of them take the
+// depth test together, one per lane.
 __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileParams& p,
                                             const Cam& c, int m, int tx0, int ty0, int tlog) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -547,9 +546,10 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
   float4* Q = sm.queue[warp];
   int* pre = sm.pre[warp];
   int qn = 0;
-  for (int base = warp * 32; base < m; base += kTileThreads) {
+  {
+    const int base = warp * 32;
     const int j = base + lane;
-    int cnt = j < m ? R.cnt[j] : 0;
+    int cnt = lane < m ? R.cnt[j] : 0;
     // the candidate pixels of the lane's face: its row spans when the face is
     // small enough (span.cuh), else the whole box-in-tile
     if (cnt > 0) {
@@ -649,7 +649,7 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
 __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TileParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tlog = p.tile_log2;
   const int T = 1 << tlog;
   if (p.counters->dropped) return;  // entries were not written: the host retries
@@ -678,6 +678,10 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
     // entries drawn first: [e0, e1); drawn last: [e1, e2)
     const int e0 = p.tile_off[item], e1 = p.tile_lo[item], e2 = p.tile_off[item + 1];
     const float4* proj = p.proj + sm.view.proj_offset;
+    if (tid == 0) {
+      sm.cursor[0] = e0;
+      sm.cursor[1] = e1;
+    }
     __syncthreads();
 
     // Per-view constants of the back-face surrogate and its error bound.
@@ -693,7 +697,8 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
       float zmax = __int_as_float(0x7f800000);
       if (phase == 1) {
         if (e2 == e1) break;
-        // deepest key of the tile (+inf while any pixel is still empty)
+        // deepest key of the tile (+inf while any pixel is still empty),
+        // once every warp has drawn its faces of the first class
         if (tid == 0) sm.zmax_bits = 0u;
         __syncthreads();
         float zm = 0.0f;
@@ -709,14 +714,21 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
         __syncthreads();
         zmax = __uint_as_float(sm.zmax_bits);
       }
-      const int eb = phase ? e1 : e0, ee = phase ? e2 : e1;
-      for (int cs = eb; cs < ee; cs += kChunk) {
-        const int m = min(kChunk, ee - cs);
-#pragma unroll 2
-        for (int j = tid; j < m; j += kTileThreads) {
-          const int2 e = p.entries[cs + j];
+      const int ee = phase ? e2 : e1;
+      // Each warp takes the class's next 32 entries, sets them up in its own
+      // 32 slots of the window and draws them; warps meet only at the class
+      // boundary, so one warp's large faces hold up no other warp.
+      for (;;) {
+        int cs = 0;
+        if (lane == 0) cs = atomicAdd(&sm.cursor[phase], 32);
+        cs = __shfl_sync(0xffffffffu, cs, 0);
+        if (cs >= ee) break;
+        const int m = min(32, ee - cs);
+        const int j = warp * 32 + lane;
+        R.cnt[j] = 0;
+        if (lane < m) do {  // `continue` leaves the slot empty
+          const int2 e = p.entries[cs + lane];
           const float zlb = __int_as_float(e.y);
-          R.cnt[j] = 0;
           if ((unsigned)e.x >= (unsigned)sm.mesh.num_faces) {  // never for k_bin's entries
             atomicAdd(&p.counters->invalid, 1u);
             continue;
@@ -757,12 +769,13 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           R.r5[j] = make_float4(z1 * z2, z0 * z2, z0 * z1, aP);
           R.r4[j] = make_uint4(0u, 0u, 0u, 0u);  // the whole box, unless raster_pass narrows it
           R.cnt[j] = bw * bh;
-        }
-        __syncthreads();
+        } while (0);
+        __syncwarp();
         raster_pass(sm, R, p, c, m, tx0, ty0, tlog);
-        __syncthreads();
+        __syncwarp();
       }
     }
+    __syncthreads();  // every face drawn
 
     // Loop C (rasterizer.cc:244-301) for the tile's pixels.
     const DevView& V = sm.view;
