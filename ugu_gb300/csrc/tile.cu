@@ -50,6 +50,7 @@ constexpr int kScanThreads = 1024;
 constexpr int kTileThreads = UGU_TILE_THREADS;  // one tile per block
 constexpr int kWarps = kTileThreads / 32;
 constexpr int kChunk = kTileThreads;  // window slots: 32 faces per warp
+constexpr int kSplitClass = 64;  // classes this small are shared out evenly over the warps
 static_assert(kChunk <= 256, "queue entries hold an 8-bit face slot");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kBinFaces = 4;     // faces per binning thread
@@ -714,16 +715,20 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
         __syncthreads();
         zmax = __uint_as_float(sm.zmax_bits);
       }
-      const int ee = phase ? e2 : e1;
-      // Each warp takes the class's next 32 entries, sets them up in its own
-      // 32 slots of the window and draws them; warps meet only at the class
-      // boundary, so one warp's large faces hold up no other warp.
+      const int eb = phase ? e1 : e0, ee = phase ? e2 : e1;
+      // Each warp takes the class's next entries (32, or a quarter of a
+      // class of at most kSplitClass entries, so that few large faces still
+      // keep every warp busy), sets them up in its own 32 slots of the window
+      // and draws them; warps meet only at the class boundary, so one warp's
+      // large faces hold up no other warp.
+      const int grab =
+          ee - eb <= kSplitClass ? min(32, max(1, (ee - eb + kWarps - 1) / kWarps)) : 32;
       for (;;) {
         int cs = 0;
-        if (lane == 0) cs = atomicAdd(&sm.cursor[phase], 32);
+        if (lane == 0) cs = atomicAdd(&sm.cursor[phase], grab);
         cs = __shfl_sync(0xffffffffu, cs, 0);
         if (cs >= ee) break;
-        const int m = min(32, ee - cs);
+        const int m = min(grab, ee - cs);
         const int j = warp * 32 + lane;
         R.cnt[j] = 0;
         if (lane < m) do {  // `continue` leaves the slot empty
