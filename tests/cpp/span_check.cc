@@ -76,10 +76,11 @@ void make_face(Rng& r, int kind, float v[6]) {
       v[2 * j + 1] += r.range(-300, 300);
       break;
     }
-    case 4: {  // medium faces, up to 8 rows
+    case 4: {  // medium faces, up to 8 or up to 16 rows
+      const double h = r.uni() < 0.5 ? 4.5 : 9.0;
       for (int i = 0; i < 3; ++i) {
         v[2 * i] = cx + r.range(-20, 20);
-        v[2 * i + 1] = cy + r.range(-4.5, 4.5);
+        v[2 * i + 1] = cy + r.range(-h, h);
       }
       break;
     }
@@ -140,7 +141,8 @@ int main(int argc, char** argv) {
           span_px += s.count;
           span_box += (long long)bw * bh;
           span_cand += s.count;
-          if (s.count > kSpanMax || !(s.start_hi & kSpanFlag)) {
+          if (s.count > kSpanMax || !(s.start[1] & kSpanFlag) ||
+              ((s.start[1] & kSpanTall) != 0) != (bh > 8)) {
             std::printf("FAIL bad count or flag: face %ld count %d\n", f, s.count);
             return 1;
           }

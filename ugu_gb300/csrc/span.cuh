@@ -23,7 +23,8 @@
 //
 // Faces with more than kSpanRows rows in the tile, more than kSpanMax
 // candidate pixels, extents above 4096 pixels, or |area| at or below the
-// threshold keep the whole box.
+// threshold keep the whole box.  Spans of up to 8 rows take 16 bytes, of
+// up to 16 rows 32.
 #pragma once
 
 #include <cmath>
@@ -37,18 +38,21 @@
 
 namespace ugu_gpu {
 
-constexpr int kSpanRows = 8;   // rows of a face's box in one tile
+constexpr int kSpanRows = 16;  // rows of a face's box in one tile
 constexpr int kSpanMax = 127;  // candidate pixels (byte-wise compares need <= 127)
 
-// Byte r of cum (lo = bytes 0..3, hi = bytes 4..7): pixels in rows before r,
-// 127 for rows past the last.  Byte r of start: tile-local x of row r's first
-// candidate.  Bit 31 of start_hi marks a face that uses spans.
+// Byte r of the 16-byte cum (word w = bytes 4w .. 4w + 3): pixels in rows
+// before r, 127 for rows past the last.  Byte r of start: tile-local x of
+// row r's first candidate.  Bit 31 of start[1] marks a face that uses spans,
+// bit 30 one with more than 8 rows (words 2 and 3 in use; for other faces
+// they hold 127s and zeros and need not be stored).
 struct FaceSpans {
-  uint32_t cum_lo, cum_hi, start_lo, start_hi;
+  uint32_t cum[4], start[4];
   int count;
 };
 
 constexpr uint32_t kSpanFlag = 0x80000000u;
+constexpr uint32_t kSpanTall = 0x40000000u;
 
 // One edge's bound x >= T(y) (lower) or x <= T(y), T(y) = c0 + c1 y +/- mu.
 struct SpanEdge {
@@ -95,7 +99,8 @@ UGU_SPAN_HD bool face_spans(float v0x, float v0y, float v1x, float v1y, float v2
   e[0] = span_edge(v1x, v1y, v2x, v2y, g, err, ymag);
   e[1] = span_edge(v2x, v2y, v0x, v0y, g, err, ymag);
   e[2] = span_edge(v0x, v0y, v1x, v1y, g, err, ymag);
-  uint32_t cum_lo = 0x7f7f7f7fu, cum_hi = 0x7f7f7f7fu, start_lo = 0u, start_hi = 0u;
+  uint32_t c0 = 0x7f7f7f7fu, c1 = 0x7f7f7f7fu, c2 = 0x7f7f7f7fu, c3 = 0x7f7f7f7fu;
+  uint32_t s0 = 0u, s1 = 0u, s2 = 0u, s3 = 0u;
   int count = 0;
   for (int r = 0; r < rows; ++r) {
     const float y = (float)(by0 + r);
@@ -109,44 +114,73 @@ UGU_SPAN_HD bool face_spans(float v0x, float v0y, float v1x, float v1y, float v2
     const int w = hi >= lo ? (int)(hi - lo) + 1 : 0;
     const int sx = w ? (int)lo - tx0 : 0;
     const int sh = 8 * (r & 3);
+    const uint32_t cm = ~(0xffu << sh), cv = (uint32_t)count << sh, sv = (uint32_t)sx << sh;
     if (r < 4) {
-      cum_lo = (cum_lo & ~(0xffu << sh)) | ((uint32_t)count << sh);
-      start_lo |= (uint32_t)sx << sh;
+      c0 = (c0 & cm) | cv;
+      s0 |= sv;
+    } else if (r < 8) {
+      c1 = (c1 & cm) | cv;
+      s1 |= sv;
+    } else if (r < 12) {
+      c2 = (c2 & cm) | cv;
+      s2 |= sv;
     } else {
-      cum_hi = (cum_hi & ~(0xffu << sh)) | ((uint32_t)count << sh);
-      start_hi |= (uint32_t)sx << sh;
+      c3 = (c3 & cm) | cv;
+      s3 |= sv;
     }
     count += w;
     if (count > kSpanMax) return false;
   }
-  o.cum_lo = cum_lo;
-  o.cum_hi = cum_hi;
-  o.start_lo = start_lo;
-  o.start_hi = start_hi | kSpanFlag;
+  o.cum[0] = c0;
+  o.cum[1] = c1;
+  o.cum[2] = c2;
+  o.cum[3] = c3;
+  o.start[0] = s0;
+  o.start[1] = s1 | kSpanFlag | (rows > 8 ? kSpanTall : 0u);
+  o.start[2] = s2;
+  o.start[3] = s3;
   o.count = count;
   return true;
 }
 
-// Tile-local (x, y) offsets of candidate number k < count of a span face
-// whose box-in-tile starts at row y0: the row is the last one whose byte in
-// cum is <= k (bytes compared four at a time: k + 128 - c keeps bit 7 set
-// exactly when k >= c, for k, c <= 127).
+// Tile-local x offset and box row of candidate number k < count of a span
+// face: the row is the last one whose byte in cum is <= k (bytes compared
+// four at a time: k + 128 - c keeps bit 7 set exactly when k >= c, for
+// k, c <= 127).  Words 2 and 3 are read only for a face flagged tall.
+UGU_SPAN_HD uint32_t span_ge(uint32_t kk, uint32_t c) { return (kk - c) & 0x80808080u; }
+
+UGU_SPAN_HD int span_popc(uint32_t v) {
+#ifdef __CUDA_ARCH__
+  return __popc(v);
+#else
+  return __builtin_popcount(v);
+#endif
+}
+
+// Byte n (0..7) of the 8 bytes lo | hi << 32.
+UGU_SPAN_HD uint32_t span_byte(uint32_t lo, uint32_t hi, int n) {
+#ifdef __CUDA_ARCH__
+  return __byte_perm(lo, hi, (uint32_t)n) & 0xffu;
+#else
+  return (uint32_t)((((uint64_t)hi << 32) | lo) >> (8 * n)) & 0xffu;
+#endif
+}
+
 UGU_SPAN_HD void span_pixel(const FaceSpans& s, int k, int& dx, int& row) {
   const uint32_t kk = ((uint32_t)k * 0x01010101u) | 0x80808080u;
-  const uint32_t a = (kk - s.cum_lo) & 0x80808080u;
-  const uint32_t b = (kk - s.cum_hi) & 0x80808080u;
-#ifdef __CUDA_ARCH__
-  row = __popc(a) + __popc(b) - 1;
-  const uint32_t c = __byte_perm(s.cum_lo, s.cum_hi, (uint32_t)row) & 0xffu;
-  const uint32_t x0 = __byte_perm(s.start_lo, s.start_hi, (uint32_t)row) & 0x1fu;
-#else
-  row = __builtin_popcount(a) + __builtin_popcount(b) - 1;
-  const uint64_t cum = (uint64_t)s.cum_lo | ((uint64_t)s.cum_hi << 32);
-  const uint64_t st = (uint64_t)s.start_lo | ((uint64_t)s.start_hi << 32);
-  const uint32_t c = (uint32_t)(cum >> (8 * row)) & 0xffu;
-  const uint32_t x0 = (uint32_t)(st >> (8 * row)) & 0x1fu;
-#endif
-  dx = (int)x0 + k - (int)c;
+  int n = span_popc(span_ge(kk, s.cum[0])) + span_popc(span_ge(kk, s.cum[1]));
+  const bool tall = (s.start[1] & kSpanTall) != 0u;
+  if (tall) n += span_popc(span_ge(kk, s.cum[2])) + span_popc(span_ge(kk, s.cum[3]));
+  row = n - 1;
+  uint32_t c, x0;
+  if (row < 8) {
+    c = span_byte(s.cum[0], s.cum[1], row);
+    x0 = span_byte(s.start[0], s.start[1], row);
+  } else {
+    c = span_byte(s.cum[2], s.cum[3], row - 8);
+    x0 = span_byte(s.start[2], s.start[3], row - 8);
+  }
+  dx = (int)(x0 & 0x1fu) + k - (int)c;
 }
 
 }  // namespace ugu_gpu

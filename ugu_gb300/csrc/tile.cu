@@ -462,7 +462,8 @@ struct Region {
   float4 r2[kChunk];  // v0.z v1.z v2.z fid-bits
   float4 r3[kChunk];  // back-face sign surrogate: sa sb sc tolerance
   float4 r5[kChunk];  // depth pre-test: z1 z2, z0 z2, z0 z1, |area| z0 z1 z2 (1 - 2^-16)
-  uint4 r4[kChunk];   // row spans (FaceSpans: cum_lo cum_hi start_lo start_hi), or 0
+  uint4 r4[kChunk];   // row spans (FaceSpans words cum 0, 1, start 0, 1), or 0
+  uint4 r6[kChunk];   // FaceSpans words cum 2, 3, start 2, 3 of a face flagged tall
   int cnt[kChunk];    // bbox-in-tile pixels, 0 when the face is skipped
 };
 
@@ -562,7 +563,9 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
       if (face_spans(a.x, a.y, a.z, a.w, b.x, b.y, b.z, bx0, bx0 + bw - 1, by0, by0 + bh - 1,
                      tx0, sp)) {
         cnt = sp.count;
-        R.r4[j] = make_uint4(sp.cum_lo, sp.cum_hi, sp.start_lo, sp.start_hi);
+        R.r4[j] = make_uint4(sp.cum[0], sp.cum[1], sp.start[0], sp.start[1]);
+        if (sp.start[1] & kSpanTall)
+          R.r6[j] = make_uint4(sp.cum[2], sp.cum[3], sp.start[2], sp.start[3]);
       }
     }
     int incl = cnt;
@@ -592,7 +595,14 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
         const unsigned box = __float_as_uint(r1.w);
         int x, y;
         if (r4.w & kSpanFlag) {  // candidate `local` of the face's row spans
-          const FaceSpans sp = {r4.x, r4.y, r4.z, r4.w, 0};
+          FaceSpans sp = {{r4.x, r4.y, 0x7f7f7f7fu, 0x7f7f7f7fu}, {r4.z, r4.w, 0u, 0u}, 0};
+          if (r4.w & kSpanTall) {
+            const uint4 r6 = R.r6[jj];
+            sp.cum[2] = r6.x;
+            sp.cum[3] = r6.y;
+            sp.start[2] = r6.z;
+            sp.start[3] = r6.w;
+          }
           int dx, row;
           span_pixel(sp, local, dx, row);
           x = tx0 + dx;
