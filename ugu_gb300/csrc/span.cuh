@@ -102,7 +102,8 @@ UGU_SPAN_HD bool face_spans(float v0x, float v0y, float v1x, float v1y, float v2
   uint32_t c0 = 0x7f7f7f7fu, c1 = 0x7f7f7f7fu, c2 = 0x7f7f7f7fu, c3 = 0x7f7f7f7fu;
   uint32_t s0 = 0u, s1 = 0u, s2 = 0u, s3 = 0u;
   int count = 0;
-  for (int r = 0; r < rows; ++r) {
+  // candidate interval of box row r: its width, and its first x relative to the tile
+  auto row_span = [&](int r, int& w, int& sx) {
     const float y = (float)(by0 + r);
     float lo = (float)bx0, hi = (float)bx1;
 #pragma unroll
@@ -111,17 +112,31 @@ UGU_SPAN_HD bool face_spans(float v0x, float v0y, float v1x, float v1y, float v2
       if (e[k].kind > 0) lo = fmaxf(lo, ceilf(t - e[k].mu));
       if (e[k].kind < 0) hi = fminf(hi, floorf(t + e[k].mu));
     }
-    const int w = hi >= lo ? (int)(hi - lo) + 1 : 0;
-    const int sx = w ? (int)lo - tx0 : 0;
+    w = hi >= lo ? (int)(hi - lo) + 1 : 0;
+    sx = w ? (int)lo - tx0 : 0;
+  };
+  const int rows_lo = rows < 8 ? rows : 8;
+  for (int r = 0; r < rows_lo; ++r) {
+    int w, sx;
+    row_span(r, w, sx);
     const int sh = 8 * (r & 3);
     const uint32_t cm = ~(0xffu << sh), cv = (uint32_t)count << sh, sv = (uint32_t)sx << sh;
     if (r < 4) {
       c0 = (c0 & cm) | cv;
       s0 |= sv;
-    } else if (r < 8) {
+    } else {
       c1 = (c1 & cm) | cv;
       s1 |= sv;
-    } else if (r < 12) {
+    }
+    count += w;
+    if (count > kSpanMax) return false;
+  }
+  for (int r = 8; r < rows; ++r) {
+    int w, sx;
+    row_span(r, w, sx);
+    const int sh = 8 * (r & 3);
+    const uint32_t cm = ~(0xffu << sh), cv = (uint32_t)count << sh, sv = (uint32_t)sx << sh;
+    if (r < 12) {
       c2 = (c2 & cm) | cv;
       s2 |= sv;
     } else {

@@ -482,13 +482,18 @@ struct TileSmem {
   unsigned long long keys[kMaxTile * kMaxTile];
   Region reg;
   float4 queue[kWarps][kQueue];  // (w0, w1, w2, face slot | x << 8 | y << 13 | bf << 18)
-  int pre[kWarps][33];
   DevView view;
   DevMesh mesh;
   int item;
   unsigned zmax_bits;
   int cursor[2];  // next entry of each draw class: warps take 32 at a time
 };
+// Seven blocks (with the 1 KB each block reserves) within the 196 KB
+// shared-memory carve-out, which leaves 60 KB of L1 for the gathers; one
+// byte more per SM and the carve-out becomes 228 KB with 28 KB of L1.
+static_assert(UGU_TILE_THREADS != 128 || UGU_TILE_BLOCKS != 7 ||
+                  7 * (sizeof(TileSmem) + 1024) <= 196 * 1024,
+              "k_tile's shared memory no longer fits the 196 KB carve-out");
 
 // The reference's back-face test fn . ray_w(x, y) > 0 (rasterizer.cc:199),
 // for the rare pixels the surrogate cannot decide; kept out of line so the
@@ -546,7 +551,6 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   float4* Q = sm.queue[warp];
-  int* pre = sm.pre[warp];
   int qn = 0;
   {
     const int base = warp * 32;
@@ -575,19 +579,21 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
       if (lane >= o) incl += t;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    pre[lane] = incl - cnt;
-    __syncwarp();
+    const int pre = incl - cnt;  // the lane's face: its first pair number
+    __syncwarp();                // the spans written above, for every lane
     for (int kb = 0; kb < total; kb += 32) {
       const int k = kb + lane;
+      // the face of pair k: the last lane whose first pair number is <= k
+      int q = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (__shfl_sync(0xffffffffu, pre, q + step) <= k) q += step;
+      const int pre_q = __shfl_sync(0xffffffffu, pre, q);
       bool cov = false;
       float4 ent;
       if (k < total) {
-        int q = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-          if (pre[q + step] <= k) q += step;
         const int jj = base + q;
-        const int local = k - pre[q];
+        const int local = k - pre_q;
         const float4 r0 = R.r0[jj];
         const float4 r1 = R.r1[jj];
         const float4 r3 = R.r3[jj];
