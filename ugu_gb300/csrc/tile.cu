@@ -18,9 +18,8 @@
 //            their candidate pixels (the box-in-tile, or conservative row
 //            spans for small faces, span.cuh), split them into (face, pixel)
 //            pairs with a warp prefix scan of their candidate counts, test
-//            every pair's coverage (Loop B's pixel test), queue the covered
-//            ones and run their z-test 32 at a time into the block's
-//            shared-memory z-buffer of
+//            every pair's coverage (Loop B's pixel test) and run the covered
+//            ones' z-test into the block's shared-memory z-buffer of
 //            64-bit (depth bits << 32 | face id << 1 | back-face bit) keys
 //            with atomicMin, then run Loop C (rasterizer.cc:244-301) for the
 //            tile's pixels: depth, face id, mask and the shading.
@@ -51,7 +50,7 @@ constexpr int kTileThreads = UGU_TILE_THREADS;  // one tile per block
 constexpr int kWarps = kTileThreads / 32;
 constexpr int kChunk = kTileThreads;  // window slots: 32 faces per warp
 constexpr int kSplitClass = 64;  // classes this small are shared out evenly over the warps
-static_assert(kChunk <= 256, "queue entries hold an 8-bit face slot");
+static_assert(kChunk <= 256, "a covered pair packs its face slot in 8 bits");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kBinFaces = 4;     // faces per binning thread
 constexpr int kAgg = 256;        // distinct tiles a binning block aggregates
@@ -464,7 +463,6 @@ struct Region {
   float4 r5[kChunk];  // depth pre-test: z1 z2, z0 z2, z0 z1, |area| z0 z1 z2 (1 - 2^-16)
   uint4 r4[kChunk];   // row spans (FaceSpans words cum 0, 1, start 0, 1), or 0
   uint4 r6[kChunk];   // FaceSpans words cum 2, 3, start 2, 3 of a face flagged tall
-  int cnt[kChunk];    // bbox-in-tile pixels, 0 when the face is skipped
 };
 
 // A face's bbox-in-tile in 32 bits: tile-local x0 and y0, width - 1 (5 bits
@@ -476,24 +474,23 @@ __device__ __forceinline__ float pack_box(int x0, int y0, int w) {
                          (m << 15));
 }
 
-constexpr int kQueue = 64;  // covered candidates a warp holds before its depth pass
 
 struct TileSmem {
   unsigned long long keys[kMaxTile * kMaxTile];
   Region reg;
-  float4 queue[kWarps][kQueue];  // (w0, w1, w2, face slot | x << 8 | y << 13 | bf << 18)
   DevView view;
   DevMesh mesh;
   int item;
   unsigned zmax_bits;
   int cursor[2];  // next entry of each draw class: warps take 32 at a time
 };
-// Seven blocks (with the 1 KB each block reserves) within the 196 KB
-// shared-memory carve-out, which leaves 60 KB of L1 for the gathers; one
-// byte more per SM and the carve-out becomes 228 KB with 28 KB of L1.
+// Seven blocks (with the 1 KB each block reserves) within the 164 KB
+// shared-memory carve-out, which leaves 92 KB of L1 for the setup and
+// shading gathers; past 164 KB the carve-out becomes 196 KB (60 KB of L1),
+// past 196 KB 228 KB (28 KB of L1), each step a few percent slower.
 static_assert(UGU_TILE_THREADS != 128 || UGU_TILE_BLOCKS != 7 ||
-                  7 * (sizeof(TileSmem) + 1024) <= 196 * 1024,
-              "k_tile's shared memory no longer fits the 196 KB carve-out");
+                  7 * (sizeof(TileSmem) + 1024) <= 164 * 1024,
+              "k_tile's shared memory no longer fits the 164 KB carve-out");
 
 // The reference's back-face test fn . ray_w(x, y) > 0 (rasterizer.cc:199),
 // for the rare pixels the surrogate cannot decide; kept out of line so the
@@ -544,18 +541,17 @@ __device__ __forceinline__ void depth_test(TileSmem& sm, const Region& R, const 
 // Loop B (rasterizer.cc:196-237) over the m <= 32 faces the warp set up in
 // its own slots of the window: flatten their (face, pixel) pairs with a
 // prefix scan and test one pair per lane: back-face sign, edge functions,
-// coverage.  Covered pairs go to the warp's queue; every 32 of them take the
-// depth test together, one per lane.
+// coverage.  A covered pair takes the depth test at once: with row spans
+// most lanes' pairs are covered, so batching them buys nothing.  `box_cnt`
+// is the lane's face's bbox-in-tile pixel count (0 for an empty slot).
 __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileParams& p,
-                                            const Cam& c, int m, int tx0, int ty0, int tlog) {
+                                            const Cam& c, int m, int tx0, int ty0, int tlog,
+                                            int box_cnt) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const unsigned below = (1u << lane) - 1u;
-  float4* Q = sm.queue[warp];
-  int qn = 0;
   {
     const int base = warp * 32;
     const int j = base + lane;
-    int cnt = lane < m ? R.cnt[j] : 0;
+    int cnt = lane < m ? box_cnt : 0;
     // the candidate pixels of the lane's face: its row spans when the face is
     // small enough (span.cuh), else the whole box-in-tile
     if (cnt > 0) {
@@ -642,25 +638,10 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
                           __int_as_float((jj & 255) | ((x - tx0) << 8) | ((y - ty0) << 13) |
                                          (bf ? 1 << 18 : 0)));
       }
-      const unsigned bal = __ballot_sync(0xffffffffu, cov);
-      if (cov) Q[qn + __popc(bal & below)] = ent;
-      qn += __popc(bal);
-      if (qn >= 32) {
-        __syncwarp();
-        depth_test(sm, R, p, Q[lane], tlog);
-        const int rest = qn - 32;
-        float4 t;
-        if (lane < rest) t = Q[32 + lane];
-        __syncwarp();
-        if (lane < rest) Q[lane] = t;
-        __syncwarp();
-        qn = rest;
-      }
+      if (cov) depth_test(sm, R, p, ent, tlog);
     }
     __syncwarp();
   }
-  __syncwarp();
-  if (lane < qn) depth_test(sm, R, p, Q[lane], tlog);
 }
 
 __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TileParams p) {
@@ -746,7 +727,7 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
         if (cs >= ee) break;
         const int m = min(grab, ee - cs);
         const int j = warp * 32 + lane;
-        R.cnt[j] = 0;
+        int box_cnt = 0;    // the slot's bbox-in-tile pixels, 0 when the face is skipped
         if (lane < m) do {  // `continue` leaves the slot empty
           const int2 e = p.entries[cs + lane];
           const float zlb = __int_as_float(e.y);
@@ -789,10 +770,10 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           R.r3[j] = make_float4(sa, sb, sc, tol);
           R.r5[j] = make_float4(z1 * z2, z0 * z2, z0 * z1, aP);
           R.r4[j] = make_uint4(0u, 0u, 0u, 0u);  // the whole box, unless raster_pass narrows it
-          R.cnt[j] = bw * bh;
+          box_cnt = bw * bh;
         } while (0);
         __syncwarp();
-        raster_pass(sm, R, p, c, m, tx0, ty0, tlog);
+        raster_pass(sm, R, p, c, m, tx0, ty0, tlog, box_cnt);
         __syncwarp();
       }
     }
