@@ -44,7 +44,7 @@ constexpr int kScanThreads = 1024;
 #define UGU_TILE_THREADS 128
 #endif
 #ifndef UGU_TILE_BLOCKS
-#define UGU_TILE_BLOCKS 7
+#define UGU_TILE_BLOCKS 8
 #endif
 constexpr int kTileThreads = UGU_TILE_THREADS;  // one tile per block
 constexpr int kWarps = kTileThreads / 32;
@@ -484,13 +484,13 @@ struct TileSmem {
   unsigned zmax_bits;
   int cursor[2];  // next entry of each draw class: warps take 32 at a time
 };
-// Seven blocks (with the 1 KB each block reserves) within the 164 KB
-// shared-memory carve-out, which leaves 92 KB of L1 for the setup and
-// shading gathers; past 164 KB the carve-out becomes 196 KB (60 KB of L1),
-// past 196 KB 228 KB (28 KB of L1), each step a few percent slower.
-static_assert(UGU_TILE_THREADS != 128 || UGU_TILE_BLOCKS != 7 ||
-                  7 * (sizeof(TileSmem) + 1024) <= 164 * 1024,
-              "k_tile's shared memory no longer fits the 164 KB carve-out");
+// Eight blocks (with the 1 KB each block reserves) within the 196 KB
+// shared-memory carve-out, which leaves 60 KB of L1 for the setup and
+// shading gathers; past 196 KB the carve-out becomes 228 KB with 28 KB of
+// L1, which costs the gathers a few percent.
+static_assert(UGU_TILE_THREADS != 128 || UGU_TILE_BLOCKS != 8 ||
+                  8 * (sizeof(TileSmem) + 1024) <= 196 * 1024,
+              "k_tile's shared memory no longer fits the 196 KB carve-out");
 
 // The reference's back-face test fn . ray_w(x, y) > 0 (rasterizer.cc:199),
 // for the rare pixels the surrogate cannot decide; kept out of line so the
