@@ -52,7 +52,7 @@ constexpr int kChunk = kTileThreads;  // window slots: 32 faces per warp
 constexpr int kSplitClass = 64;  // classes this small are shared out evenly over the warps
 static_assert(kChunk <= 256, "a covered pair packs its face slot in 8 bits");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
-constexpr int kBinFaces = 4;     // faces per binning thread
+constexpr int kBinFaces = 2;     // faces per binning thread
 constexpr int kAgg = 256;        // distinct tiles a binning block aggregates
 constexpr int kAggPerFace = 2;   // faces touching more tiles take cursor positions
 constexpr int kAggProbes = 8;
@@ -197,7 +197,7 @@ __device__ __forceinline__ int find_slot(const BinSmem& sb, int t) {
 // per-group cursors after the fast ones; entries whose tile finds no slot
 // in the table (at most kAggProbes probes) become runs of one.
 #ifndef UGU_BIN_BLOCKS
-#define UGU_BIN_BLOCKS 4
+#define UGU_BIN_BLOCKS 6
 #endif
 __global__ void __launch_bounds__(kBinThreads, UGU_BIN_BLOCKS) k_bin(TileParams p) {
   __shared__ BinSmem sb;
