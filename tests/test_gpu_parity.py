@@ -57,6 +57,63 @@ def test_triangle_soup_seeds(ctx, oracle_lib, seed):
         compare(ref, got, f"soup{seed}")
 
 
+def span_scene(cam, n=2500, seed=31):
+    """Faces of the shapes the tiled path's row spans must handle, placed in
+    screen space and lifted to camera depths 1.5 .. 6: small faces, slivers
+    (one vertex 1e-6 .. 1 pixel off a long edge), vertices on integer and
+    half-integer pixel lines, faces of 9 to 16 rows, near-collinear faces
+    around the spans' area threshold, and nearly horizontal or vertical
+    edges."""
+    rng = np.random.default_rng(seed)
+    W, H = cam.width, cam.height
+    verts, faces = [], []
+    for i in range(n):
+        kind = i % 6
+        cx, cy = rng.uniform(-4, W + 4), rng.uniform(-4, H + 4)
+        if kind == 0:
+            s = 0.3 + 12 * rng.uniform() ** 2
+            p = np.stack([cx + s * (rng.uniform(size=3) - 0.5), cy + s * (rng.uniform(size=3) - 0.5)], 1)
+        elif kind == 1:
+            ln, ang = 1 + 40 * rng.uniform(), 2 * np.pi * rng.uniform()
+            dx, dy = ln * np.cos(ang), ln * np.sin(ang)
+            t, off = rng.uniform(), 10 ** rng.uniform(-6, 0) * rng.choice([-1, 1])
+            p = np.array([[cx, cy], [cx + dx, cy + dy],
+                          [cx + t * dx - off * dy / ln, cy + t * dy + off * dx / ln]])
+        elif kind == 2:
+            p = np.stack([np.floor(cx) + 0.5 * rng.integers(0, 13, 3) - 3,
+                          np.floor(cy) + 0.5 * rng.integers(0, 13, 3) - 3], 1)
+        elif kind == 3:
+            p = np.stack([cx + rng.uniform(-12, 12, 3), cy + rng.uniform(-8.5, 8.5, 3)], 1)
+        elif kind == 4:
+            dx, dy, t = rng.uniform(-12, 12), rng.uniform(-6, 6), rng.uniform()
+            p = np.array([[cx, cy], [cx + dx, cy + dy], [cx + t * dx, cy + t * dy]], np.float32)
+            p[2] = np.nextafter(p[2], p[2] + rng.choice([-1, 1]) * 1e3)
+        else:
+            p = np.array([[cx, cy], [cx + rng.uniform(-10, 10), cy + rng.uniform(-1e-4, 1e-4)],
+                          [cx + rng.uniform(-1e-4, 1e-4), cy + rng.uniform(-6, 6)]])
+            if rng.uniform() < 0.5:
+                p = p[:, ::-1].copy()
+        z = rng.uniform(1.5, 6.0)
+        k = len(verts)
+        verts += [adv.unproject(cam, float(x), float(y), z) for x, y in p]
+        faces.append([k, k + 1, k + 2])
+    return adv._finish(np.array(verts, np.float32), np.array(faces, np.int32))
+
+
+@pytest.mark.parametrize("seed", [31, 32])
+def test_span_shapes_tiled(ctx, oracle_lib, seed):
+    """The tiled path with its row spans against the oracle on faces shaped
+    to stress the spans' bound and encoding (slivers, pixel-line vertices,
+    9-16-row faces, near-threshold areas): every output bit for bit."""
+    cam = adv.identity_camera(W=256, H=192, f=160.0)
+    m = span_scene(cam, seed=seed)
+    for opt in (adv.option(1, 1, 1, 0, True), adv.option(2, 0, 0, 1, False)):
+        ref, _ = oracle_render(oracle_lib, m, cam, opt)
+        rc, got = gpu_render(ctx, m, cam, opt)
+        assert rc == 0, ctx.last_error()
+        compare(ref, got, f"spans{seed}")
+
+
 def test_uv_sphere_vertex_color_640x480(ctx, oracle_lib):
     m, cam = scenes.scene_uv_sphere_vertex_color()
     opt = adv.option(2, 1, 1, 0, True)
