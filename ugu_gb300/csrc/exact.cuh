@@ -161,6 +161,18 @@ UGU_HD float perspective(const FaceSetup& s, Bary& b) {
   return z;
 }
 
+// The same weights when z is already known: z must be what perspective()
+// returns for these inputs (the depth the z-test stored for the pixel), so
+// that the result is bit-identical; one division fewer.
+UGU_HD void perspective_at(const FaceSetup& s, Bary& b, float z) {
+  const float w0 = fdiv(fdiv(b.w0, s.area), s.v0.z);
+  const float w1 = fdiv(fdiv(b.w1, s.area), s.v1.z);
+  const float w2 = fdiv(fdiv(b.w2, s.area), s.v2.z);
+  b.w0 = fmul(w0, z);
+  b.w1 = fmul(w1, z);
+  b.w2 = fmul(w2, z);
+}
+
 // 64-bit z-buffer key: depth bits, then face id, then the back-face flag.
 // For depths in [FLT_MIN, +inf] the unsigned order of the key is the order
 // of (depth, face id): atomicMin keeps the nearest candidate and, on equal

@@ -126,12 +126,18 @@ __device__ __forceinline__ void shade_uv(const ShadeOpts& p, const DevMesh& m, c
 }
 
 // Loop C body for a pixel whose final face id is > 0 (rasterizer.cc:254-299),
-// given the winning face's projected vertices and area.
-__device__ __forceinline__ void shade_face_pixel(const ShadeOpts& p, const DevMesh& m,
-                                                 const Cam& c, int fid, const FaceSetup& s,
-                                                 int x, int y, Shaded& out) {
+// given the winning face's projected vertices and area; with kDepth, the
+// pixel's z-buffer depth `z` stands in for the one perspective() would
+// recompute (bit-identical: the same inputs and operations).
+template <bool kDepth>
+__device__ __forceinline__ void shade_face_pixel_t(const ShadeOpts& p, const DevMesh& m,
+                                                   const Cam& c, int fid, const FaceSetup& s,
+                                                   int x, int y, float z, Shaded& out) {
   Bary w = edges_at(s, x, y);
-  perspective(s, w);
+  if (kDepth)
+    perspective_at(s, w, z);
+  else
+    perspective(s, w);
 
   // shading normal (:268-279) from the stored weights
   float sn[3] = {0.0f, 0.0f, 0.0f};
@@ -151,6 +157,12 @@ __device__ __forceinline__ void shade_face_pixel(const ShadeOpts& p, const DevMe
   }
   // the colorizer's u = w1, v = w2
   shade_uv(p, m, c, fid, w.w1, w.w2, sn, x, y, out);
+}
+
+__device__ __forceinline__ void shade_face_pixel(const ShadeOpts& p, const DevMesh& m,
+                                                 const Cam& c, int fid, const FaceSetup& s,
+                                                 int x, int y, Shaded& out) {
+  shade_face_pixel_t<false>(p, m, c, fid, s, x, y, 0.0f, out);
 }
 
 

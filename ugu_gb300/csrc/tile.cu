@@ -814,7 +814,7 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           s.v1 = make_float3(b.x, b.y, b.z);
           s.v2 = make_float3(d.x, d.y, d.z);
           s.area = edge_fn(a.x, a.y, b.x, b.y, d.x, d.y);
-          shade_face_pixel(p.shade, sm.mesh, c, fid, s, tx0 + lx, ty0 + ly, sh);
+          shade_face_pixel_t<true>(p.shade, sm.mesh, c, fid, s, tx0 + lx, ty0 + ly, depth, sh);
         }
         if (V.color) {
           V.color[3 * pix + 0] = sh.c[0];
