@@ -9,10 +9,11 @@ VisibilityInfo the way the reference does on the host -- per vertex the
 keyframes it is visible from, per face the keyframes all three of its
 vertices (corners) are visible from, with the averaged viewing angle and
 distance and the projected triangle's area (TestFaces, :551-604) -- and
-computes the simple statistics of CalcStat (mean colour, distance and
-viewing angle; the minimum-viewing-angle and minimum-distance keyframes;
-FaceInfo's max-area, min-viewing-angle and min-distance keyframes).
-Medians, weighted medians and modes of CalcStat are not reproduced.
+computes CalcStat's statistics (:68-176 and :202-224) with the float
+arithmetic of ugu's math helpers (include/ugu/util/math_util.h).  One case
+is not pinned: Median of an odd count >= 5 without force_org_val averages
+the element std::nth_element leaves just below the middle, which the C++
+standard does not fix; this takes the sorted one.
 """
 from __future__ import annotations
 
@@ -25,6 +26,96 @@ from . import capi
 from .rasterizer import Context
 
 F32 = np.float32
+
+
+def first_min(vals) -> int:
+    """Index std::min_element returns: the first minimum under `<`."""
+    idx = 0
+    for i in range(1, len(vals)):
+        if vals[i] < vals[idx]:
+            idx = i
+    return idx
+
+
+def normalize_weights(weights):
+    """NormalizeWeights (math_util.h:28-48): float weights plus 1e-6, divided
+    by their float sum when it exceeds 1e-6, else all 1 / n."""
+    nw = [F32(F32(w) + F32(1e-6)) for w in weights]
+    total = F32(0.0)
+    for w in nw:
+        total = F32(total + w)
+    if float(total) > 0.000001:
+        return [F32(w / total) for w in nw]
+    return [F32(F32(1.0) / F32(len(nw)))] * len(nw)
+
+
+def weighted_average(data, weights) -> np.ndarray:
+    """WeightedAverage (math_util.h:51-70): float products of the normalised
+    weights summed in double, then cast to float."""
+    nw = normalize_weights(weights)
+    acc = [0.0, 0.0, 0.0]
+    for d, w in zip(data, nw):
+        for k in range(3):
+            acc[k] += float(F32(F32(d[k]) * w))
+    return np.array(acc, np.float32)
+
+
+def weighted_median(data, weights):
+    """WeightedMedian (math_util.h:72-100): the element at which the float
+    running sum of the ascending normalised weights first exceeds 0.5 (the
+    first element when it never does).  The sort is stable, which is the
+    order std::sort gives for up to 16 elements (insertion sort); for more,
+    and only among equal weights, the C++ order is not fixed."""
+    nw = normalize_weights(weights)
+    order = sorted(range(len(data)), key=lambda i: float(nw[i]))
+    total, index = F32(0.0), 0
+    for i, j in enumerate(order):
+        total = F32(total + nw[j])
+        if total > F32(0.5):
+            index = i
+            break
+    return data[order[index]]
+
+
+def median(data, force_org_val: bool = False):
+    """Median (math_util.h:102-124) of floats: one value as is; two values
+    averaged (the first one with force_org_val); otherwise the (n/2)-th
+    smallest for an even count or force_org_val (not the mean of the two
+    middle ones), and for an odd count the mean of the middle one and the
+    next larger one."""
+    n = len(data)
+    if n == 1:
+        return F32(data[0])
+    if n == 2:
+        return F32(data[0]) if force_org_val else F32(F32(F32(data[0]) + F32(data[1])) * F32(0.5))
+    srt = sorted(F32(x) for x in data)
+    h = n // 2
+    if force_org_val or n % 2 == 0:
+        return srt[h]
+    return F32(F32(srt[h] + srt[h + 1]) * F32(0.5))
+
+
+def median_color(colors) -> np.ndarray:
+    """MedianColor (src/util/math_util.cc:44-56): Median per channel."""
+    return np.array([median([c[k] for c in colors]) for k in range(3)], np.float32)
+
+
+def mode(colors, weights=None):
+    """Both Mode overloads (math_util.h:127-180): counts (or float sums of
+    `weights`) per distinct colour in visit order; the mode is the first
+    colour whose total exceeds every earlier best.  Returns (mode, total,
+    occurrence dict keyed by colour tuples)."""
+    occ, best, freq = {}, None, (F32(0.0) if weights is not None else 0)
+    for i, c in enumerate(colors):
+        key = tuple(float(F32(x)) for x in c)
+        if weights is None:
+            occ[key] = occ.get(key, 0) + 1
+        else:
+            occ[key] = F32(occ.get(key, F32(0.0)) + F32(weights[i]))
+        if freq < occ[key]:
+            freq = occ[key]
+            best = np.array(key, np.float32)
+    return best, freq, occ
 
 
 @dataclass
@@ -82,16 +173,34 @@ class FaceInfoPerKeyframe:
 
 @dataclass
 class VertexInfo:
+    """VertexInfo (visibility_tester.h:75-126)."""
     visible_keyframes: list = field(default_factory=list)
     mean_color: np.ndarray | None = None
-    mean_distance: float = -1.0
-    mean_viewing_angle: float = -1.0
+    median_color: np.ndarray | None = None
     min_viewing_angle_index: int = -1
     min_viewing_angle_id: int = -1
     min_viewing_angle_color: np.ndarray | None = None
+    mean_viewing_angle_color: np.ndarray | None = None    # weighted by 1 / viewing angle
+    median_viewing_angle_color: np.ndarray | None = None  # weighted by 1 / viewing angle
     min_distance_index: int = -1
     min_distance_id: int = -1
     min_distance_color: np.ndarray | None = None
+    mean_distance_color: np.ndarray | None = None    # weighted by 1 / distance
+    median_distance_color: np.ndarray | None = None  # weighted by 1 / distance
+    min_intensity: float = float(np.finfo(np.float32).max)
+    median_intensity: float = float(np.finfo(np.float32).max)
+    median_intensity_color: np.ndarray | None = None
+    min_intensity_color: np.ndarray | None = None
+    mean_viewing_angle: float = -1.0
+    median_viewing_angle: float = -1.0
+    mean_distance: float = -1.0
+    median_distance: float = -1.0
+    mode: np.ndarray | None = None
+    mode_frequency: int = -1
+    mode_viewing_angle_color: np.ndarray | None = None
+    mode_frequency_viewing_angle_color: float = -1.0
+    occurrence: dict = field(default_factory=dict)
+    occurrence_viewing_angle: dict = field(default_factory=dict)
 
     def VisibleFrom(self, kf_id: int) -> int:  # visibility_tester.cc:178-194
         for i, v in enumerate(self.visible_keyframes):
@@ -99,23 +208,50 @@ class VertexInfo:
                 return i
         return -1
 
-    def CalcStat(self):  # the mean / min parts of :68-176
-        if not self.visible_keyframes:
+    def CalcStat(self):  # visibility_tester.cc:68-176
+        kfs = self.visible_keyframes
+        if not kfs:
             return
-        cols = np.array([v.color for v in self.visible_keyframes], np.float32)
-        self.mean_color = cols.sum(0, dtype=np.float32) / F32(len(cols))
-        self.mean_distance = float(sum(v.distance for v in self.visible_keyframes)
-                                   / len(self.visible_keyframes))
-        self.mean_viewing_angle = float(sum(v.viewing_angle for v in self.visible_keyframes)
-                                        / len(self.visible_keyframes))
-        va = [v.viewing_angle for v in self.visible_keyframes]
-        di = [v.distance for v in self.visible_keyframes]
-        self.min_viewing_angle_index = int(np.argmin(va))
-        self.min_viewing_angle_id = self.visible_keyframes[self.min_viewing_angle_index].kf_id
-        self.min_viewing_angle_color = self.visible_keyframes[self.min_viewing_angle_index].color
-        self.min_distance_index = int(np.argmin(di))
-        self.min_distance_id = self.visible_keyframes[self.min_distance_index].kf_id
-        self.min_distance_color = self.visible_keyframes[self.min_distance_index].color
+        n = F32(len(kfs))
+        mc = np.zeros(3, np.float32)
+        md, mva = F32(0.0), F32(0.0)
+        for kf in kfs:  # float sums in visit order
+            mc = (mc + np.asarray(kf.color, np.float32)).astype(np.float32)
+            md = F32(md + F32(kf.distance))
+            mva = F32(mva + F32(kf.viewing_angle))
+        self.mean_color = (mc / n).astype(np.float32)
+        self.mean_distance = float(F32(md / n))
+        self.mean_viewing_angle = float(F32(mva / n))
+        colors = [np.asarray(kf.color, np.float32) for kf in kfs]
+        dist = [F32(kf.distance) for kf in kfs]
+        va = [F32(kf.viewing_angle) for kf in kfs]
+        inten = [F32(kf.intensity) for kf in kfs]
+        with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+            inv_d = [F32(F32(1.0) / d) for d in dist]
+            inv_va = [F32(F32(1.0) / a) for a in va]
+            i = first_min(va)
+            self.min_viewing_angle_index, self.min_viewing_angle_id = i, kfs[i].kf_id
+            self.min_viewing_angle_color = kfs[i].color
+            i = first_min(dist)
+            self.min_distance_index, self.min_distance_id = i, kfs[i].kf_id
+            self.min_distance_color = kfs[i].color
+            self.median_viewing_angle = float(median(va))
+            self.median_distance = float(median(dist))
+            self.median_color = median_color(colors)
+            self.mean_viewing_angle_color = weighted_average(colors, inv_va)
+            self.mean_distance_color = weighted_average(colors, inv_d)
+            self.median_viewing_angle_color = weighted_median(colors, inv_va)
+            self.median_distance_color = weighted_median(colors, inv_d)
+            i = first_min(inten)
+            self.min_intensity, self.min_intensity_color = float(inten[i]), colors[i]
+            mi = median(inten, True)
+            self.median_intensity = float(mi)
+            j = next((k for k, v in enumerate(inten) if v == mi), len(inten))  # std::find
+            self.median_intensity_color = colors[j] if j < len(colors) else None
+            self.mode, self.mode_frequency, self.occurrence = mode(colors)
+            (self.mode_viewing_angle_color, f,
+             self.occurrence_viewing_angle) = mode(colors, inv_va)
+            self.mode_frequency_viewing_angle_color = float(f)
 
 
 @dataclass
@@ -131,14 +267,14 @@ class FaceInfo:
     def CalcStat(self):  # visibility_tester.cc:202-224
         if not self.visible_keyframes:
             return
-        a = [f.area for f in self.visible_keyframes]
-        va = [f.viewing_angle for f in self.visible_keyframes]
-        di = [f.distance for f in self.visible_keyframes]
-        self.max_area_index = int(np.argmax(a))
+        a = [F32(f.area) for f in self.visible_keyframes]
+        va = [F32(f.viewing_angle) for f in self.visible_keyframes]
+        di = [F32(f.distance) for f in self.visible_keyframes]
+        self.max_area_index = first_min([-x for x in a])  # std::max_element: first maximum
         self.max_area_id = self.visible_keyframes[self.max_area_index].kf_id
-        self.min_viewing_angle_index = int(np.argmin(va))
+        self.min_viewing_angle_index = first_min(va)
         self.min_viewing_angle_id = self.visible_keyframes[self.min_viewing_angle_index].kf_id
-        self.min_distance_index = int(np.argmin(di))
+        self.min_distance_index = first_min(di)
         self.min_distance_id = self.visible_keyframes[self.min_distance_index].kf_id
 
 
