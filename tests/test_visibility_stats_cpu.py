@@ -101,6 +101,20 @@ def test_vertex_calc_stat():
     assert np.allclose(v.mean_distance_color, ref, rtol=1e-4)
 
 
+def test_vertex_calc_stat_float_overflow_is_silent():
+    """The tester's no-hit quirk reports FLT_MAX distances: their float sum
+    is inf, as in C++, and no warning is raised."""
+    import warnings
+    big = float(np.finfo(np.float32).max)
+    v = vis.VertexInfo(visible_keyframes=[_kf(1, [1, 2, 3], 10, 0.5, big),
+                                          _kf(2, [4, 5, 6], 20, 0.0, big)])
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        v.CalcStat()
+    assert v.mean_distance == float("inf")
+    assert v.min_viewing_angle_index == 1
+
+
 def test_face_calc_stat_first_max_area():
     f = vis.FaceInfo(visible_keyframes=[
         vis.FaceInfoPerKeyframe(1, 0, 4.0, 0.5, 2.0, np.zeros((3, 2), np.float32)),

@@ -213,20 +213,22 @@ class VertexInfo:
         if not kfs:
             return
         n = F32(len(kfs))
-        mc = np.zeros(3, np.float32)
-        md, mva = F32(0.0), F32(0.0)
-        for kf in kfs:  # float sums in visit order
-            mc = (mc + np.asarray(kf.color, np.float32)).astype(np.float32)
-            md = F32(md + F32(kf.distance))
-            mva = F32(mva + F32(kf.viewing_angle))
-        self.mean_color = (mc / n).astype(np.float32)
-        self.mean_distance = float(F32(md / n))
-        self.mean_viewing_angle = float(F32(mva / n))
         colors = [np.asarray(kf.color, np.float32) for kf in kfs]
         dist = [F32(kf.distance) for kf in kfs]
         va = [F32(kf.viewing_angle) for kf in kfs]
         inten = [F32(kf.intensity) for kf in kfs]
+        # float arithmetic as in C++: FLT_MAX distances sum to inf, 1 / 0 is
+        # inf, and so on, without warnings
         with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+            mc = np.zeros(3, np.float32)
+            md, mva = F32(0.0), F32(0.0)
+            for kf in kfs:  # float sums in visit order
+                mc = (mc + np.asarray(kf.color, np.float32)).astype(np.float32)
+                md = F32(md + F32(kf.distance))
+                mva = F32(mva + F32(kf.viewing_angle))
+            self.mean_color = (mc / n).astype(np.float32)
+            self.mean_distance = float(F32(md / n))
+            self.mean_viewing_angle = float(F32(mva / n))
             inv_d = [F32(F32(1.0) / d) for d in dist]
             inv_va = [F32(F32(1.0) / a) for a in va]
             i = first_min(va)
