@@ -234,6 +234,13 @@ typedef struct {
   float* intensity;
 } ugu_gpu_visibility_out;
 
+/* TextureMappingOption (include/ugu/texturing/texture_mapper.h:22-30)
+ * fields of the kSimpleProjection / kUseOriginalMeshUv path. */
+typedef struct {
+  int32_t tex_w, tex_h;     /* texture size (1024 x 1024) */
+  int32_t padding_kernel;   /* PaddingSimple's window (3) */
+} ugu_gpu_texture_option;
+
 /* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
 typedef struct {
   int32_t path;             /* UGU_GPU_PATH_TILED (default) or UGU_GPU_PATH_GLOBAL */
@@ -258,6 +265,23 @@ typedef struct {
   double tile_kernel_ms;        /* summed device time of timed tile-kernel launches */
   uint64_t tile_kernel_launches; /* launches timed (UGU_GPU_TIME_KERNELS renders) */
 } ugu_gpu_stats;
+
+/* --- texture mapping ---------------------------------------------------- */
+/* TextureMapping (src/texturing/texture_mapper.cc:1009-1017) with
+ * kSimpleProjection and kUseOriginalMeshUv (:294-345): a tex_h x tex_w RGB8
+ * texture and its mask (255 where written) on the uv of mesh slot `mesh`.
+ * face_kf[f] is the id of face f's best keyframe, chosen on the host from
+ * the VisibilityInfo (:924-970), -1 for none; like the reference, the id
+ * indexes `keyframes` (only their camera width/height and colour are read).
+ * face_tri[6 f] is the face's projected triangle in that keyframe.  Faces
+ * are drawn in order (a later face overwrites an earlier one) and then
+ * padded (PaddingSimple, :148-201).  With UGU_GPU_DEVICE_POINTERS the
+ * images, face arrays and outputs are device pointers; otherwise host. */
+UGU_GPU_API int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
+                                        const ugu_gpu_keyframe* keyframes,
+                                        const int32_t* face_kf, const float* face_tri,
+                                        const ugu_gpu_texture_option* option,
+                                        uint8_t* texture, uint8_t* mask, uint32_t flags);
 
 /* --- context ------------------------------------------------------------ */
 UGU_GPU_API int ugu_gpu_create(int32_t device, ugu_gpu_context** out);

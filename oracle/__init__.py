@@ -4,5 +4,6 @@ Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this package.  See raster_oracle.c for the reference lines each part restates.
 """
 from .oracle import (  # noqa: F401
-    build, load, render, raytrace, visualize, gbuffer, test_visibility, ray_w, interp_f64, backward_f64, calc_normals, Stats,
+    build, load, render, raytrace, visualize, gbuffer, test_visibility, texture_mapping, ray_w,
+    interp_f64, backward_f64, calc_normals, Stats,
 )

@@ -115,6 +115,9 @@ def load():
         lib.oracle_visualize.argtypes = [C.c_int32, C.c_int32, P, P, P, P, P, P, P, C.c_float,
                                          C.c_float, C.c_int32]
         lib.oracle_visualize.restype = None
+        lib.oracle_texture_mapping.argtypes = [C.c_int32, P, P, C.c_int32, P, P, P, P, P,
+                                               C.c_int32, C.c_int32, C.c_int32, P, P]
+        lib.oracle_texture_mapping.restype = C.c_int
         lib.oracle_gbuffer.argtypes = [P] * 11
         lib.oracle_gbuffer.restype = C.c_int64
         lib.oracle_test_visibility.argtypes = [P, C.c_int32, P, C.c_int32, P, C.c_int32, P, P,
@@ -292,6 +295,30 @@ def visualize(depth=None, normal=None, face_id=None, min_d=200.0, max_d=1500.0,
                          _ptr(out.get("vis_face_id")), float(min_d), float(max_d),
                          1 if gl_coord else 0)
     return out
+
+
+def texture_mapping(uv, uv_indices, kf_colors, face_kf, face_tri, tex_w=1024, tex_h=1024,
+                    padding_kernel=3):
+    """TextureMapping's texture on the mesh's own uv (kUseOriginalMeshUv):
+    face_kf[f] the id of face f's keyframe (-1: none; ids index kf_colors),
+    face_tri[f] its projected triangle (3 x 2) in that keyframe.  Returns
+    (status, texture H x W x 3 uint8, mask H x W uint8)."""
+    lib = load()
+    uv = np.ascontiguousarray(uv, np.float32)
+    uvi = np.ascontiguousarray(uv_indices, np.int32)
+    fk = np.ascontiguousarray(face_kf, np.int32)
+    ft = np.ascontiguousarray(face_tri, np.float32)
+    cols = [np.ascontiguousarray(c, np.uint8) for c in kf_colors]
+    kw = np.array([c.shape[1] for c in cols], np.int32)
+    kh = np.array([c.shape[0] for c in cols], np.int32)
+    ptrs = (C.c_void_p * max(1, len(cols)))(*[c.ctypes.data for c in cols])
+    tex = np.zeros((tex_h, tex_w, 3), np.uint8)
+    mask = np.zeros((tex_h, tex_w), np.uint8)
+    rc = lib.oracle_texture_mapping(len(fk), uv.ctypes.data, uvi.ctypes.data, len(cols),
+                                    kw.ctypes.data, kh.ctypes.data, C.addressof(ptrs),
+                                    fk.ctypes.data, ft.ctypes.data, tex_w, tex_h,
+                                    padding_kernel, tex.ctypes.data, mask.ctypes.data)
+    return rc, tex, mask
 
 
 GBUFFER = ("pos_wld", "pos_cam", "normal_wld", "normal_cam", "bary", "uv")

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdint>
 #include <random>
+#include <vector>
 
 namespace {
 
@@ -65,4 +66,116 @@ extern "C" void oracle_visualize(int32_t width, int32_t height, const float* dep
       vis_face_id[3 * i + 2] = c[2];
     }
   }
+}
+
+/* TextureMapping with kSimpleProjection and kUseOriginalMeshUv
+ * (src/texturing/texture_mapper.cc:924-1006 and :294-345): faces in order,
+ * each one's uv triangle rasterized into a tex_w x tex_h texture
+ * (RasterizeTriangle, :234-292) with texels sampled from its keyframe's
+ * colour image at the same barycentric point of the face's projected
+ * triangle (BilinearInterpolation, include/ugu/util/image_util.h:156-192);
+ * a later face overwrites an earlier one.  Then PaddingSimple (:148-201).
+ * face_kf[f] is the id of the face's best keyframe (-1: none); like the
+ * reference, the id indexes the keyframe list.  Returns 0, or -1 when an id
+ * is outside the list.  Pixel reads outside an image's allocation are
+ * clamped to it. */
+namespace {
+
+constexpr float FLT_MIN_ = 1.17549435e-38f;  // std::numeric_limits<float>::min()
+
+float edge(float ax, float ay, float bx, float by, float cx, float cy) {
+  return (cx - ax) * (by - ay) - (cy - ay) * (bx - ax);
+}
+
+uint8_t f2u8(float v) { return (uint8_t)(uint32_t)trunc_i32((double)v); }
+
+void bilinear3(float x, float y, const uint8_t* img, int32_t cols, int32_t rows, uint8_t out[3]) {
+  int32_t x0 = trunc_i32((double)std::floor(x)), y0 = trunc_i32((double)std::floor(y));
+  int32_t x1 = x0 + 1, y1 = y0 + 1;
+  if (x0 < 0) x0 = 0;
+  if (y0 < 0) y0 = 0;
+  if (cols <= x1) x1 = cols - 1;
+  if (rows <= y1) y1 = rows - 1;
+  const float lu = x - (float)x0, lv = y - (float)y0;
+  const int64_t n = (int64_t)cols * rows;
+  auto px = [&](int32_t yy, int32_t xx) {
+    int64_t i = (int64_t)yy * cols + xx;
+    i = i < 0 ? 0 : (i >= n ? n - 1 : i);
+    return img + 3 * i;
+  };
+  const uint8_t *a = px(y0, x0), *b = px(y0, x1), *c = px(y1, x0), *d = px(y1, x1);
+  for (int k = 0; k < 3; ++k) {
+    const float v = (1.0f - lu) * (1.0f - lv) * (float)a[k] + lu * (1.0f - lv) * (float)b[k] +
+                    (1.0f - lu) * lv * (float)c[k] + lu * lv * (float)d[k];
+    out[k] = f2u8(v);
+  }
+}
+
+}  // namespace
+
+extern "C" int oracle_texture_mapping(int32_t num_faces, const float* uv, const int32_t* uv_idx,
+                                      int32_t num_kf, const int32_t* kf_w, const int32_t* kf_h,
+                                      const uint8_t* const* kf_color, const int32_t* face_kf,
+                                      const float* face_tri, int32_t tex_w, int32_t tex_h,
+                                      int32_t padding_kernel, uint8_t* texture, uint8_t* mask) {
+  const size_t n = (size_t)tex_w * tex_h;
+  std::fill(texture, texture + 3 * n, 0);
+  std::fill(mask, mask + n, 0);
+  for (int32_t f = 0; f < num_faces; ++f) {
+    const int32_t k = face_kf[f];
+    if (k < 0) continue;
+    if (k >= num_kf) return -1;
+    float tx[3], ty[3];
+    for (int j = 0; j < 3; ++j) {
+      const float* t = uv + 2 * (size_t)uv_idx[3 * (size_t)f + j];
+      tx[j] = t[0] * (float)tex_w - 0.5f;
+      ty[j] = (1.0f - t[1]) * (float)tex_h - 0.5f;
+    }
+    const float* s = face_tri + 6 * (size_t)f;
+    float area = edge(tx[0], ty[0], tx[1], ty[1], tx[2], ty[2]);
+    if (std::fabs(area) < FLT_MIN_) area = area > 0 ? FLT_MIN_ : -FLT_MIN_;
+    const float inv_area = 1.0f / area;
+    auto clampi = [](int32_t v, int32_t hi) { return std::max(0, std::min(v, hi)); };
+    const int32_t xmin = clampi(trunc_i32((double)(std::min({tx[0], tx[1], tx[2]}) - 1)), tex_w - 1);
+    const int32_t xmax = clampi(trunc_i32((double)(std::max({tx[0], tx[1], tx[2]}) + 1)), tex_w - 1);
+    const int32_t ymin = clampi(trunc_i32((double)(std::min({ty[0], ty[1], ty[2]}) - 1)), tex_h - 1);
+    const int32_t ymax = clampi(trunc_i32((double)(std::max({ty[0], ty[1], ty[2]}) + 1)), tex_h - 1);
+    for (int32_t y = ymin; y <= ymax; ++y)
+      for (int32_t x = xmin; x <= xmax; ++x) {
+        const float px = (float)x, py = (float)y;
+        float w0 = edge(tx[1], ty[1], tx[2], ty[2], px, py);
+        float w1 = edge(tx[2], ty[2], tx[0], ty[0], px, py);
+        float w2 = edge(tx[0], ty[0], tx[1], ty[1], px, py);
+        w0 *= inv_area;
+        w1 *= inv_area;
+        w2 *= inv_area;
+        if (w0 < 0 || w1 < 0 || w2 < 0) continue;
+        const float sx = w0 * s[0] + w1 * s[2] + w2 * s[4];
+        const float sy = w0 * s[1] + w1 * s[3] + w2 * s[5];
+        bilinear3(sx, sy, kf_color[k], kf_w[k], kf_h[k], texture + 3 * ((size_t)y * tex_w + x));
+        mask[(size_t)y * tex_w + x] = 255;
+      }
+  }
+  // PaddingSimple: each empty texel away from the border takes the float
+  // mean of the valid texels of its kernel window, read before any fill
+  std::vector<uint8_t> org_t(texture, texture + 3 * n), org_m(mask, mask + n);
+  const int32_t hk = padding_kernel / 2;
+  for (int32_t j = hk; j < tex_h - hk; ++j)
+    for (int32_t i = hk; i < tex_w - hk; ++i) {
+      if (org_m[(size_t)j * tex_w + i] == 255) continue;
+      float sum[3] = {0, 0, 0};
+      int cnt = 0;
+      for (int32_t jj = -hk; jj <= hk; ++jj)
+        for (int32_t ii = -hk; ii <= hk; ++ii) {
+          const size_t q = (size_t)(j + jj) * tex_w + (i + ii);
+          if (org_m[q] != 255) continue;
+          for (int c = 0; c < 3; ++c) sum[c] += (float)org_t[3 * q + c];
+          ++cnt;
+        }
+      if (!cnt) continue;
+      const size_t p = (size_t)j * tex_w + i;
+      mask[p] = 255;
+      for (int c = 0; c < 3; ++c) texture[3 * p + c] = f2u8(sum[c] / (float)cnt);
+    }
+  return 0;
 }

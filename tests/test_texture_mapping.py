@@ -1,0 +1,141 @@
+"""TextureMapping on the mesh's own uv (src/texturing/texture_mapper.cc:
+TextureMappingSimple :924-1006 with kUseOriginalMeshUv, RasterizeTriangle
+:234-292, PaddingSimple :148-201) through ugu_gpu_texture_mapping, against
+the oracle's restatement (oracle/vis_oracle.cc: oracle_texture_mapping):
+texture and mask bit for bit.  The face arrays are seeded: uv triangles that
+overlap heavily (a later face overwrites an earlier one), source triangles
+reaching outside their keyframe images, faces without a keyframe."""
+import numpy as np
+import pytest
+
+from ugu_gb300 import capi, scenes
+from ugu_gb300 import visibility as vis
+
+
+def overlapping_faces(n_faces=600, n_kf=3, seed=5):
+    rng = np.random.default_rng(seed)
+    # uv triangles of 2 to 40 texels packed into the middle of the texture
+    c = rng.uniform(0.3, 0.7, (n_faces, 1, 2))
+    uv = (c + rng.normal(0.0, 1.0, (n_faces, 3, 2)) * rng.uniform(0.002, 0.03, (n_faces, 1, 1)))
+    uv = uv.reshape(-1, 2).astype(np.float32)
+    uvi = np.arange(3 * n_faces, dtype=np.int32).reshape(-1, 3)
+    sizes = [(80, 60), (64, 64), (97, 41)][:n_kf]
+    imgs = [rng.integers(0, 256, (h, w, 3)).astype(np.uint8) for w, h in sizes]
+    face_kf = rng.integers(-1, n_kf, n_faces).astype(np.int32)
+    face_tri = np.zeros((n_faces, 3, 2), np.float32)
+    for f in range(n_faces):
+        w, h = sizes[max(face_kf[f], 0)]
+        face_tri[f] = rng.uniform([-4, -4], [w + 4, h + 4], (3, 2))
+    return uv, uvi, imgs, face_kf, face_tri
+
+
+def test_oracle_single_face_copies_and_pads(oracle_lib):
+    img = np.arange(8 * 8 * 3, dtype=np.uint8).reshape(8, 8, 3)
+    uv = np.array([[0.0, 1.0], [1.0, 1.0], [0.0, 0.0]], np.float32)
+    tri = np.array([[[-0.5, -0.5], [7.5, -0.5], [-0.5, 7.5]]], np.float32)
+    rc, tex, mask = oracle_lib.texture_mapping(uv, [[0, 1, 2]], [img], [0], tri, 8, 8, 3)
+    assert rc == 0
+    # the uv triangle maps texel (x, y) to source point (x, y): texels copied
+    assert np.array_equal(tex[0, 0], img[0, 0]) and np.array_equal(tex[2, 3], img[2, 3])
+    rc, tex0, mask0 = oracle_lib.texture_mapping(uv, [[0, 1, 2]], [img], [0], tri, 8, 8, 0)
+    # padded texels: inside the border, empty before, the truncated mean of
+    # the 3 x 3 window's valid texels after; the border is never padded
+    padded = np.argwhere((mask == 255) & (mask0 == 0))
+    assert len(padded) > 0 and mask[1, 7] == 0 and mask0[1, 7] == 0
+    y, x = padded[0]
+    win = mask0[y - 1:y + 2, x - 1:x + 2] == 255
+    mean = tex0[y - 1:y + 2, x - 1:x + 2][win].astype(np.float32).sum(0) / np.float32(win.sum())
+    assert np.array_equal(tex[y, x], mean.astype(np.uint8))
+    assert oracle_lib.texture_mapping(uv, [[0, 1, 2]], [img], [1], tri, 8, 8, 3)[0] == -1
+
+
+def _face_info(rows):
+    fi = vis.FaceInfo(visible_keyframes=[
+        vis.FaceInfoPerKeyframe(k, 0, a, va, d, np.full((3, 2), k, np.float32))
+        for k, a, va, d in rows])
+    fi.CalcStat()
+    return fi
+
+
+def test_best_keyframes_by_criteria():
+    info = vis.VisibilityInfo(0, 0)
+    info.face_info_list = [_face_info([(0, 4.0, 0.5, 2.0), (1, 9.0, 0.2, 3.0), (2, 1.0, 0.9, 1.0)]),
+                           vis.FaceInfo()]
+    for crit, want in ((vis.ViewSelectionCriteria.kMaxArea, 1),
+                       (vis.ViewSelectionCriteria.kMinViewingAngle, 1),
+                       (vis.ViewSelectionCriteria.kMinDistance, 2)):
+        fk, ft = vis.best_keyframes(info, crit)
+        assert list(fk) == [want, -1] and ft[0, 0, 0] == want
+    with pytest.raises(ValueError):
+        vis.best_keyframes(info, 3)
+
+
+def test_texture_mapping_uv_types_not_built_return_false():
+    m = scenes.icosphere_textured(1, 8)
+    opt = vis.TextureMappingOption()  # kGenerateSimpleTile, the reference's default
+    assert vis.TextureMapping([], vis.VisibilityInfo(m.num_vertices, m.num_faces), m, opt) is False
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("size,kernel", [((256, 192), 3), ((300, 130), 5), ((128, 128), 0)])
+def test_gpu_texture_mapping_matches_oracle(gpu_lib, oracle_lib, size, kernel):
+    from ugu_gb300.rasterizer import Context
+    uv, uvi, imgs, face_kf, face_tri = overlapping_faces()
+    tw, th = size
+    rc, want_t, want_m = oracle_lib.texture_mapping(uv, uvi, imgs, face_kf, face_tri, tw, th, kernel)
+    assert rc == 0
+    n = len(uvi)
+    m = scenes.Mesh(vertices=np.zeros((3 * n, 3), np.float32), vertex_indices=uvi.copy())
+    m.uv, m.uv_indices = uv, uvi
+    ctx = Context(0)
+    try:
+        ctx.check(ctx.set_mesh(0, m))
+        descs = []
+        for k, img in enumerate(imgs):
+            d = capi.KeyframeDesc()
+            d.id = k
+            d.camera = capi.camera_struct(scenes.camera_desc(img.shape[1], img.shape[0], 50.0,
+                                                             50.0, 20.0, 20.0))
+            d.color = img.ctypes.data
+            descs.append(d)
+        tex = np.zeros((th, tw, 3), np.uint8)
+        mask = np.zeros((th, tw), np.uint8)
+        ctx.check(ctx.texture_mapping(0, descs, face_kf, face_tri.reshape(-1, 6),
+                                      capi.TextureOption(tw, th, kernel), tex, mask))
+        assert np.array_equal(mask, want_m)
+        bad = np.argwhere((tex != want_t).any(-1))
+        assert len(bad) == 0, (len(bad), bad[:5])
+        assert (want_m == 255).mean() > 0.05
+        # an id past the keyframe list is an error, as an index past it is in C++
+        face_kf2 = face_kf.copy()
+        face_kf2[7] = len(imgs)
+        assert ctx.texture_mapping(0, descs, face_kf2, face_tri.reshape(-1, 6),
+                                   capi.TextureOption(tw, th, kernel), tex, mask) != 0
+    finally:
+        ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_texture_mapping_pipeline(gpu_lib, oracle_lib):
+    """VisibilityTester, then TextureMapping on the mesh's own uv: the
+    texture equals the oracle's for the same best keyframes."""
+    from test_visibility import keyframes, option
+    m = scenes.icosphere_textured(3, 64)
+    kfs = [(i, cam, im) for i, (_, cam, im) in enumerate(keyframes(oracle_lib, m, n=4))]
+    vt = vis.VisibilityTester(option())
+    vt.set_data(m.vertices, m.normals, m.vertex_indices)
+    assert vt.PrepareData()
+    info = vis.VisibilityInfo(m.num_vertices, m.num_faces)
+    frames = [vis.Keyframe(kid, cam, im["color"], im["depth"], im["mask"]) for kid, cam, im in kfs]
+    assert vt.Test(info, facewise=False, keyframes=frames)
+    opt = vis.TextureMappingOption(uv_type=vis.TexturingOutputUvType.kUseOriginalMeshUv,
+                                   tex_w=256, tex_h=256)
+    face_kf, face_tri = vis.best_keyframes(info, opt.criteria)
+    assert (face_kf >= 0).mean() > 0.3
+    rc, want_t, want_m = oracle_lib.texture_mapping(m.uv, m.uv_indices, [f.color for f in frames],
+                                                    face_kf, face_tri, 256, 256, 3)
+    assert rc == 0
+    assert vis.TextureMapping(frames, info, m, opt, ctx=vt._ctx, slot=1)
+    assert np.array_equal(m.texture_mask, want_m)
+    assert np.array_equal(m.textures[0], want_t)
+    assert list(np.unique(m.material_ids)) == [0]

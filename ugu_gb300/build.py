@@ -23,7 +23,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPI
            "-Xcompiler", "-fvisibility=hidden", "-I" + os.path.join(ROOT, "include")]
 
 SOURCES = ["capi.cu", "raster.cu", "tile.cu", "backward.cu", "noalloc.cu", "ray.cu", "bvh.cu",
-           "vis.cu"]
+           "vis.cu", "texmap.cu"]
 
 
 def _sources():

@@ -97,7 +97,7 @@ EXPORTS = [
     "ugu_gpu_set_tuning", "ugu_gpu_get_tuning", "ugu_gpu_autotune", "ugu_gpu_get_stats",
     "ugu_gpu_synchronize", "ugu_gpu_set_stream", "ugu_gpu_render_noalloc",
     "ugu_gpu_get_device_mesh", "ugu_gpu_visualize", "ugu_gpu_render_gbuffer",
-    "ugu_gpu_test_visibility",
+    "ugu_gpu_test_visibility", "ugu_gpu_texture_mapping",
 ]
 
 NOALLOC_MAX_PIXELS = 2097152
@@ -154,6 +154,8 @@ def load(path: str | None = None):
     lib.ugu_gpu_render_gbuffer.argtypes = [P, C.c_int32, P, C.c_uint32]
     lib.ugu_gpu_test_visibility.argtypes = [P, C.c_int32, P, C.c_int32, P, P, C.c_int32, P,
                                             C.c_uint32]
+    lib.ugu_gpu_texture_mapping.argtypes = [P, C.c_int32, C.c_int32, P, P, P, P, P, P,
+                                            C.c_uint32]
     for name in EXPORTS:
         if name != "ugu_gpu_last_error":
             getattr(lib, name).restype = C.c_int
@@ -197,6 +199,11 @@ class VisibilityOption(C.Structure):
                 ("max_viewing_angle", C.c_float),
                 ("max_distance_from_camera_to_vertex", C.c_float),
                 ("max_depth_difference", C.c_float), ("eps", C.c_float)]
+
+
+class TextureOption(C.Structure):
+    """ugu_gpu_texture_option (TextureMappingOption's texture size and padding)."""
+    _fields_ = [("tex_w", C.c_int32), ("tex_h", C.c_int32), ("padding_kernel", C.c_int32)]
 
 
 class VisibilityOut(C.Structure):

@@ -1302,6 +1302,117 @@ int ugu_gpu_plan_destroy(ugu_gpu_plan* plan) {
   return UGU_GPU_OK;
 }
 
+// TextureMapping with kUseOriginalMeshUv (texture_mapper.cc:924-1006,
+// :294-345); texmap.cu draws the texture.
+int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
+                            const ugu_gpu_keyframe* keyframes, const int32_t* face_kf,
+                            const float* face_tri, const ugu_gpu_texture_option* option,
+                            uint8_t* texture, uint8_t* mask, uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  cudaSetDevice(ctx->device);
+  if (n < 0 || (n > 0 && !keyframes) || !face_kf || !face_tri || !option || !texture || !mask)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad keyframes, face arrays, option or output");
+  if (option->tex_w <= 0 || option->tex_h <= 0 || option->padding_kernel < 0)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad texture size or padding kernel");
+  if (mesh < 0 || mesh >= kMaxMeshes || !ctx->meshes[mesh].present)
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh has not been initialized");
+  MeshSlot& ms = ctx->meshes[mesh];
+  const int F = ms.dev.num_faces;
+  if (!ms.dev.uv || !ms.dev.uvidx)  // :986-993
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                     "OutputUvType kUseOriginalMeshUv is specified but UV on mesh is invalid");
+  const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
+  for (int k = 0; k < n; ++k)
+    if (!keyframes[k].color || keyframes[k].camera.width <= 0 || keyframes[k].camera.height <= 0)
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "keyframe color is empty");
+  if (!dev)  // the reference indexes the keyframe list by id: an id past it is an error here
+    for (int f = 0; f < F; ++f)
+      if (face_kf[f] >= n)
+        return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                         "face %d: keyframe id %d is not an index of the %d keyframes", f,
+                         face_kf[f], n);
+  const size_t texels = (size_t)option->tex_w * option->tex_h;
+  size_t img_bytes = 0;
+  if (!dev)
+    for (int k = 0; k < n; ++k)
+      img_bytes += align256(3 * (size_t)keyframes[k].camera.width * keyframes[k].camera.height);
+  const size_t total = align256(sizeof(DevKeyframe) * (size_t)std::max(n, 1)) + img_bytes +
+                       (dev ? 0 : align256(4 * (size_t)F) + align256(24 * (size_t)F)) +
+                       align256(4 * texels) + align256(3 * texels) + align256(texels) +
+                       (dev ? 0 : align256(3 * texels) + align256(texels));
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (total > ctx->vis_cap) {
+    cudaFree(ctx->vis_buf);
+    ctx->vis_buf = nullptr;
+    ctx->vis_cap = 0;
+    CK(ctx, cudaMalloc(&ctx->vis_buf, total), "cudaMalloc(texture mapping buffers)");
+    ctx->vis_cap = total;
+  }
+  uint8_t* q = ctx->vis_buf;
+  auto take = [&](size_t bytes) {
+    uint8_t* r = q;
+    q += align256(bytes);
+    return r;
+  };
+  DevKeyframe* d_kfs = reinterpret_cast<DevKeyframe*>(take(sizeof(DevKeyframe) * std::max(n, 1)));
+  std::vector<DevKeyframe> hk((size_t)std::max(n, 1));
+  for (int k = 0; k < n; ++k) {
+    DevKeyframe& d = hk[k];
+    std::memset(&d, 0, sizeof(d));
+    fill_cam(d.cam, keyframes[k].camera);
+    d.id = keyframes[k].id;
+    if (dev) {
+      d.color = keyframes[k].color;
+      continue;
+    }
+    const size_t px = (size_t)keyframes[k].camera.width * keyframes[k].camera.height;
+    uint8_t* c = take(3 * px);
+    CK(ctx, cudaMemcpyAsync(c, keyframes[k].color, 3 * px, cudaMemcpyHostToDevice, ctx->stream),
+       "cudaMemcpyAsync(keyframe color)");
+    d.color = c;
+  }
+  CK(ctx, cudaMemcpyAsync(d_kfs, hk.data(), sizeof(DevKeyframe) * hk.size(),
+                          cudaMemcpyHostToDevice, ctx->stream),
+     "cudaMemcpyAsync(keyframes)");
+  TexMapParams p{};
+  p.uv = ms.dev.uv;
+  p.uvidx = ms.dev.uvidx;
+  p.num_faces = F;
+  p.kf = d_kfs;
+  p.tex_w = option->tex_w;
+  p.tex_h = option->tex_h;
+  p.hk = option->padding_kernel / 2;
+  if (dev) {
+    p.face_kf = face_kf;
+    p.face_tri = face_tri;
+  } else {
+    int32_t* fk = reinterpret_cast<int32_t*>(take(4 * (size_t)F));
+    float* ft = reinterpret_cast<float*>(take(24 * (size_t)F));
+    CK(ctx, cudaMemcpyAsync(fk, face_kf, 4 * (size_t)F, cudaMemcpyHostToDevice, ctx->stream),
+       "cudaMemcpyAsync(face keyframes)");
+    CK(ctx, cudaMemcpyAsync(ft, face_tri, 24 * (size_t)F, cudaMemcpyHostToDevice, ctx->stream),
+       "cudaMemcpyAsync(face triangles)");
+    p.face_kf = fk;
+    p.face_tri = ft;
+  }
+  p.owner = reinterpret_cast<int32_t*>(take(4 * texels));
+  p.tex0 = take(3 * texels);
+  p.mask0 = take(texels);
+  p.tex = dev ? texture : take(3 * texels);
+  p.mask = dev ? mask : take(texels);
+  launch_texture_mapping(p, ctx->stream);
+  CK(ctx, cudaGetLastError(), "texture mapping launch");
+  ctx->launches += F > 0 ? 3 : 2;
+  if (!dev) {
+    CK(ctx, cudaMemcpyAsync(texture, p.tex, 3 * texels, cudaMemcpyDeviceToHost, ctx->stream),
+       "cudaMemcpyAsync(texture)");
+    CK(ctx, cudaMemcpyAsync(mask, p.mask, texels, cudaMemcpyDeviceToHost, ctx->stream),
+       "cudaMemcpyAsync(texture mask)");
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "texture mapping");
+  return UGU_GPU_OK;
+}
+
 int ugu_gpu_synchronize(ugu_gpu_context* ctx) {
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");

@@ -218,6 +218,21 @@ struct VisParams {
 };
 void launch_visibility(const VisParams& p, cudaStream_t s);
 
+// TextureMapping on the mesh's own uv (texmap.cu).
+struct TexMapParams {
+  const float2* uv;
+  const int4* uvidx;
+  int num_faces;
+  const int32_t* face_kf;   // per face: its keyframe (an index of kf), or -1
+  const float* face_tri;    // per face: projected triangle in that keyframe, 6 floats
+  const DevKeyframe* kf;    // colour images (cam.width x cam.height RGB8)
+  int tex_w, tex_h, hk;     // texture size; half the padding kernel
+  int32_t* owner;           // per texel: the last face covering it, or -1
+  uint8_t *tex0, *mask0;    // before padding
+  uint8_t *tex, *mask;      // results
+};
+void launch_texture_mapping(const TexMapParams& p, cudaStream_t s);
+
 // Raytracer (ray.cu): the views of one group, one thread per pixel.
 struct RayParams {
   const DevMesh* meshes;

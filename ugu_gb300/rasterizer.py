@@ -196,6 +196,16 @@ class Context:
         arr = (capi.Vis * len(items))(*items)
         return self.lib.ugu_gpu_visualize(self.h, len(items), C.addressof(arr), int(flags))
 
+    def texture_mapping(self, slot: int, kf_descs, face_kf, face_tri, option,
+                        texture: np.ndarray, mask: np.ndarray) -> int:
+        """ugu_gpu_texture_mapping with host buffers."""
+        arr = (capi.KeyframeDesc * max(1, len(kf_descs)))(*kf_descs)
+        fk = np.ascontiguousarray(face_kf, np.int32)
+        ft = np.ascontiguousarray(face_tri, np.float32)
+        return self.lib.ugu_gpu_texture_mapping(self.h, int(slot), len(kf_descs), C.addressof(arr),
+                                                fk.ctypes.data, ft.ctypes.data, C.byref(option),
+                                                texture.ctypes.data, mask.ctypes.data, 0)
+
     def stats(self) -> capi.Stats:
         s = capi.Stats()
         self.check(self.lib.ugu_gpu_get_stats(self.h, C.byref(s)))

@@ -432,3 +432,90 @@ class VisibilityTester:
         info.face_info_list[f].visible_keyframes.append(
             FaceInfoPerKeyframe(int(kf_id), int(f), _area(tri), float(va / F32(3)),
                                 float(di / F32(3)), tri))
+
+
+# --- TextureMapping (include/ugu/texturing/texture_mapper.h,
+#     src/texturing/texture_mapper.cc) --------------------------------------
+
+class ViewSelectionCriteria:  # visibility_tester.h:23-37
+    kMinViewingAngle = 0
+    kMinDistance = 1
+    kMaxArea = 6
+
+
+class TexturingOutputUvType:  # texture_mapper.h:14-19
+    kGenerateSimpleTile = 0
+    kUseOriginalMeshUv = 1
+    kGenerateSimpleTriangles = 2
+    kGenerateSimpleCharts = 3
+
+
+@dataclass
+class TextureMappingOption:
+    """TextureMappingOption (texture_mapper.h:22-30), same defaults."""
+    criteria: int = ViewSelectionCriteria.kMaxArea
+    type: int = 0  # TextureMappingType::kSimpleProjection
+    uv_type: int = TexturingOutputUvType.kGenerateSimpleTile
+    texture_base_name: str = "ugutex"
+    tex_w: int = 1024
+    tex_h: int = 1024
+    padding_kernel: int = 3
+
+
+def best_keyframes(info: VisibilityInfo, criteria: int):
+    """Each face's best keyframe (texture_mapper.cc:938-970): the
+    FaceInfoPerKeyframe at FaceInfo's min-viewing-angle, min-distance or
+    max-area index.  Returns (kf id per face, -1 for faces seen by none;
+    projected triangle per face, F x 3 x 2)."""
+    pick = {ViewSelectionCriteria.kMinViewingAngle: "min_viewing_angle_index",
+            ViewSelectionCriteria.kMinDistance: "min_distance_index",
+            ViewSelectionCriteria.kMaxArea: "max_area_index"}.get(criteria)
+    if pick is None:
+        raise ValueError(f"ViewSelectionCriteria {criteria} is not implemented")
+    F = len(info.face_info_list)
+    face_kf = np.full(F, -1, np.int32)
+    face_tri = np.zeros((F, 3, 2), np.float32)
+    for f, fi in enumerate(info.face_info_list):
+        if not fi.visible_keyframes:
+            continue
+        best = fi.visible_keyframes[getattr(fi, pick)]
+        face_kf[f] = best.kf_id
+        face_tri[f] = np.asarray(best.projected_tri, np.float32)
+    return face_kf, face_tri
+
+
+def TextureMapping(keyframes, info: VisibilityInfo, mesh, option: TextureMappingOption,
+                   ctx: Context | None = None, slot: int = 0) -> bool:
+    """TextureMapping (texture_mapper.cc:1009-1017) with kSimpleProjection and
+    kUseOriginalMeshUv, drawn on the GPU (ugu_gpu_texture_mapping): sets the
+    mesh's one material to the texture and every face's material id to 0,
+    as GenerateTextureOnOriginalUv (:336-343) does; the texture's mask (255
+    where a face or the padding wrote) is left in mesh.texture_mask.  The
+    atlas-generating uv types are not built (False, like an unimplemented
+    type)."""
+    if option.type != 0 or option.uv_type != TexturingOutputUvType.kUseOriginalMeshUv:
+        return False
+    if (mesh.uv is None or len(mesh.uv) == 0 or mesh.uv_indices is None
+            or len(mesh.uv_indices) != len(mesh.vertex_indices)):
+        return False  # :986-993
+    face_kf, face_tri = best_keyframes(info, option.criteria)
+    ctx = ctx or Context(0)
+    ctx.check(ctx.set_mesh(slot, mesh))
+    descs, keep = [], []
+    for kf in keyframes:
+        d = capi.KeyframeDesc()
+        d.id = int(kf.id)
+        d.camera = capi.camera_struct(kf.camera)
+        c = np.ascontiguousarray(kf.color, np.uint8)
+        keep.append(c)
+        d.color = c.ctypes.data
+        descs.append(d)
+    tex = np.zeros((option.tex_h, option.tex_w, 3), np.uint8)
+    mask = np.zeros((option.tex_h, option.tex_w), np.uint8)
+    opt = capi.TextureOption(int(option.tex_w), int(option.tex_h), int(option.padding_kernel))
+    ctx.check(ctx.texture_mapping(slot, descs, face_kf, face_tri.reshape(-1, 6), opt, tex, mask))
+    mesh.textures = [tex]
+    mesh.textures_f32 = [None]
+    mesh.material_ids = np.zeros(len(mesh.vertex_indices), np.int32)
+    mesh.texture_mask = mask
+    return True
