@@ -14,7 +14,8 @@
 //            the front, faces drawn last from the back.
 //   k_tile   persistent blocks pull (view, tile) items from a work queue.
 //            For one tile, each warp on its own: take the next 32 listed
-//            faces, set them up in the warp's slots of shared memory with
+//            faces (a quarter of a small draw class), set them up in the
+//            warp's slots of shared memory with
 //            their candidate pixels (the box-in-tile, or conservative row
 //            spans for small faces, span.cuh), split them into (face, pixel)
 //            pairs with a warp prefix scan of their candidate counts, test
