@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--views", type=int, default=N_VIEWS)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-backward", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the bit-for-bit check of the timed replay against the oracle")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the single-view and texture-descent configurations")
     ap.add_argument("--workload", default="ring64",
                     choices=["ring64", "uvsphere", "single1080", "texdescent256", "raytrace64"],
                     help="ring64 (default): the batched-forward workload; the others "
@@ -75,15 +79,22 @@ class ClockSampler:
         self.proc = None
 
     def start(self):
+        """Starts sampling every 20 ms and returns once the first sample is in
+        (at most 3 s), so that the timed region that follows is covered."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.rows and time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            time.sleep(0.005)
+        self.first = len(self.rows)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -98,11 +109,14 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.t.join(timeout=2)
-        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        # the rows taken while the timed region ran (the first one, taken
+        # before it started, only when nothing later came in)
+        rows = self.rows[getattr(self, "first", 0):] or self.rows
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
-        for r in self.rows:
+        for r in rows:
             if len(r) >= 9:
                 for n, v in zip(names, r[5:9]):
                     if v.lower().startswith("active"):
@@ -138,18 +152,41 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """Per-launch DRAM bytes of the tile kernel from an ncu capture, as
-    summarised in profiles/k_tile_traffic.txt (null when absent)."""
+# The sources the tile kernel is compiled from: a committed ncu figure is
+# used only while their content hash equals the one it was measured on.
+TILE_SOURCES = ("tile.cu", "shade.cuh", "span.cuh", "exact.cuh", "internal.cuh")
+
+
+def tile_source_hash():
+    import hashlib
+    h = hashlib.sha256()
+    for name in TILE_SOURCES:
+        with open(os.path.join(ROOT, "ugu_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def committed_tile_profile():
+    """Per-launch DRAM bytes and warp instructions of the tile kernel on the
+    64-view workload, from the ncu capture summarised in
+    profiles/k_tile_traffic.txt, and whether that capture measured the
+    current sources (a stale figure is reported as null)."""
     p = os.path.join(ROOT, "profiles", "k_tile_traffic.txt")
+    vals = {}
     try:
         with open(p) as f:
             for line in f:
-                if line.strip().startswith("k_tile_dram_bytes_per_launch:"):
-                    return int(line.split(":", 1)[1])
+                k, sep, v = line.strip().partition(":")
+                if sep and k in ("k_tile_dram_bytes_per_launch", "k_tile_warp_instructions_per_launch",
+                                 "tile_sources_sha256_16"):
+                    vals[k] = v.strip()
     except Exception:
-        pass
-    return None
+        return None, None, "absent"
+    if vals.get("tile_sources_sha256_16") != tile_source_hash():
+        return None, None, "stale (tile kernel sources changed since the capture)"
+    tr = vals.get("k_tile_dram_bytes_per_launch")
+    ins = vals.get("k_tile_warp_instructions_per_launch")
+    return (int(tr) if tr else None), (int(ins) if ins else None), "current"
 
 
 def workload(n_views):
@@ -172,28 +209,67 @@ def algorithmic_bytes(m, cams):
     return px * BYTES_PER_PX + geometry + texture, px
 
 
-def cpu_oracle_views_per_s(m, cams, threads, max_views=None):
-    """Times the oracle port on `threads` host threads over the views."""
+def ring_config(m, cams):
+    """The workload's `config`, identical in both arms."""
+    return {"workload": "ring64_icosphere7_tex2048_bilinear", "views": len(cams),
+            "pixels": sum(c.width * c.height for c in cams), "mesh_faces": m.num_faces,
+            "mesh_vertices": m.num_vertices, "texture": "2048x2048 RGB8",
+            "outputs": "color,depth,normal,mask,face_id",
+            "l2": "outputs (1.30 GB) exceed L2; the GPU arm also flushes L2 (256 MB write) "
+                  "between timed steps"}
+
+
+OUT_KEYS = ("color", "depth", "normal", "mask", "face_id")
+
+
+def oracle_all_views(m, cams, threads, keep=False):
+    """Renders every view once with the oracle port on `threads` host
+    threads, largest views first; returns (seconds, outputs or None)."""
     import concurrent.futures as cf
 
     import oracle
     oracle.build()
     opt = option()
-    views = cams if max_views is None else cams[:max_views]
+    order = sorted(range(len(cams)), key=lambda i: -cams[i].width * cams[i].height)
+    res = [None] * len(cams)
 
-    def one(c):
-        rc, _, _ = oracle.render(m, c, opt)
+    def one(i):
+        rc, out, _ = oracle.render(m, cams[i], opt)
         assert rc == 0
-        return c.width * c.height
+        if keep:
+            res[i] = {k: out[k] for k in OUT_KEYS}
 
     t0 = time.perf_counter()
     if threads == 1:
-        px = sum(one(c) for c in views)
+        for i in order:
+            one(i)
     else:
         with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-            px = sum(ex.map(one, views))
-    dt = time.perf_counter() - t0
-    return len(views) / dt, px / dt / 1e9, dt, len(views)
+            list(ex.map(one, order))
+    return time.perf_counter() - t0, (res if keep else None)
+
+
+def view_digest(outs):
+    import hashlib
+    h = hashlib.blake2b(digest_size=16)
+    for k in OUT_KEYS:
+        h.update(outs[k].tobytes())
+    return h.hexdigest()
+
+
+def mismatched_pixels(ref, got):
+    """Pixels where any output differs from the oracle's bits."""
+    import numpy as np
+    bad = None
+    for k in OUT_KEYS:
+        a, b = ref[k], got[k]
+        if a.dtype.kind == "f":
+            a, b = a.view(np.uint32), b.view(np.uint32)
+        d = a != b
+        if d.ndim == 3:
+            d = d.any(axis=2)
+        bad = d if bad is None else (bad | d)
+    return int(bad.sum())
 
 
 def measure_fwd_bwd(ctx, torch, dev, stream, flush, timed, args, n_views=16, size=(640, 480)):
@@ -253,60 +329,42 @@ def measure_fwd_bwd(ctx, torch, dev, stream, flush, timed, args, n_views=16, siz
 
 
 def run_reference(args):
+    """The reference arm: the oracle restatement of Rasterizer::Render (the
+    reference's own build does not travel to the Arm machine), every one of the
+    workload's views rendered in each step, on all host threads, largest
+    views first."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     m, cams = workload(args.views)
     threads = os.cpu_count() or 1
-    import concurrent.futures as cf
-
-    import oracle
-    oracle.build()
-    opt = option()
-    # each step renders a bounded sample of the 64 views (round robin)
-    per_step = max(threads, 8)
-    order = sorted(range(len(cams)), key=lambda i: i)
-
-    def one(i):
-        rc, _, _ = oracle.render(m, cams[i], opt)
-        assert rc == 0
-        return cams[i].width * cams[i].height
-
-    pos = 0
-    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        for _ in range(args.warmup):
-            list(ex.map(one, [order[(pos + k) % len(order)] for k in range(2)]))
-        times, views, pix = [], 0, 0
-        for _ in range(args.steps):
-            sel = [order[(pos + k) % len(order)] for k in range(per_step)]
-            pos += per_step
-            t0 = time.perf_counter()
-            pix += sum(ex.map(one, sel))
-            times.append(time.perf_counter() - t0)
-            views += len(sel)
+    for _ in range(args.warmup):
+        oracle_all_views(m, cams, threads)
+    times = [oracle_all_views(m, cams, threads)[0] for _ in range(args.steps)]
     total = sum(times)
-    v = views / total
+    v = len(cams) * args.steps / total
+    px = sum(c.width * c.height for c in cams)
     line = {
         "impl": "reference", "metric": "views/s", "value": v, "unit": "views/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "ring64_icosphere7_tex2048_bilinear", "views": len(cams),
-                   "pixels": sum(c.width * c.height for c in cams)},
-        "gpix_per_s": pix / total / 1e9,
+        "config": ring_config(m, cams),
+        "gpix_per_s": px * args.steps / total / 1e9,
         "cpu_baseline": {"value": v, "unit": "views/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} of the 64 views per step, round robin, "
-                                   f"{threads} host threads, oracle restatement of "
+                         "sample": f"all {len(cams)} views per step, largest first, on "
+                                   f"{threads} host threads; oracle restatement of "
                                    f"Rasterizer::Render (-O2 -ffp-contract=off)"},
         "e2e": {"value": v, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_single(args, which):
-    """One view per step through the C ABI (device outputs, graph replay):
-    the UV-sphere vertex-colour view at 640x480 or the textured icosphere-7
-    view at 1920x1080; the oracle on one host core beside it."""
+def measure_single(which, steps, warmup, cpu=True):
+    """One view per step through the C ABI with device outputs: the UV-sphere
+    vertex-colour view at 640x480 (uvsphere) or the textured icosphere-7 view
+    at 1920x1080 (single1080), as one graph replay per step and as one direct
+    render call per step; the oracle on one host core beside it."""
     import torch
 
     from ugu_gb300 import capi, scenes
@@ -337,34 +395,62 @@ def run_single(args, which):
     tuned = ctx.autotune([v])
     plan = ctx.plan_create([v], capi.DEVICE_POINTERS)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    for _ in range(max(3, args.warmup)):
-        ctx.check(plan.launch())
-    ctx.check(ctx.synchronize())
-    ev = []
-    for _ in range(args.steps):
-        flush.zero_()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        ctx.check(plan.launch())
-        b.record(stream)
-        ev.append((a, b))
-    ctx.check(ctx.synchronize())
-    ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
-    import oracle
-    oracle.build()
-    reps = 3
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        rc, _, _ = oracle.render(m, cam, opt)
-    cpu = reps / (time.perf_counter() - t0)
-    print(json.dumps({"metric": "views/s", "value": 1e3 / ms, "unit": "views/s", "n_gpus": 1,
-                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-                      "gpix_per_s": W * H / (ms / 1e3) / 1e9,
-                      "config": {"workload": which, "pixels": W * H, "faces": m.num_faces,
-                                 "tuning": {"path": ["tiled", "global"][tuned.path],
-                                            "tile": 1 << tuned.tile_log2}},
-                      "cpu_baseline": {"value": cpu, "unit": "views/s", "cores": 1,
-                                       "kind": "port"}}), flush=True)
+
+    def timed(fn):
+        for _ in range(max(3, warmup)):
+            fn()
+        ctx.check(ctx.synchronize())
+        # a timed region of at least 0.3 s (one step here takes well under a
+        # millisecond), so that the clock sampler sees it
+        t0 = time.perf_counter()
+        fn()
+        ctx.check(ctx.synchronize())
+        n = max(steps, int(0.3 / max(time.perf_counter() - t0, 1e-5)))
+        ev = []
+        for _ in range(n):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            ev.append((a, b))
+        ctx.check(ctx.synchronize())
+        return sum(a.elapsed_time(b) for a, b in ev) / len(ev), n
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms, n_steps = timed(lambda: ctx.check(plan.launch()))
+    ms_direct, _ = timed(lambda: ctx.check(ctx.render_views([v], capi.DEVICE_POINTERS | capi.ASYNC)))
+    clocks = sampler.stop()
+    plan.close()
+    ctx.close()
+    cpu_line = None
+    if cpu:
+        import oracle
+        oracle.build()
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            rc, _, _ = oracle.render(m, cam, opt)
+            assert rc == 0
+        cpu_line = {"value": reps / (time.perf_counter() - t0), "unit": "views/s", "cores": 1,
+                    "kind": "port", "sample": f"{reps} renders of the view on one host core"}
+    return {"metric": "views/s", "value": 1e3 / ms, "unit": "views/s", "n_gpus": 1,
+            "steps": n_steps, "warmup": max(3, warmup), "ms_per_step": ms,
+            "gpix_per_s": W * H / (ms / 1e3) / 1e9,
+            "direct_call": {"views_per_s": 1e3 / ms_direct, "ms_per_step": ms_direct,
+                            "gpix_per_s": W * H / (ms_direct / 1e3) / 1e9},
+            "config": {"workload": which, "pixels": W * H, "faces": m.num_faces,
+                       "launch": "one CUDA-graph replay of the one-view render per step "
+                                 "(direct_call: one ugu_gpu_render_views call per step)",
+                       "l2": "flushed (256 MB write) between timed steps",
+                       "tuning": {"path": ["tiled", "global"][tuned.path],
+                                  "tile": 1 << tuned.tile_log2}},
+            "cpu_baseline": cpu_line, "clocks": clocks}
+
+
+def run_single(args, which):
+    print(json.dumps(measure_single(which, args.steps, args.warmup)), flush=True)
 
 
 class _DeviceArray:
@@ -375,7 +461,7 @@ class _DeviceArray:
                                          "data": (int(ptr), False), "version": 3}
 
 
-def run_texdescent(args, n_views=256, iters=20, lr=0.1):
+def measure_texdescent(warmup, n_views=256, iters=20, lr=0.1):
     """The large forward+backward: icosphere-8 (1,310,720 faces, radial noise
     0.01), a 4096^2 float texture, 256 Fibonacci-sphere cameras at distance
     3, 1280x720, fx = 1000; 20 iterations of texture gradient descent
@@ -390,16 +476,7 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
     from ugu_gb300 import capi, scenes
     from ugu_gb300.rasterizer import Context, RendererCpuOption
     t_setup = time.perf_counter()
-    m = scenes.icosphere(8, 1.0, 0.01, seed=1)
-    scenes.calc_normals(m)
-    scenes.with_texture(m, 4096, seed=3, f32=True)
-    # float texels in [0, 1], as multi-view texturing optimises them (a step
-    # of 0.1 on 0..255 values overshoots and diverges)
-    m.textures_f32 = [m.textures_f32[0] / np.float32(255.0)]
-    tm = m.copy()
-    tm.textures = [scenes.random_u8(5, m.textures[0].shape)]
-    tm.textures_f32 = [tm.textures[0].astype(np.float32) / np.float32(255.0)]
-    cams = scenes.fibonacci_cameras(n_views, 3.0, 1280, 720, 1000.0)
+    m, tm, cams = scenes.scene_texdescent(n_views)
     ctx = Context(0)
     ctx.check(ctx.set_option(RendererCpuOption(diffuse_color=1, interp=1, shading_normal=1,
                                                backface_culling=True)))
@@ -438,7 +515,7 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
     setup_s = time.perf_counter() - t_setup
     # warm-up iterations run every kernel of a step (the first use of each
     # loads its module) and leave the texels unchanged
-    warm = max(3, args.warmup)
+    warm = max(3, warmup)
     for _ in range(warm):
         ctx.check(plan.launch())
         grad.zero_()
@@ -451,6 +528,8 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
     losses = []
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
     e0.record(stream)
     for it in range(iters):
         ctx.check(plan.launch())
@@ -463,19 +542,32 @@ def run_texdescent(args, n_views=256, iters=20, lr=0.1):
         losses.append(loss.sum() / n_views)
     e1.record(stream)
     ctx.check(ctx.synchronize())
+    clocks = sampler.stop()
     ms = e0.elapsed_time(e1)
-    losses = [float(x) for x in losses]
+    # the loss after the last update (one more forward + backward, untimed)
+    ctx.check(plan.launch())
+    loss.zero_()
+    ctx.check(ctx.backward(fviews, tptr, grad.data_ptr(), None, None, loss.data_ptr(),
+                           capi.DEVICE_POINTERS | capi.ASYNC))
+    losses = [float(x) for x in losses] + [float(loss.sum() / n_views)]
     px = sum(c.width * c.height for c in cams)
     plan.close()
     ctx.close()
-    print(json.dumps({
+    return {
         "metric": "views/s (forward+backward)", "value": iters * n_views / (ms / 1e3),
         "unit": "views/s", "n_gpus": 1, "steps": iters, "warmup": warm,
         "ms_per_step": ms / iters, "gpix_per_s": iters * px / (ms / 1e3) / 1e9,
         "config": {"workload": "texdescent256_icosphere8_tex4096_f32_1280x720",
                    "views": n_views, "iterations": iters, "lr": lr, "faces": m.num_faces,
-                   "texels": "float32 in [0, 1]"},
-        "loss_first": losses[0], "loss_last": losses[-1], "setup_s": setup_s}), flush=True)
+                   "texels": "float32 in [0, 1]",
+                   "step": "one graph-replayed forward (face_id + float colour), one "
+                           "backward (texel gradient), one texel update per iteration"},
+        "loss_iter0": losses[0], "loss_iter20": losses[iters], "loss_curve": losses,
+        "setup_s": setup_s, "clocks": clocks}
+
+
+def run_texdescent(args):
+    print(json.dumps(measure_texdescent(args.warmup)), flush=True)
 
 
 def run_raytrace(args):
@@ -656,6 +748,8 @@ def main():
     launches = ctx.stats().launches - launches0
     ms_step = max_over_ranks(sum(ms) / len(ms), world)
     views_per_s = replica_views_per_s(len(cams), ms_step, world)
+    # the last timed replay's images, kept for the parity check below
+    replay = [{k: x.cpu().numpy() for k, x in t.items()} for t in outs]
 
     # the dominant kernel on its own: CUDA events around each tile-kernel
     # launch of a non-graph render of the same views (UGU_GPU_TIME_KERNELS),
@@ -670,6 +764,7 @@ def main():
 
     # per-view launch sequences (no graph), same outputs
     per_view = None
+    same_as_replay = {}
     if not args.no_per_view:
         def step_pv():
             ctx.check(ctx.render_views(views, capi.DEVICE_POINTERS | capi.PER_VIEW | capi.ASYNC))
@@ -679,6 +774,9 @@ def main():
         pv = timed(step_pv, max(2, min(args.steps, 5)))
         ctx.check(ctx.synchronize())
         per_view = len(cams) / (sum(pv) / len(pv) / 1e3)
+        same_as_replay["per_view"] = all(
+            view_digest({k: x.cpu().numpy() for k, x in t.items()}) == view_digest(r)
+            for t, r in zip(outs, replay))
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -711,6 +809,10 @@ def main():
         h2d = len(cams) * 256  # the per-view descriptor table (DevView, 248 B padded)
         e2e = {"value": world * len(cams) / dt, "unit": "views/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h + 32 * 64}
+        same_as_replay["e2e_host_buffers"] = all(
+            view_digest({k: x.numpy() for k, x in t.items()}) == view_digest(r)
+            for t, r in zip(host, replay))
+        del host
 
     # forward + backward: 16 ring views at 640x480 of the same mesh with float
     # texels; a step is one graph-replayed forward (face_id + float colour)
@@ -718,47 +820,78 @@ def main():
     fwd_bwd = None
     if not args.no_backward:
         fwd_bwd = measure_fwd_bwd(ctx, torch, dev, stream, flush, timed, args)
+    plan.close()
+    ctx.close()
 
+    # the oracle on all host threads over the same views: the CPU baseline,
+    # and the bit-for-bit check of the timed replay's images
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    parity = None
+    if rank == 0 and not (args.no_cpu_baseline and args.no_parity):
         threads = os.cpu_count() or 1
-        vps, gps, dt, nv = cpu_oracle_views_per_s(m, cams, threads)
-        cpu = {"value": vps, "unit": "views/s", "cores": threads, "kind": "port",
-               "sample": f"all {nv} views once on {threads} host threads ({dt:.1f} s wall), "
-                         "oracle restatement of Rasterizer::Render (-O2 -ffp-contract=off)"}
+        dt, ref = oracle_all_views(m, cams, threads, keep=not args.no_parity)
+        if not args.no_cpu_baseline:
+            cpu = {"value": len(cams) / dt, "unit": "views/s", "cores": threads, "kind": "port",
+                   "sample": f"all {len(cams)} views once, largest first, on {threads} host "
+                             f"threads ({dt:.2f} s wall); oracle restatement of "
+                             "Rasterizer::Render (-O2 -ffp-contract=off)"}
+        if ref is not None:
+            bad = [mismatched_pixels(r, g) for r, g in zip(ref, replay)]
+            parity = {"views": len(cams), "mismatched_px": int(sum(bad)),
+                      "mismatched_views": int(sum(b > 0 for b in bad)),
+                      "outputs": list(OUT_KEYS), "against": "oracle, bit for bit",
+                      "checked": "the last timed graph replay",
+                      "identical_to_replay": same_as_replay}
+            del ref
+    del replay
 
     peak, peak_kind = measured_peak_hbm()
+    traffic, warp_inst, prof_state = committed_tile_profile()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
     # the tile kernel writes every output byte (24 B/px) and reads the
     # texture and the geometry: the step's algorithmic bytes
     achieved = alg_bytes / (tile_ms / 1e3) / 1e9
     step_achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    # issue-side ceiling: warp instructions over what the SMs' 4 schedulers
+    # can issue in the kernel's time at the sampled SM clock
+    issue_frac = None
+    if warp_inst and clk.get("sm_mhz"):
+        issue_frac = warp_inst / (sms * 4 * clk["sm_mhz"] * 1e6 * tile_ms / 1e3)
+    config = ring_config(m, cams)
     line = {
         "metric": "views/s", "value": views_per_s, "unit": "views/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "ring64_icosphere7_tex2048_bilinear", "views": len(cams),
-                   "pixels": total_px, "mesh_faces": m.num_faces, "mesh_vertices": m.num_vertices,
-                   "texture": "2048x2048 RGB8", "outputs": "color,depth,normal,mask,face_id",
-                   "l2": "flushed (256 MB write) between timed steps",
-                   "launch": "one CUDA-graph replay of the batched render per step",
-                   "tuning": tuning},
+        "config": config,
+        "launch": "one CUDA-graph replay of the batched render per step",
+        "tuning": tuning,
         "gpix_per_s": world * total_px / (ms_step / 1e3) / 1e9,
         "per_view_views_per_s": per_view,
         "batched_over_per_view": (views_per_s / world / per_view) if per_view else None,
         "fwd_bwd": fwd_bwd,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": committed_traffic(),
+                     "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": f"profiles/k_tile_traffic.txt ({prof_state})",
                      "peak_source": peak_kind, "kernel": "k_tile",
                      "kernel_ms": tile_ms, "algorithmic_bytes": alg_bytes,
-                     "step_achieved": step_achieved, "step_frac": step_achieved / peak},
+                     "step_achieved": step_achieved, "step_frac": step_achieved / peak,
+                     "warp_instructions": warp_inst, "issue_frac": issue_frac},
+        "parity": parity,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk,
         "gpu_launches": int(launches),
     }
-    plan.close()
-    ctx.close()
+    if rank == 0 and not args.no_extras:
+        # the other configurations, each with its own clock record: the
+        # single-view forwards (UV sphere 640x480, textured icosphere-7
+        # 1920x1080) and the large forward+backward texture descent
+        line["extra"] = {
+            "c1_uvsphere_640x480": measure_single("uvsphere", args.steps, args.warmup),
+            "c2_icosphere7_1920x1080": measure_single("single1080", args.steps, args.warmup),
+            "c5_texdescent256": measure_texdescent(args.warmup),
+        }
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -378,18 +378,28 @@ UGU_GPU_API int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream);
  *
  * Limits: width * height <= UGU_GPU_NOALLOC_MAX_PIXELS, at most
  * UGU_GPU_NOALLOC_MAX_MATERIALS materials; larger requests return
- * UGU_GPU_ERR_CAPACITY.  The mesh arrays must be in the 4-wide layout below
- * (16-byte aligned) with in-range indices: device-resident indices are not
- * checked.  The first call on a device looks up the array's device address
- * for that device; make that first call before any stream capture.  All
- * calls share the array and it keeps the last call's contents (each call
- * clears what it needs first), so calls whose GPU work overlaps -- on
- * different streams or from different host threads -- race and must be
- * serialised by the caller.  Runs on the current device and on `stream`
- * (NULL = default stream) and returns when the images are written; errors
- * are reported in ugu_gpu_last_error(NULL). */
+ * UGU_GPU_ERR_CAPACITY before any work.  Faces whose screen box exceeds 256
+ * pixels are drawn as (face, 16x16 tile) items, at most
+ * UGU_GPU_NOALLOC_MAX_ITEMS per call (about 32 full-screen faces at
+ * 1920x1080); past that the call returns UGU_GPU_ERR_CAPACITY after the
+ * kernels ran, and the images are then not valid.  The mesh arrays must be
+ * in the 4-wide layout below (16-byte aligned) with in-range indices:
+ * device-resident indices are not checked.  Face normals are required
+ * whenever the mesh has faces: the reference's z pass reads them at every
+ * pixel of every face (rasterizer.cc:199).  The first call on a device
+ * looks up the array's device address for that device and keeps it for the
+ * life of the process; make that first call before any stream capture, and
+ * do not cudaDeviceReset a device while this library is in use there (the
+ * kept address would be stale).  All calls share the array and it keeps
+ * the last call's contents (each call clears what it needs first), so
+ * calls whose GPU work overlaps -- on different streams or from different
+ * host threads -- race and must be serialised by the caller.  Runs on the
+ * current device and on `stream` (NULL = default stream) and is
+ * synchronous: it returns when the images are written.  Errors are
+ * reported in ugu_gpu_last_error(NULL). */
 #define UGU_GPU_NOALLOC_MAX_PIXELS 2097152 /* e.g. 1920 x 1080 */
 #define UGU_GPU_NOALLOC_MAX_MATERIALS 16
+#define UGU_GPU_NOALLOC_MAX_ITEMS 262144
 
 typedef struct {
   int32_t width, height;

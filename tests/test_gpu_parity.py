@@ -310,3 +310,30 @@ def test_python_rasterizer_mirror(gpu_lib, oracle_lib):
     ok, outw = r.RenderW(depth=True)
     assert ok and outw["depth"].dtype == np.uint16
     assert np.array_equal(outw["depth"], np.trunc(ref["depth"]).astype(np.uint16))
+
+
+@pytest.mark.parametrize("path", [capi.PATH_TILED, capi.PATH_GLOBAL])
+def test_mesh_without_faces(ctx, oracle_lib, path):
+    """Vertices but no faces: the reference's checks pass (culling off,
+    vertex normals and colours present) and it renders empty images; so do
+    both paths here (no zero-block launch)."""
+    cam = adv.identity_camera()
+    m = adv.shared_edge_quad(cam)
+    m.vertex_indices = np.zeros((0, 3), np.int32)
+    m.face_normals = np.zeros((0, 3), np.float32)
+    m.normal_indices = np.zeros((0, 3), np.int32)
+    m.uv_indices = np.zeros((0, 3), np.int32)
+    m.material_ids = np.zeros(0, np.int32)
+    opt = adv.option(2, 1, 1, 0, False)
+    ref, _ = oracle_render(oracle_lib, m, cam, opt)
+    assert (ref["face_id"] == -1).all()
+    t0 = ctx.tuning()
+    ctx.check(ctx.set_tuning(capi.Tuning(path, 4, 0 if path == capi.PATH_TILED else 2048, 256,
+                                         1 << 22, 0)))
+    try:
+        for _ in range(2):
+            rc, got = gpu_render(ctx, m, cam, opt)
+            assert rc == 0, ctx.last_error()
+            compare(ref, got, "no faces")
+    finally:
+        ctx.check(ctx.set_tuning(t0))

@@ -2,8 +2,8 @@
 device memory (a plug-in given only finished buffers, code under another
 allocator's fixed budget, a frame loop that cannot take cudaMalloc's implicit
 synchronisation).  It must produce exactly what the regular entry point
-produces for the same view, on two calls in a row (the second call reuses the
-static scratch the first one left behind).
+produces for the same view, and what the oracle produces, on two calls in a
+row (the second call reuses the static scratch the first one left behind).
 
 Collected last on purpose: if it fails, a run that stops at the first
 failure has already run every other test.  It creates everything it uses, so
@@ -60,7 +60,7 @@ def _device_mesh(torch, m):
     return d, keep
 
 
-def test_noalloc_matches_regular_entry_point_twice(gpu_lib):
+def test_noalloc_matches_regular_entry_point_twice(gpu_lib, oracle_lib):
     torch = pytest.importorskip("torch")
     from ugu_gb300.rasterizer import Context
     m = scenes.icosphere_textured(5, 256)
@@ -85,6 +85,9 @@ def test_noalloc_matches_regular_entry_point_twice(gpu_lib):
                 ref = {k: v.cpu().numpy() for k, v in want[i].items()}
                 out = {k: v.cpu().numpy() for k, v in got[i].items()}
                 compare(ref, out, f"noalloc view {i}")
+                rc, orc, _ = oracle_lib.render(m, cam, opt, color_f32=True)
+                assert rc == 0
+                compare(orc, out, f"noalloc view {i} vs oracle")
             del keep
     finally:
         ctx.close()
@@ -103,3 +106,63 @@ def test_noalloc_rejects_oversized_images(gpu_lib):
                                         C.byref(capi.camera_struct(cam)), C.byref(im), None)
     assert rc == capi.ERR_CAPACITY
     assert b"UGU_GPU_NOALLOC_MAX_PIXELS" in gpu_lib.ugu_gpu_last_error(None)
+
+
+def test_noalloc_mesh_without_faces(gpu_lib, oracle_lib):
+    """A mesh with vertices but no faces renders empty images, as the
+    reference does when its checks pass (culling off, vertex normals and
+    colours present); no face normals are needed then."""
+    torch = pytest.importorskip("torch")
+    cam = adv.identity_camera()
+    m = adv.shared_edge_quad(cam)
+    m.vertex_indices = np.zeros((0, 3), np.int32)
+    m.face_normals = np.zeros((0, 3), np.float32)
+    m.normal_indices = np.zeros((0, 3), np.int32)
+    m.uv_indices = np.zeros((0, 3), np.int32)
+    m.material_ids = np.zeros(0, np.int32)
+    opt = adv.option(2, 1, 1, 0, False)
+    rc, ref, _ = oracle_lib.render(m, cam, opt, color_f32=True)
+    assert rc == 0 and (ref["face_id"] == -1).all()
+    dmesh, keep = _device_mesh(torch, m)
+    dmesh.face_normals4 = None
+    dmesh.normal_indices4 = None
+    o = to_option(opt).to_struct()
+    got, gviews = device_views(torch, [cam, cam], [0, 0])
+    for i in range(2):
+        rc = gpu_lib.ugu_gpu_render_noalloc(C.byref(dmesh), C.byref(o),
+                                            C.byref(capi.camera_struct(cam)),
+                                            C.byref(gviews[i].images), None)
+        assert rc == 0, gpu_lib.ugu_gpu_last_error(None)
+        compare(ref, {k: v.cpu().numpy() for k, v in got[i].items()}, f"no faces, call {i}")
+
+
+def test_noalloc_reports_item_overflow(gpu_lib):
+    """Forty faces that each cover the whole 1920x1080 image need 326,400
+    (face, 16x16 tile) items, more than UGU_GPU_NOALLOC_MAX_ITEMS: the call
+    reports UGU_GPU_ERR_CAPACITY (its images are then not valid), and the
+    next call in range succeeds."""
+    torch = pytest.importorskip("torch")
+    cam = adv.identity_camera(W=1920, H=1080, f=1000.0)
+    verts, faces = [], []
+    for k in range(40):
+        z = 2.0 + 0.01 * k
+        base = len(verts)
+        verts += [adv.unproject(cam, -3000.0, -3000.0, z), adv.unproject(cam, 6000.0, -3000.0, z),
+                  adv.unproject(cam, -3000.0, 6000.0, z)]
+        faces.append([base, base + 1, base + 2])
+    m = adv._finish(np.array(verts, np.float32), np.array(faces, np.int32))
+    dmesh, keep = _device_mesh(torch, m)
+    o = to_option(adv.option(2, 1, 1, 0, False)).to_struct()
+    got, gviews = device_views(torch, [cam], [0], outputs=("face_id",))
+    rc = gpu_lib.ugu_gpu_render_noalloc(C.byref(dmesh), C.byref(o),
+                                        C.byref(capi.camera_struct(cam)),
+                                        C.byref(gviews[0].images), None)
+    assert rc == capi.ERR_CAPACITY
+    assert b"large-face tile items" in gpu_lib.ugu_gpu_last_error(None)
+    small = adv.identity_camera()
+    got, gviews = device_views(torch, [small], [0], outputs=("face_id",))
+    rc = gpu_lib.ugu_gpu_render_noalloc(C.byref(dmesh), C.byref(o),
+                                        C.byref(capi.camera_struct(small)),
+                                        C.byref(gviews[0].images), None)
+    assert rc == 0, gpu_lib.ugu_gpu_last_error(None)
+    assert (got[0]["face_id"].cpu().numpy() == 0).all()  # face 0 is nearest everywhere

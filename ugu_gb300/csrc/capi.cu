@@ -329,12 +329,14 @@ int validate_view(ugu_gpu_context* ctx, const ugu_gpu_view& v, bool any_output) 
   if (!any_output)
     return set_error(ctx, UGU_GPU_ERR_NO_OUTPUT, "all arguments are nullptr. nothing to do");
   // Preconditions the reference leaves undefined (it would read past its
-  // arrays): the z pass reads face normals for the back-face test; the
-  // texture path reads uv, uv_indices and material_ids.
-  if (!m.has_fnormals)
+  // arrays): the z pass reads face normals for the back-face test
+  // (rasterizer.cc:199); the texture path reads uv, uv_indices and
+  // material_ids.  A mesh without faces reads none of them.
+  const bool has_faces = m.dev.num_faces > 0;
+  if (has_faces && !m.has_fnormals)
     return set_error(ctx, UGU_GPU_ERR_NO_FACE_NORMALS,
                      "face normals are required: the z pass reads them for every face");
-  if (o.diffuse_color == 1 && (!m.has_uv || !m.has_matids))
+  if (has_faces && o.diffuse_color == 1 && (!m.has_uv || !m.has_matids))
     return set_error(ctx, UGU_GPU_ERR_NO_TEXTURE,
                      "texture colour needs uv, uv_indices and material_ids");
   const ugu_gpu_camera& c = v.camera;

@@ -11,7 +11,8 @@
 // and the large-face tile list -- from one file-scope __device__ array.
 //
 // Limits: at most kMaxPixels pixels per view, kMaxMaterials materials and
-// kMaxItems (face, tile) items for faces whose bbox exceeds 256 pixels.
+// kMaxItems (face, tile) items for faces whose bbox exceeds 256 pixels (past
+// that the call returns UGU_GPU_ERR_CAPACITY and the images are not valid).
 // Every GPU that loads this library holds the array (about 20 MB) until the
 // process exits.  All calls share it: two calls whose work overlaps on the GPU
 // (different streams, or different host threads) race on it and must be
@@ -35,7 +36,7 @@ using namespace ugu_gpu;
 
 constexpr int64_t kMaxPixels = UGU_GPU_NOALLOC_MAX_PIXELS;
 constexpr int kMaxMaterials = UGU_GPU_NOALLOC_MAX_MATERIALS;
-constexpr int64_t kMaxItems = 262144;
+constexpr int64_t kMaxItems = UGU_GPU_NOALLOC_MAX_ITEMS;
 constexpr size_t kHeadBytes = 4096;
 
 struct Head {
@@ -64,7 +65,9 @@ int fail(int code, const char* msg) {
 }
 
 // Device address of the scratch on the current device, looked up once per
-// device (the first call on a device does this set-up).
+// device (the first call on a device does this set-up) and kept for the life
+// of the process: a cudaDeviceReset on that device while the library is in
+// use would leave the kept address stale.
 int scratch_address(int dev, unsigned char** out) {
   std::lock_guard<std::mutex> lock(g_mu);
   if (!g_addr[dev]) {
@@ -100,13 +103,15 @@ int validate(const ugu_gpu_device_mesh& m, const ugu_gpu_option& o, const ugu_gp
     return fail(UGU_GPU_ERR_NO_VERTEX_COLORS, "specified vertex color as diffuse color but vertex color is empty.");
   if (o.shading_normal == 0 && !m.face_normals4)
     return fail(UGU_GPU_ERR_NO_FACE_NORMALS_FOR_SHADING, "specified face normal as shading normal but face normal is empty.");
-  if (o.shading_normal == 1 && (!m.normals4 || !m.normal_indices4))
+  if (o.shading_normal == 1 && (!m.normals4 || (m.num_faces > 0 && !m.normal_indices4)))
     return fail(UGU_GPU_ERR_NO_VERTEX_NORMALS, "specified vertex normal as shading normal but vertex normal is empty.");
   if (!im.color && !im.depth && !im.normal && !im.mask && !im.face_id && !im.color_f32)
     return fail(UGU_GPU_ERR_NO_OUTPUT, "all arguments are nullptr. nothing to do");
-  if (!m.face_normals4)
+  // rasterizer.cc:199 reads the face normal at every pixel of every face's
+  // box; a mesh without faces reads none (nor uv, uv indices, material ids)
+  if (m.num_faces > 0 && !m.face_normals4)
     return fail(UGU_GPU_ERR_NO_FACE_NORMALS, "face normals are required: the z pass reads them");
-  if (o.diffuse_color == 1 && (!m.uv2 || !m.uv_indices4 || !m.material_ids))
+  if (m.num_faces > 0 && o.diffuse_color == 1 && (!m.uv2 || !m.uv_indices4 || !m.material_ids))
     return fail(UGU_GPU_ERR_NO_TEXTURE, "texture colour needs uv, uv_indices and material_ids");
   if (m.num_vertices < 0 || m.num_faces < 0 || (m.num_faces > 0 && (!m.vertices4 || !m.vertex_indices4)))
     return fail(UGU_GPU_ERR_INVALID_ARGUMENT, "vertices or faces missing");

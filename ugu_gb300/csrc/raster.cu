@@ -192,6 +192,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(RenderParams p) {
 
 void launch_raster(const RenderParams& p, int max_faces, int num_sms, cudaStream_t s) {
   (void)num_sms;
+  if (max_faces <= 0) return;  // no face to draw: k_resolve writes the empty images
   dim3 grid((max_faces + kRasterThreads - 1) / kRasterThreads, p.num_views);
   k_raster<<<grid, kRasterThreads, 0, s>>>(p);
 }

@@ -842,9 +842,13 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
 
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
   constexpr int kPerBlock = kBinThreads * kBinFaces;
-  k_proj<<<dim3((p.max_vertices + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads, 0,
-           s>>>(p);
-  k_bin<<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0, s>>>(p);
+  // a mesh without vertices or faces bins nothing (a grid of zero blocks is
+  // a launch error); the scan, gather and tile kernels then write empty images
+  if (p.max_vertices > 0)
+    k_proj<<<dim3((p.max_vertices + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads,
+             0, s>>>(p);
+  if (max_faces > 0)
+    k_bin<<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0, s>>>(p);
   k_scan<<<1, kScanThreads, 0, s>>>(p);
 }
 

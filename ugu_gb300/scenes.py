@@ -484,3 +484,22 @@ def scene_ring_batch(n_views: int = 64, subdiv: int = 7, tex_size: int = 2048, s
     m = icosphere_textured(subdiv, tex_size)
     cams = ring_cameras(n_views, 3.0, seeded_sizes(n_views, seed))
     return m, cams
+
+
+def scene_texdescent(n_views: int = 256, subdiv: int = 8, tex_size: int = 4096):
+    """The large forward+backward configuration: an icosphere subdivided 8
+    times (655,362 vertices / 1,310,720 faces, radial noise sigma 0.01, seed
+    1), a tex_size^2 float32 texture with texels in [0, 1] (seed 3), the
+    target mesh with a second texture (seed 5), and n cameras on a
+    Fibonacci sphere at distance 3, 1280x720, fx = 1000.  Returns (mesh,
+    target mesh, cameras)."""
+    m = icosphere(subdiv, 1.0, 0.01, seed=1)
+    calc_normals(m)
+    with_texture(m, tex_size, seed=3, f32=True)
+    # float texels in [0, 1], as multi-view texturing optimises them
+    m.textures_f32 = [m.textures_f32[0] / np.float32(255.0)]
+    tm = m.copy()
+    tm.textures = [random_u8(5, m.textures[0].shape)]
+    tm.textures_f32 = [tm.textures[0].astype(np.float32) / np.float32(255.0)]
+    cams = fibonacci_cameras(n_views, 3.0, 1280, 720, 1000.0)
+    return m, tm, cams
