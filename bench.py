@@ -420,8 +420,12 @@ def measure_single(which, steps, warmup, cpu=True):
     sampler = ClockSampler(0)
     sampler.start()
     ms, n_steps = timed(lambda: ctx.check(plan.launch()))
+    ctx.check(ctx.synchronize())
+    replay = {k: x.cpu().numpy() for k, x in t.items()}
     ms_direct, _ = timed(lambda: ctx.check(ctx.render_views([v], capi.DEVICE_POINTERS | capi.ASYNC)))
     clocks = sampler.stop()
+    ctx.check(ctx.synchronize())  # reports any asynchronous render that overflowed
+    direct_same = view_digest({k: x.cpu().numpy() for k, x in t.items()}) == view_digest(replay)
     plan.close()
     ctx.close()
     cpu_line = None
@@ -439,7 +443,8 @@ def measure_single(which, steps, warmup, cpu=True):
             "steps": n_steps, "warmup": max(3, warmup), "ms_per_step": ms,
             "gpix_per_s": W * H / (ms / 1e3) / 1e9,
             "direct_call": {"views_per_s": 1e3 / ms_direct, "ms_per_step": ms_direct,
-                            "gpix_per_s": W * H / (ms_direct / 1e3) / 1e9},
+                            "gpix_per_s": W * H / (ms_direct / 1e3) / 1e9,
+                            "same_images_as_replay": direct_same},
             "config": {"workload": which, "pixels": W * H, "faces": m.num_faces,
                        "launch": "one CUDA-graph replay of the one-view render per step "
                                  "(direct_call: one ugu_gpu_render_views call per step)",

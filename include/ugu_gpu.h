@@ -138,7 +138,11 @@ typedef struct {
 enum {
   UGU_GPU_DEVICE_POINTERS = 1u << 0, /* images are device pointers (else host) */
   UGU_GPU_PER_VIEW = 1u << 1,        /* one launch sequence per view (baseline) */
-  UGU_GPU_ASYNC = 1u << 2,           /* do not synchronise (device pointers only) */
+  UGU_GPU_ASYNC = 1u << 2,           /* do not synchronise (device pointers only); on the
+                                        tiled path the first such render of a view list
+                                        runs a sizing pass first (synchronous, as
+                                        ugu_gpu_plan_create does); its status comes from
+                                        the next ugu_gpu_synchronize */
   UGU_GPU_TIME_KERNELS = 1u << 3,    /* time the per-tile raster kernel with CUDA events
                                         (ugu_gpu_stats.tile_kernel_ms); not with ASYNC */
   UGU_GPU_RAYTRACE = 1u << 4         /* render with ugu::Raytracer's semantics
@@ -358,6 +362,11 @@ UGU_GPU_API int ugu_gpu_test_visibility(ugu_gpu_context* ctx, int32_t mesh, cons
                                         const ugu_gpu_visibility_option* option,
                                         int32_t facewise, const ugu_gpu_visibility_out* out,
                                         uint32_t flags);
+/* Waits for the context's stream, then reports what the asynchronous renders
+ * and plan replays since the last call left: UGU_GPU_ERR_CAPACITY when a
+ * (face, tile) list overflowed (those images are not valid; render again,
+ * the lists have grown), UGU_GPU_ERR_DEGENERATE_DEPTH for a covered sample
+ * with depth < FLT_MIN or NaN. */
 UGU_GPU_API int ugu_gpu_synchronize(ugu_gpu_context* ctx);
 /* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
 UGU_GPU_API int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream);

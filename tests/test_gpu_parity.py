@@ -337,3 +337,66 @@ def test_mesh_without_faces(ctx, oracle_lib, path):
             compare(ref, got, "no faces")
     finally:
         ctx.check(ctx.set_tuning(t0))
+
+
+def test_async_render_sizes_first_and_matches_oracle(gpu_lib, oracle_lib, torch_cuda):
+    """A fresh context's first UGU_GPU_ASYNC render of the 1920x1080
+    icosphere-7 view on 16x16 tiles needs more (face, tile) entries than the
+    default lists hold: it sizes them first, so the images are exact and the
+    next synchronize reports nothing."""
+    torch = torch_cuda
+    from gpu_helpers import to_option
+    from ugu_gb300.rasterizer import Context
+    m, cam = scenes.scene_icosphere_single_view()
+    opt = adv.option(1, 1, 1, 0, True)
+    c = Context(0)
+    try:
+        t = c.tuning()
+        t.path, t.tile_log2 = capi.PATH_TILED, 4
+        c.check(c.set_tuning(t))
+        c.check(c.set_mesh(0, m))
+        c.check(c.set_option(to_option(opt)))
+        tensors, views = device_views(torch, [cam], [0])
+        ref, _ = oracle_render(oracle_lib, m, cam, opt)
+        for _ in range(2):
+            c.check(c.render_views(views, capi.DEVICE_POINTERS | capi.ASYNC))
+            assert c.synchronize() == 0, c.last_error()
+            compare(ref, {k: v.cpu().numpy() for k, v in tensors[0].items()}, "async")
+            for x in tensors[0].values():
+                x.fill_(3)
+    finally:
+        c.close()
+
+
+def test_async_overflow_is_reported_at_synchronize(gpu_lib, torch_cuda):
+    """The global path keeps a fixed list of (face, tile) items: 200 faces
+    over a whole 1920x1080 image in 8x8 tiles need 6.5 M of them.  An
+    asynchronous render cannot retry, so ugu_gpu_synchronize reports the
+    overflow (its images are not valid); a synchronous render, which grows
+    the list and retries, then succeeds."""
+    torch = torch_cuda
+    from gpu_helpers import to_option
+    from ugu_gb300.rasterizer import Context
+    cam = adv.identity_camera(W=1920, H=1080, f=1000.0)
+    verts, faces = [], []
+    for k in range(200):
+        z = 2.0 + 0.001 * k
+        b = len(verts)
+        verts += [adv.unproject(cam, -3000.0, -3000.0, z), adv.unproject(cam, 6000.0, -3000.0, z),
+                  adv.unproject(cam, -3000.0, 6000.0, z)]
+        faces.append([b, b + 1, b + 2])
+    m = adv._finish(np.array(verts, np.float32), np.array(faces, np.int32))
+    c = Context(0)
+    try:
+        c.check(c.set_tuning(capi.Tuning(capi.PATH_GLOBAL, 3, 0, 0, 1 << 22, 0)))
+        c.check(c.set_mesh(0, m))
+        c.check(c.set_option(to_option(adv.option(2, 1, 1, 0, False))))
+        tensors, views = device_views(torch, [cam], [0], outputs=("face_id",))
+        c.check(c.render_views(views, capi.DEVICE_POINTERS | capi.ASYNC))
+        assert c.synchronize() == capi.ERR_CAPACITY
+        assert c.synchronize() == 0  # reported once
+        c.check(c.render_views(views, capi.DEVICE_POINTERS))
+        assert (tensors[0]["face_id"].cpu().numpy() == 0).all()
+        assert c.synchronize() == 0
+    finally:
+        c.close()

@@ -76,6 +76,9 @@ struct Scratch {
   TileCounters* h_tcounters = nullptr;  // pinned
   size_t tcounters_cap = 0;
   bool tiles_dirty = false;
+  // signature of the view list the entry and run lists were last sized for
+  // by a sizing pass (asynchronous renders size before they enqueue)
+  uint64_t sized_sig = 0;
   size_t list_min = size_t(1) << 22;  // capacity of the item / overflow lists
   // backward: per-view target pointers, hi + lo projection table
   void* proj64 = nullptr;    // 32 bytes per vertex of every view
@@ -127,6 +130,16 @@ struct ugu_gpu_context {
   uint64_t large_items = 0;
   // counters of the last asynchronous plan replay, checked at synchronize
   ugu_gpu_plan* pending_plan = nullptr;
+  // groups of the last UGU_GPU_ASYNC render, whose counters synchronize checks
+  size_t pending_async_groups = 0;
+  // sticky status word the kernels set (kStickyOverflow, kStickySpecial):
+  // read and cleared by ugu_gpu_synchronize, so that no asynchronous render
+  // or replay whose lists overflowed passes unreported
+  unsigned long long* d_sticky = nullptr;
+  // set while an asynchronous render or a plan is enqueued: only those use
+  // the sticky word (a synchronous render checks and retries on its own)
+  bool sticky_on = false;
+  uint64_t mesh_generation = 0;  // bumped by every ugu_gpu_set_mesh
   // set while a UGU_GPU_RAYTRACE render or plan is being prepared and enqueued
   bool raytrace = false;
   // plans created on this context and not destroyed yet (destroyed with it)
@@ -576,6 +589,7 @@ RenderParams base_params(ugu_gpu_context* ctx, const Scratch& s) {
   p.item_capacity = (int64_t)s.items_cap;
   p.tile_log2 = ctx->tuning.tile_log2;
   p.small_bbox_max = ctx->tuning.small_bbox_max;
+  p.sticky = ctx->sticky_on ? ctx->d_sticky : nullptr;
   return p;
 }
 
@@ -615,6 +629,7 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.staged = s.entries + s.entries_cap;
   p.runs = s.runs;
   p.counters = s.tcounters + gi;
+  p.sticky = ctx->sticky_on ? ctx->d_sticky : nullptr;
   return p;
 }
 
@@ -798,7 +813,6 @@ int prepare_scratch(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& 
   return ensure_tiled(ctx, s, groups);
 }
 
-// Everything one render enqueues once its view table is on the device.
 // Everything one render enqueues once its view table is on the device.  With
 // host outputs, each group's copies run on the copy stream as soon as the
 // group's kernels are done, overlapping the next group's kernels; the
@@ -903,6 +917,26 @@ int ensure_bvhs(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views) {
   return UGU_GPU_OK;
 }
 
+// FNV-1a over what decides a tiled render's entry and run counts: the views'
+// meshes and cameras, the mesh uploads and the tuning.
+uint64_t view_list_signature(const ugu_gpu_context* ctx, int n, const ugu_gpu_view* views,
+                             uint32_t flags) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const void* p, size_t len) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < len; ++i) h = (h ^ b[i]) * 1099511628211ull;
+  };
+  mix(&n, sizeof(n));
+  mix(&flags, sizeof(flags));
+  mix(&ctx->mesh_generation, sizeof(ctx->mesh_generation));
+  mix(&ctx->tuning, sizeof(ctx->tuning));
+  for (int i = 0; i < n; ++i) {
+    mix(&views[i].mesh, sizeof(views[i].mesh));
+    mix(&views[i].camera, sizeof(views[i].camera));
+  }
+  return h | 1ull;  // never 0, the "not sized" value
+}
+
 int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t flags) {
   if (n < 0 || (n > 0 && !views))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view list");
@@ -935,6 +969,17 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
     CK(ctx, cudaMemcpyAsync(s.d_views, s.h_views, n * sizeof(DevView), cudaMemcpyHostToDevice,
                             ctx->stream),
        "cudaMemcpyAsync(views)");
+    // An asynchronous render cannot be retried once its lists overflowed, so
+    // on the tiled path it first counts its entries with a sizing pass (as a
+    // plan does), unless these very views were sized last.
+    const bool async = (flags & UGU_GPU_ASYNC) != 0;
+    if (async && !ray && ctx->tuning.path != UGU_GPU_PATH_GLOBAL) {
+      const uint64_t sig = view_list_signature(ctx, n, views, flags);
+      if (sig != s.sized_sig) {
+        if ((rc = size_tiled(ctx, s, groups))) return rc;
+        s.sized_sig = sig;
+      }
+    }
     int kernels = 0;
     ctx->time_tile = (flags & UGU_GPU_TIME_KERNELS) != 0;
     ctx->timed_groups = 0;
@@ -943,14 +988,19 @@ int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t
       CK(ctx, cudaEventCreate(&e), "cudaEventCreate");
       ctx->tile_events.push_back(e);
     }
+    ctx->sticky_on = async;
     rc = enqueue_render(ctx, s, groups, views, n, dev, &kernels);
+    ctx->sticky_on = false;
     ctx->time_tile = false;
     if (rc) {
       s.keys_dirty = s.tiles_dirty = true;
       return rc;
     }
     ctx->launches += kernels;
-    if (flags & UGU_GPU_ASYNC) return UGU_GPU_OK;
+    if (async) {
+      ctx->pending_async_groups = ray ? 0 : groups.size();
+      return UGU_GPU_OK;
+    }
     CK(ctx, cudaStreamSynchronize(ctx->stream), "render");
     if (ray) return UGU_GPU_OK;
     rc = check_counters(ctx, s, groups.size());
@@ -1004,11 +1054,14 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_meshes, kMaxMeshes * sizeof(DevMesh));
   if (e == cudaSuccess) e = cudaMemset(ctx->d_meshes, 0, kMaxMeshes * sizeof(DevMesh));
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_sticky, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_sticky, 0, sizeof(unsigned long long));
   if (e != cudaSuccess) {
     set_error(nullptr, UGU_GPU_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     cudaFree(ctx->d_meshes);
+    cudaFree(ctx->d_sticky);
     delete ctx;
     return UGU_GPU_ERR_CUDA;
   }
@@ -1041,6 +1094,7 @@ int ugu_gpu_destroy(ugu_gpu_context* ctx) {
   for (MeshSlot& s : ctx->meshes) free_slot(s);
   free_scratch(ctx->scratch);
   cudaFree(ctx->d_meshes);
+  cudaFree(ctx->d_sticky);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
@@ -1069,6 +1123,7 @@ int ugu_gpu_set_mesh(ugu_gpu_context* ctx, int32_t slot, const ugu_gpu_mesh* m) 
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   MeshSlot& s = ctx->meshes[slot];
   free_slot(s);
+  ++ctx->mesh_generation;
   DevMesh empty{};
   CK(ctx, cudaMemcpy(ctx->d_meshes + slot, &empty, sizeof(DevMesh), cudaMemcpyHostToDevice),
      "cudaMemcpy(mesh table)");
@@ -1260,7 +1315,9 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
   }
   if (!rc) {
     int k = 0;
+    ctx->sticky_on = true;
     rc = enqueue_render(ctx, s, plan->groups, views, n, true, &k);
+    ctx->sticky_on = false;
     plan->kernels = k;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &plan->graph);
     if (!rc && e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaStreamEndCapture");
@@ -1418,13 +1475,35 @@ int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
 int ugu_gpu_synchronize(ugu_gpu_context* ctx) {
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  int rc = UGU_GPU_OK;
+  // the last asynchronous render's and replay's counters (an overflow grows
+  // the lists for the next render), then what any earlier one left sticky
+  if (ctx->pending_async_groups) {
+    const size_t g = ctx->pending_async_groups;
+    ctx->pending_async_groups = 0;
+    rc = check_counters(ctx, ctx->scratch, g);
+    if (rc == UGU_GPU_ERR_CAPACITY) ctx->scratch.sized_sig = 0;
+  }
   if (ctx->pending_plan) {
     ugu_gpu_plan* p = ctx->pending_plan;
     ctx->pending_plan = nullptr;
-    if (p->raytrace) return UGU_GPU_OK;
-    return check_counters(ctx, p->scratch, p->groups.size());
+    const int prc = p->raytrace ? UGU_GPU_OK : check_counters(ctx, p->scratch, p->groups.size());
+    if (!rc) rc = prc;
   }
-  return UGU_GPU_OK;
+  unsigned long long sticky = 0;
+  CK(ctx, cudaMemcpy(&sticky, ctx->d_sticky, sizeof(sticky), cudaMemcpyDeviceToHost),
+     "cudaMemcpy(status)");
+  if (sticky) {
+    CK(ctx, cudaMemset(ctx->d_sticky, 0, sizeof(sticky)), "cudaMemset(status)");
+    if (!rc && (sticky & kStickyOverflow))
+      rc = set_error(ctx, UGU_GPU_ERR_CAPACITY,
+                     "an asynchronous render overflowed its tile lists: its images are not "
+                     "valid; render it again");
+    if (!rc && (sticky & kStickySpecial))
+      rc = set_error(ctx, UGU_GPU_ERR_DEGENERATE_DEPTH,
+                     "an asynchronous render had covered samples with depth < FLT_MIN or NaN");
+  }
+  return rc;
 }
 
 int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream) {

@@ -80,6 +80,10 @@ struct DevView {
   float* color_f32;
 };
 
+// Bits of the sticky status word (RenderParams::sticky, TileParams::sticky).
+constexpr unsigned long long kStickyOverflow = 1ull;
+constexpr unsigned long long kStickySpecial = 2ull;
+
 // Counters shared by the kernels of one render (device memory).
 struct DevCounters {
   unsigned long long special;     // covered samples with unorderable depth
@@ -119,6 +123,10 @@ struct RenderParams {
   int64_t item_capacity;
   int32_t tile_log2;
   int32_t small_bbox_max;
+  // sticky status of the context, or NULL: bit 0 a list overflowed (the
+  // render's images are not valid), bit 1 a covered sample had an
+  // unorderable depth; kept until ugu_gpu_synchronize reads and clears it
+  unsigned long long* sticky;
 };
 
 // Counters of one tiled render (memset before every launch).
@@ -158,6 +166,7 @@ struct TileParams {
   int4* runs;           // (tile, draw class, first staged entry, count)
   int2* entries;        // entries in tile order
   TileCounters* counters;
+  unsigned long long* sticky;  // as RenderParams::sticky
 };
 
 struct BackwardParams {

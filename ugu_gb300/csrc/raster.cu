@@ -55,14 +55,15 @@ __device__ __forceinline__ bool setup_face(const DevMesh& m, const Cam& c, int f
 __device__ __forceinline__ void raster_pixel(const Cam& c, const FaceSetup& s, float4 fn,
                                              int f, int x, int y,
                                              unsigned long long* keys,
-                                             DevCounters* counters) {
+                                             const RenderParams& p) {
   float3 r = ray_w(c, x, y);
   bool bf = dot3(fn.x, fn.y, fn.z, r.x, r.y, r.z) > 0.0f;
   Bary b = edges_at(s, x, y);
   if (!covered(b, bf)) return;
   float z = perspective(s, b);
   if (!orderable_depth(z)) {
-    atomicAdd(&counters->special, 1ull);
+    atomicAdd(&p.counters->special, 1ull);
+    if (p.sticky) atomicOr(p.sticky, kStickySpecial);
     return;
   }
   unsigned long long key = make_key(z, f, bf);
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(RenderParams p) {
   if (npx <= p.small_bbox_max) {
     float4 fn = __ldg(&sm.fnormals[f]);
     for (int y = s.y0; y <= s.y1; ++y)
-      for (int x = s.x0; x <= s.x1; ++x) raster_pixel(c, s, fn, f, x, y, keys, p.counters);
+      for (int x = s.x0; x <= s.x1; ++x) raster_pixel(c, s, fn, f, x, y, keys, p);
     return;
   }
   const int ts = p.tile_log2;
@@ -99,6 +100,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(RenderParams p) {
     unsigned long long slot = base + k;
     if (slot >= (unsigned long long)p.item_capacity) {
       atomicAdd(&p.counters->overflow, (unsigned long long)(n - k));
+      if (p.sticky) atomicOr(p.sticky, kStickyOverflow);
       break;
     }
     TileItem it;
@@ -137,7 +139,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(RenderParams p) {
     unsigned long long* keys = p.keys + sv.key_offset;
     if (w > 0 && h > 0)
       for (int k = threadIdx.x; k < w * h; k += blockDim.x)
-        raster_pixel(c, s, fn, it.face, xa + k % w, ya + k / w, keys, p.counters);
+        raster_pixel(c, s, fn, it.face, xa + k % w, ya + k / w, keys, p);
   }
 }
 

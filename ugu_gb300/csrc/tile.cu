@@ -306,7 +306,10 @@ __global__ void __launch_bounds__(kBinThreads, UGU_BIN_BLOCKS) k_bin(TileParams 
     const unsigned long long r = nr ? atomicAdd(&p.counters->total_runs, nr) : 0;
     const bool ok = b + ne <= (unsigned long long)p.entry_cap &&
                     r + nr <= (unsigned long long)p.run_cap;
-    if (!ok) atomicExch(&p.counters->dropped, 1ull);
+    if (!ok) {
+      atomicExch(&p.counters->dropped, 1ull);
+      if (p.sticky) atomicOr(p.sticky, kStickyOverflow);
+    }
     sb.base = b;
     sb.run_base = r;
     sb.ok = ok;
@@ -450,7 +453,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
   }
   if (tid == 0) {
     p.tile_off[T] = (int)carry;  // k_bin's cursor keeps the render's entry count
-    if (carry > p.entry_cap) p.counters->dropped = 1ull;
+    if (carry > p.entry_cap) {
+      p.counters->dropped = 1ull;
+      if (p.sticky) atomicOr(p.sticky, kStickyOverflow);
+    }
   }
 }
 
@@ -481,6 +487,7 @@ struct TileSmem {
   Region reg;
   DevView view;
   DevMesh mesh;
+  DevTexture tex0;  // the view's mesh's first material, for the resolve
   int item;
   unsigned zmax_bits;
   int cursor[2];  // next entry of each draw class: warps take 32 at a time
@@ -533,6 +540,7 @@ __device__ __forceinline__ void depth_test(TileSmem& sm, const Region& R, const 
   const float z = perspective(s, b);
   if (!orderable_depth(z)) {
     atomicAdd(&p.counters->special, 1ull);
+    if (p.sticky) atomicOr(p.sticky, kStickySpecial);
     return;
   }
   const unsigned long long key = make_key(z, __float_as_int(r2.w), bf);
@@ -664,6 +672,10 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
       copy_words(sm.view, p.views[v]);
       __syncthreads();
       copy_words(sm.mesh, p.meshes[sm.view.mesh]);
+      if (tid == 0) {
+        const DevMesh& gm = p.meshes[sm.view.mesh];
+        sm.tex0 = gm.num_materials > 0 ? gm.textures[0] : DevTexture{0, 0, nullptr, nullptr};
+      }
       v_begin = p.views[v].tile_base;
       v_end = v + 1 < p.num_views ? p.views[v + 1].tile_base : p.total_tiles;
     }
@@ -805,18 +817,8 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
         sh.c[0] = sh.c[1] = sh.c[2] = 0;
         sh.cf[0] = sh.cf[1] = sh.cf[2] = 0.0f;
         sh.n[0] = sh.n[1] = sh.n[2] = 0.0f;
-        if (fid > 0) {
-          FaceSetup s;
-          const int4 vi = __ldg(&sm.mesh.vidx_ranked[fid]);
-          const float4 a = __ldg(&proj[vi.x]);
-          const float4 b = __ldg(&proj[vi.y]);
-          const float4 d = __ldg(&proj[vi.z]);
-          s.v0 = make_float3(a.x, a.y, a.z);
-          s.v1 = make_float3(b.x, b.y, b.z);
-          s.v2 = make_float3(d.x, d.y, d.z);
-          s.area = edge_fn(a.x, a.y, b.x, b.y, d.x, d.y);
-          shade_face_pixel_t<true>(p.shade, sm.mesh, c, fid, s, tx0 + lx, ty0 + ly, depth, sh);
-        }
+        if (fid > 0)
+          shade_tile_pixel(p.shade, sm.mesh, sm.tex0, c, proj, fid, tx0 + lx, ty0 + ly, depth, sh);
         if (V.color) {
           V.color[3 * pix + 0] = sh.c[0];
           V.color[3 * pix + 1] = sh.c[1];
