@@ -715,7 +715,11 @@ def main():
         views.append(v)
     tuned = ctx.autotune(views) if not args.no_autotune else ctx.tuning()
     tuning = {"path": ["tiled", "global"][tuned.path], "tile": 1 << tuned.tile_log2,
-              "entry_capacity": tuned.entry_capacity}
+              "ctas_per_sm": tuned.ctas_per_sm or "occupancy limit",
+              "split_class": tuned.split_class, "agg_per_face": tuned.agg_per_face,
+              "small_bbox_max": tuned.small_bbox_max, "group_pixels": tuned.group_pixels,
+              "chosen_by": "ugu_gpu_autotune (coordinate search, timed on these views)"
+              if not args.no_autotune else "defaults"}
     plan = ctx.plan_create(views, capi.DEVICE_POINTERS)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define UGU_GPU_ABI_VERSION 3
+#define UGU_GPU_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define UGU_GPU_API __attribute__((visibility("default")))
@@ -254,6 +254,12 @@ typedef struct {
   int32_t small_bbox_max;   /* global: faces with larger bboxes are split by tile */
   int32_t group_pixels;     /* global: pixels of z-buffer kept live per view group */
   int32_t ctas_per_sm;      /* persistent-kernel blocks per SM (0 = occupancy limit) */
+  int32_t split_class;      /* tiled: a draw class of at most this many (face, tile)
+                               entries is shared out evenly over a tile's warps
+                               (0 = 64; 1 = never) */
+  int32_t agg_per_face;     /* tiled binning: faces touching at most this many tiles
+                               rank their entries by warp aggregation, others by
+                               per-tile cursors (1, 2 or 4; 0 = 2) */
 } ugu_gpu_tuning;
 
 enum {
@@ -335,7 +341,14 @@ UGU_GPU_API int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_
 
 UGU_GPU_API int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* tuning);
 UGU_GPU_API int ugu_gpu_get_tuning(const ugu_gpu_context* ctx, ugu_gpu_tuning* tuning);
-/* Time candidate tunings on `views` (device pointers) and keep the fastest. */
+/* Times candidate tunings on the given views (device pointers) and keeps the
+ * fastest: the path and tile size, then the persistent grid's blocks per
+ * SM and the draw and binning thresholds (split_class, agg_per_face), or
+ * the global path's small_bbox_max and group_pixels; every candidate gives
+ * the same images.  The result is cached per workload shape (view sizes,
+ * meshes, options), so a repeated call returns at once; when the
+ * environment variable UGU_GPU_TUNING_CACHE names a file, results are also
+ * read from and appended to it. */
 UGU_GPU_API int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                      ugu_gpu_tuning* chosen);
 

@@ -38,7 +38,7 @@ def test_binding_lists_every_symbol():
 
 
 def test_abi_version(gpu_lib):
-    assert gpu_lib.ugu_gpu_abi_version() == 3
+    assert gpu_lib.ugu_gpu_abi_version() == 4
 
 
 def test_create_without_gpu_fails_cleanly(gpu_lib):

@@ -134,24 +134,29 @@ def test_icosphere7_textured_1080p(ctx, oracle_lib):
     compare(ref, got, "icosphere7")
 
 
-TUNINGS = [  # (path, tile_log2, entry_capacity, small_bbox_max, group_pixels)
-    (capi.PATH_TILED, 5, 0, 256, 1 << 22),
-    (capi.PATH_TILED, 4, 0, 256, 1 << 22),
-    (capi.PATH_TILED, 5, 16, 256, 1 << 22),   # entries overflow: the render is retried
-    (capi.PATH_TILED, 4, 1, 256, 1 << 22),
-    (capi.PATH_GLOBAL, 3, 2048, 0, 1 << 22),  # every face split into tile items
-    (capi.PATH_GLOBAL, 4, 2048, 0, 1 << 22),
-    (capi.PATH_GLOBAL, 5, 2048, 16, 1 << 22),
-    (capi.PATH_GLOBAL, 6, 2048, 1 << 20, 1 << 22),
+TUNINGS = [  # (path, tile_log2, entry_capacity, small_bbox_max, group_pixels, ctas_per_sm,
+             #  split_class, agg_per_face)
+    (capi.PATH_TILED, 5, 0, 256, 1 << 22, 0, 64, 2),
+    (capi.PATH_TILED, 4, 0, 256, 1 << 22, 0, 64, 2),
+    (capi.PATH_TILED, 5, 16, 256, 1 << 22, 0, 64, 2),   # entries overflow: the render is retried
+    (capi.PATH_TILED, 4, 1, 256, 1 << 22, 0, 64, 2),
+    (capi.PATH_TILED, 5, 0, 256, 1 << 22, 6, 1, 1),     # the autotuner's other candidates
+    (capi.PATH_TILED, 5, 0, 256, 1 << 22, 7, 256, 4),
+    (capi.PATH_TILED, 4, 0, 256, 1 << 22, 0, 4096, 4),
+    (capi.PATH_GLOBAL, 3, 2048, 0, 1 << 22, 0, 0, 0),  # every face split into tile items
+    (capi.PATH_GLOBAL, 4, 2048, 0, 1 << 22, 0, 0, 0),
+    (capi.PATH_GLOBAL, 5, 2048, 16, 1 << 22, 0, 0, 0),
+    (capi.PATH_GLOBAL, 6, 2048, 1 << 20, 1 << 22, 0, 0, 0),
 ]
 
 
 def with_tuning(ctx, tup):
-    path, tl, cap, small, gp = tup
-    return capi.Tuning(path, tl, cap, small, gp, 0)
+    return capi.Tuning(*tup)
 
 
-@pytest.mark.parametrize("tup", TUNINGS, ids=[f"p{t[0]}_t{t[1]}_c{t[2]}_s{t[3]}" for t in TUNINGS])
+@pytest.mark.parametrize("tup", TUNINGS,
+                         ids=[f"p{t[0]}_t{t[1]}_c{t[2]}_s{t[3]}_k{t[5]}_sc{t[6]}_a{t[7]}"
+                              for t in TUNINGS])
 def test_tuning_does_not_change_results(ctx, oracle_lib, tup):
     cam = adv.identity_camera(W=200, H=150, f=120.0)
     m = adv.triangle_soup(cam, n_faces=800, seed=9)
@@ -195,7 +200,7 @@ def test_batched_views_two_meshes(ctx, oracle_lib, torch_cuda, flags, path):
     meshes = [m0] * len(cams) + [m1]
     t = ctx.tuning()
     # several view groups on the global path; 16x16 tiles on the tiled one
-    ctx.check(ctx.set_tuning(capi.Tuning(path, 4, 1024, 256, 100_000, 0)))
+    ctx.check(ctx.set_tuning(capi.Tuning(path, 4, 1024, 256, 100_000, 0, 64, 2)))
     try:
         tensors, views = device_views(torch, all_cams, slots)
         rc = ctx.render_views(views, capi.DEVICE_POINTERS | flags)
@@ -329,7 +334,7 @@ def test_mesh_without_faces(ctx, oracle_lib, path):
     assert (ref["face_id"] == -1).all()
     t0 = ctx.tuning()
     ctx.check(ctx.set_tuning(capi.Tuning(path, 4, 0 if path == capi.PATH_TILED else 2048, 256,
-                                         1 << 22, 0)))
+                                         1 << 22, 0, 64, 2)))
     try:
         for _ in range(2):
             rc, got = gpu_render(ctx, m, cam, opt)
@@ -388,7 +393,7 @@ def test_async_overflow_is_reported_at_synchronize(gpu_lib, torch_cuda):
     m = adv._finish(np.array(verts, np.float32), np.array(faces, np.int32))
     c = Context(0)
     try:
-        c.check(c.set_tuning(capi.Tuning(capi.PATH_GLOBAL, 3, 0, 0, 1 << 22, 0)))
+        c.check(c.set_tuning(capi.Tuning(capi.PATH_GLOBAL, 3, 0, 0, 1 << 22, 0, 64, 2)))
         c.check(c.set_mesh(0, m))
         c.check(c.set_option(to_option(adv.option(2, 1, 1, 0, False))))
         tensors, views = device_views(torch, [cam], [0], outputs=("face_id",))
@@ -400,3 +405,39 @@ def test_async_overflow_is_reported_at_synchronize(gpu_lib, torch_cuda):
         assert c.synchronize() == 0
     finally:
         c.close()
+
+
+def test_autotune_caches_per_workload(gpu_lib, oracle_lib, torch_cuda, tmp_path, monkeypatch):
+    """ugu_gpu_autotune picks among path, tile size, blocks per SM and the
+    draw and binning thresholds; its choice renders exactly what the oracle
+    renders, a second call on the same workload shape returns the cached
+    choice, and the choice is appended to UGU_GPU_TUNING_CACHE and read back
+    by a new context."""
+    torch = torch_cuda
+    from gpu_helpers import to_option
+    from ugu_gb300.rasterizer import Context
+    cache = tmp_path / "tuning.txt"
+    monkeypatch.setenv("UGU_GPU_TUNING_CACHE", str(cache))
+    m, cams = _ring(5, 6)
+    opt = adv.option(1, 1, 1, 0, True)
+    fields = [f for f, _ in capi.Tuning._fields_]
+    chosen = []
+    for _ in range(2):
+        c = Context(0)
+        try:
+            c.check(c.set_mesh(0, m))
+            c.check(c.set_option(to_option(opt)))
+            tensors, views = device_views(torch, cams, [0] * len(cams))
+            t1 = c.autotune(views)
+            t2 = c.autotune(views)  # cached
+            assert [getattr(t1, f) for f in fields] == [getattr(t2, f) for f in fields]
+            chosen.append([getattr(t1, f) for f in fields])
+            c.check(c.render_views(views, capi.DEVICE_POINTERS))
+            for i, cam in enumerate(cams):
+                ref, _ = oracle_render(oracle_lib, m, cam, opt)
+                compare(ref, {k: v.cpu().numpy() for k, v in tensors[i].items()}, f"view{i}")
+        finally:
+            c.close()
+    assert chosen[0] == chosen[1]
+    lines = cache.read_text().split("\n")
+    assert len([x for x in lines if x.strip()]) == 1  # the second context read it back

@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -140,6 +142,8 @@ struct ugu_gpu_context {
   // the sticky word (a synchronous render checks and retries on its own)
   bool sticky_on = false;
   uint64_t mesh_generation = 0;  // bumped by every ugu_gpu_set_mesh
+  // ugu_gpu_autotune's results, keyed by workload shape
+  std::map<uint64_t, ugu_gpu_tuning> tuned;
   // set while a UGU_GPU_RAYTRACE render or plan is being prepared and enqueued
   bool raytrace = false;
   // plans created on this context and not destroyed yet (destroyed with it)
@@ -618,6 +622,8 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.tile_log2 = ctx->tuning.tile_log2;
   p.total_tiles = (int32_t)gr.tiles;
   p.max_vertices = gr.max_vertices;
+  p.split_class = ctx->tuning.split_class > 0 ? ctx->tuning.split_class : 64;
+  p.agg_per_face = ctx->tuning.agg_per_face > 0 ? ctx->tuning.agg_per_face : 2;
   p.entry_cap = (int64_t)s.entries_cap;
   p.run_cap = (int64_t)s.runs_cap;
   p.proj = s.proj;
@@ -1082,6 +1088,8 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->tuning.small_bbox_max = 256;
   ctx->tuning.group_pixels = 4 << 20;
   ctx->tuning.ctas_per_sm = 0;
+  ctx->tuning.split_class = 64;
+  ctx->tuning.agg_per_face = 2;
   *out = ctx;
   return UGU_GPU_OK;
 }
@@ -1519,7 +1527,9 @@ int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
   if ((t->path != UGU_GPU_PATH_TILED && t->path != UGU_GPU_PATH_GLOBAL) ||
       (tiled && (t->tile_log2 < 4 || t->tile_log2 > 5)) ||
       (!tiled && (t->tile_log2 < 3 || t->tile_log2 > 6)) || t->entry_capacity < 0 ||
-      t->small_bbox_max < 0 || t->group_pixels < 1 || t->ctas_per_sm < 0)
+      t->small_bbox_max < 0 || t->group_pixels < 1 || t->ctas_per_sm < 0 ||
+      t->split_class < 0 || !(t->agg_per_face == 0 || t->agg_per_face == 1 ||
+                              t->agg_per_face == 2 || t->agg_per_face == 4))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "tuning out of range");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   if (t->tile_log2 != ctx->tuning.tile_log2 || t->entry_capacity != ctx->tuning.entry_capacity) {
@@ -1544,66 +1554,188 @@ int ugu_gpu_get_tuning(const ugu_gpu_context* ctx, ugu_gpu_tuning* t) {
   return UGU_GPU_OK;
 }
 
+namespace {
+
+// What the fastest tuning of a render depends on: the views' sizes and
+// meshes (their face, vertex and texture sizes), the options and the device.
+uint64_t workload_shape(const ugu_gpu_context* ctx, int n, const ugu_gpu_view* views) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const void* p, size_t len) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < len; ++i) h = (h ^ b[i]) * 1099511628211ull;
+  };
+  mix(&n, sizeof(n));
+  mix(&ctx->num_sms, sizeof(ctx->num_sms));
+  mix(&ctx->opt, sizeof(ctx->opt));
+  for (int i = 0; i < n; ++i) {
+    const ugu_gpu_camera& c = views[i].camera;
+    mix(&c.width, sizeof(c.width));
+    mix(&c.height, sizeof(c.height));
+    const DevMesh& m = ctx->meshes[views[i].mesh].dev;
+    const int32_t dims[4] = {m.num_vertices, m.num_faces, ctx->meshes[views[i].mesh].tex0_w,
+                             ctx->meshes[views[i].mesh].tex0_h};
+    mix(dims, sizeof(dims));
+  }
+  return h;
+}
+
+const char* tuning_cache_file() {
+  const char* f = std::getenv("UGU_GPU_TUNING_CACHE");
+  return (f && *f) ? f : nullptr;
+}
+
+// One line per entry: the shape key in hex, then the tuning's nine fields.
+bool read_cached_tuning(uint64_t key, ugu_gpu_tuning* t) {
+  const char* fn = tuning_cache_file();
+  if (!fn) return false;
+  FILE* f = std::fopen(fn, "r");
+  if (!f) return false;
+  bool found = false;
+  unsigned long long k = 0;
+  ugu_gpu_tuning r{};
+  while (std::fscanf(f, "%llx %d %d %d %d %d %d %d %d", &k, &r.path, &r.tile_log2,
+                     &r.entry_capacity, &r.small_bbox_max, &r.group_pixels, &r.ctas_per_sm,
+                     &r.split_class, &r.agg_per_face) == 9)
+    if (k == key) {
+      *t = r;  // the last entry for a key wins
+      found = true;
+    }
+  std::fclose(f);
+  return found;
+}
+
+void write_cached_tuning(uint64_t key, const ugu_gpu_tuning& t) {
+  const char* fn = tuning_cache_file();
+  if (!fn) return;
+  FILE* f = std::fopen(fn, "a");
+  if (!f) return;
+  std::fprintf(f, "%llx %d %d %d %d %d %d %d %d\n", (unsigned long long)key, t.path, t.tile_log2,
+               t.entry_capacity, t.small_bbox_max, t.group_pixels, t.ctas_per_sm, t.split_class,
+               t.agg_per_face);
+  std::fclose(f);
+}
+
+}  // namespace
+
 int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                      ugu_gpu_tuning* chosen) {
   if (!ctx || n <= 0 || !views)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad autotune arguments");
   cudaSetDevice(ctx->device);
+  int rc = validate_views(ctx, n, views);
+  if (rc) return rc;
+  const uint64_t key = workload_shape(ctx, n, views);
+  ugu_gpu_tuning cached{};
+  auto hit = ctx->tuned.find(key);
+  if (hit != ctx->tuned.end() || read_cached_tuning(key, &cached)) {
+    if (hit != ctx->tuned.end()) cached = hit->second;
+    ctx->tuned[key] = cached;
+    if ((rc = ugu_gpu_set_tuning(ctx, &cached))) return rc;
+    if (chosen) *chosen = cached;
+    return UGU_GPU_OK;
+  }
   const ugu_gpu_tuning start = ctx->tuning;
-  // Candidates: the tiled path at both tile sizes and the global path at
-  // its default grouping.
-  std::vector<ugu_gpu_tuning> cands;
-  for (int tl : {4, 5}) {
-    ugu_gpu_tuning t = start;
-    t.path = UGU_GPU_PATH_TILED;
-    t.tile_log2 = tl;
-    t.entry_capacity = 0;
-    t.ctas_per_sm = 0;
-    cands.push_back(t);
-  }
-  {
-    ugu_gpu_tuning t = start;
-    t.path = UGU_GPU_PATH_GLOBAL;
-    t.tile_log2 = 4;
-    t.small_bbox_max = 256;
-    t.group_pixels = 8 << 20;
-    cands.push_back(t);
-  }
   cudaEvent_t e0, e1;
   CK(ctx, cudaEventCreate(&e0), "cudaEventCreate");
   CK(ctx, cudaEventCreate(&e1), "cudaEventCreate");
+  // The median of three timed renders of the views on one candidate, after
+  // an untimed one that sizes its lists; a failed candidate is skipped.
+  auto time_of = [&](const ugu_gpu_tuning& t, float* ms_out) -> int {
+    int r = ugu_gpu_set_tuning(ctx, &t);
+    if (!r) r = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS | UGU_GPU_ASYNC);
+    if (!r) r = ugu_gpu_synchronize(ctx);
+    float ms[3];
+    for (int k = 0; k < 3 && !r; ++k) {
+      cudaEventRecord(e0, ctx->stream);
+      r = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS | UGU_GPU_ASYNC);
+      cudaEventRecord(e1, ctx->stream);
+      if (!r) r = ugu_gpu_synchronize(ctx);
+      ms[k] = 0.0f;
+      cudaEventElapsedTime(&ms[k], e0, e1);
+    }
+    if (r) return r;
+    std::sort(ms, ms + 3);
+    *ms_out = ms[1];
+    return UGU_GPU_OK;
+  };
   float best = 1e30f;
   ugu_gpu_tuning best_t = start;
-  int rc = UGU_GPU_OK;
-  for (const ugu_gpu_tuning& t : cands) {
-    if ((rc = ugu_gpu_set_tuning(ctx, &t))) break;
-    // warm up (allocates the candidate's scratch), then time three renders
-    if ((rc = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS))) break;
+  bool any = false;
+  auto consider = [&](const ugu_gpu_tuning& t) {
     float ms = 0.0f;
-    for (int r = 0; r < 3 && !rc; ++r) {
-      cudaEventRecord(e0, ctx->stream);
-      rc = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS | UGU_GPU_ASYNC);
-      cudaEventRecord(e1, ctx->stream);
-      cudaEventSynchronize(e1);
-      float m = 0.0f;
-      cudaEventElapsedTime(&m, e0, e1);
-      ms += m;
-    }
-    if (rc) break;
-    if (ms < best) {
+    if (time_of(t, &ms) == UGU_GPU_OK && ms < best) {
       best = ms;
       best_t = t;
+      any = true;
+    }
+  };
+  // Stage 1: the path and the tile size, each at its default thresholds.
+  ugu_gpu_tuning base = start;
+  base.entry_capacity = 0;
+  base.ctas_per_sm = 0;
+  base.split_class = 64;
+  base.agg_per_face = 2;
+  base.small_bbox_max = 256;
+  base.group_pixels = 8 << 20;
+  for (int tl : {4, 5}) {
+    ugu_gpu_tuning t = base;
+    t.path = UGU_GPU_PATH_TILED;
+    t.tile_log2 = tl;
+    consider(t);
+  }
+  {
+    ugu_gpu_tuning t = base;
+    t.path = UGU_GPU_PATH_GLOBAL;
+    t.tile_log2 = 4;
+    consider(t);
+  }
+  // Stage 2: each threshold of the chosen path in turn, the others held.
+  if (any && best_t.path == UGU_GPU_PATH_TILED) {
+    const ugu_gpu_tuning s1 = best_t;
+    for (int v : {6, 7}) {
+      ugu_gpu_tuning t = s1;
+      t.ctas_per_sm = v;
+      consider(t);
+    }
+    const ugu_gpu_tuning s2 = best_t;
+    for (int v : {1, 256}) {
+      ugu_gpu_tuning t = s2;
+      t.split_class = v;
+      consider(t);
+    }
+    const ugu_gpu_tuning s3 = best_t;
+    for (int v : {1, 4}) {
+      ugu_gpu_tuning t = s3;
+      t.agg_per_face = v;
+      consider(t);
+    }
+  } else if (any) {
+    const ugu_gpu_tuning s1 = best_t;
+    for (int v : {64, 1024}) {
+      ugu_gpu_tuning t = s1;
+      t.small_bbox_max = v;
+      consider(t);
+    }
+    const ugu_gpu_tuning s2 = best_t;
+    for (int v : {4 << 20, 16 << 20}) {
+      ugu_gpu_tuning t = s2;
+      t.group_pixels = v;
+      consider(t);
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (rc) {
+  if (!any) {
+    const std::string why = ctx->last_error;
     ugu_gpu_set_tuning(ctx, &start);
-    return rc;
+    return set_error(ctx, UGU_GPU_ERR_CUDA, "no candidate tuning rendered: %s", why.c_str());
   }
   rc = ugu_gpu_set_tuning(ctx, &best_t);
+  if (rc) return rc;
+  ctx->tuned[key] = best_t;
+  write_cached_tuning(key, best_t);
   if (chosen) *chosen = best_t;
-  return rc;
+  return UGU_GPU_OK;
 }
 
 int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,

@@ -155,6 +155,8 @@ struct TileParams {
   int32_t tile_log2;
   int32_t total_tiles;
   int32_t max_vertices;
+  int32_t split_class;  // draw classes of at most this many entries are shared over the warps
+  int32_t agg_per_face; // binning: faces touching at most this many tiles aggregate by warp
   int64_t entry_cap;    // entries (and staged entries) the buffers hold
   int64_t run_cap;      // runs the run list holds
   float4* proj;         // projected vertices (x, y, camera z, 0) of every view

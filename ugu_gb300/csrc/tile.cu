@@ -50,12 +50,10 @@ constexpr int kScanThreads = 1024;
 constexpr int kTileThreads = UGU_TILE_THREADS;  // one tile per block
 constexpr int kWarps = kTileThreads / 32;
 constexpr int kChunk = kTileThreads;  // window slots: 32 faces per warp
-constexpr int kSplitClass = 64;  // classes this small are shared out evenly over the warps
 static_assert(kChunk <= 256, "a covered pair packs its face slot in 8 bits");
 constexpr int kMaxTile = 32;     // tile edge <= 32 pixels
 constexpr int kBinFaces = 2;     // faces per binning thread
 constexpr int kAgg = 256;        // distinct tiles a binning block aggregates
-constexpr int kAggPerFace = 2;   // faces touching more tiles take cursor positions
 constexpr int kAggProbes = 8;
 constexpr int kScanItems = 8;    // tile counts per scan thread and round
 constexpr float kU64 = 3.814697265625e-06f;  // 2^-18 = 64 ulp(1)
@@ -193,13 +191,15 @@ __device__ __forceinline__ int find_slot(const BinSmem& sb, int t) {
 // faces.  The block sorts its (face, tile) entries by (tile, class) in
 // shared memory, claims a range of the staging buffer and of the run list
 // with one global atomic each, and writes each (tile, class) group as one
-// run.  Faces touching at most kAggPerFace tiles take their ranks with one
+// run.  Faces touching at most kAggPerFace tiles (a tuning field,
+// TileParams::agg_per_face: 1, 2 or 4) take their ranks with one
 // shared atomic per warp and key; faces touching more take positions from
 // per-group cursors after the fast ones; entries whose tile finds no slot
 // in the table (at most kAggProbes probes) become runs of one.
 #ifndef UGU_BIN_BLOCKS
 #define UGU_BIN_BLOCKS 6
 #endif
+template <int kAggPerFace>
 __global__ void __launch_bounds__(kBinThreads, UGU_BIN_BLOCKS) k_bin(TileParams p) {
   __shared__ BinSmem sb;
   copy_words(sb.view, p.views[blockIdx.y]);
@@ -727,12 +727,12 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
       }
       const int eb = phase ? e1 : e0, ee = phase ? e2 : e1;
       // Each warp takes the class's next entries (32, or a quarter of a
-      // class of at most kSplitClass entries, so that few large faces still
+      // class of at most p.split_class entries, so that few large faces still
       // keep every warp busy), sets them up in its own 32 slots of the window
       // and draws them; warps meet only at the class boundary, so one warp's
       // large faces hold up no other warp.
       const int grab =
-          ee - eb <= kSplitClass ? min(32, max(1, (ee - eb + kWarps - 1) / kWarps)) : 32;
+          ee - eb <= p.split_class ? min(32, max(1, (ee - eb + kWarps - 1) / kWarps)) : 32;
       for (;;) {
         int cs = 0;
         if (lane == 0) cs = atomicAdd(&sm.cursor[phase], grab);
@@ -849,8 +849,15 @@ void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
   if (p.max_vertices > 0)
     k_proj<<<dim3((p.max_vertices + kBinThreads - 1) / kBinThreads, p.num_views), kBinThreads,
              0, s>>>(p);
-  if (max_faces > 0)
-    k_bin<<<dim3((max_faces + kPerBlock - 1) / kPerBlock, p.num_views), kBinThreads, 0, s>>>(p);
+  if (max_faces > 0) {
+    const dim3 grid((max_faces + kPerBlock - 1) / kPerBlock, p.num_views);
+    if (p.agg_per_face == 1)
+      k_bin<1><<<grid, kBinThreads, 0, s>>>(p);
+    else if (p.agg_per_face == 4)
+      k_bin<4><<<grid, kBinThreads, 0, s>>>(p);
+    else
+      k_bin<2><<<grid, kBinThreads, 0, s>>>(p);
+  }
   k_scan<<<1, kScanThreads, 0, s>>>(p);
 }
 
@@ -879,7 +886,7 @@ int tile_kernel_blocks_per_sm() {
 int bin_kernel_blocks_per_sm() {
   static int blocks = 0;
   if (!blocks) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_bin, kBinThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_bin<2>, kBinThreads, 0);
     if (blocks < 1) blocks = 1;
   }
   return blocks;
