@@ -293,6 +293,30 @@ UGU_GPU_API int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int3
                                         const ugu_gpu_texture_option* option,
                                         uint8_t* texture, uint8_t* mask, uint32_t flags);
 
+/* TextureMapping with kGenerateSimpleTriangles
+ * (GenerateSimpleTrianglesTextureAndUv, texture_mapper.cc:347-440): as
+ * ugu_gpu_texture_mapping, but face f is drawn into the triangle
+ * face_target[6 f .. 6 f + 5] (texel coordinates) of the caller's layout
+ * instead of its uv triangle; the layout and the output uv are the host's
+ * (the reference pads with a 3-texel window: padding_kernel 3). */
+UGU_GPU_API int ugu_gpu_texture_mapping_targets(ugu_gpu_context* ctx, int32_t num_faces,
+                                                const float* face_target, int32_t n,
+                                                const ugu_gpu_keyframe* keyframes,
+                                                const int32_t* face_kf, const float* face_tri,
+                                                const ugu_gpu_texture_option* option,
+                                                uint8_t* texture, uint8_t* mask, uint32_t flags);
+
+/* MakeTiledImage (texture_mapper.cc:29-60), the texture of
+ * kGenerateSimpleTile: keyframe image i copied to tile (i % x_tiles,
+ * i / x_tiles) of an RGB8 texture x_tiles images wide and n / x_tiles
+ * high.  Every image must have the first one's size and the n images must
+ * fill whole rows of tiles (the reference writes past its texture
+ * otherwise); UGU_GPU_ERR_INVALID_ARGUMENT else.  Images and texture are
+ * device pointers with UGU_GPU_DEVICE_POINTERS, else host. */
+UGU_GPU_API int ugu_gpu_tile_images(ugu_gpu_context* ctx, int32_t n,
+                                    const ugu_gpu_keyframe* keyframes, int32_t x_tiles,
+                                    uint8_t* texture, uint32_t flags);
+
 /* --- context ------------------------------------------------------------ */
 UGU_GPU_API int ugu_gpu_create(int32_t device, ugu_gpu_context** out);
 UGU_GPU_API int ugu_gpu_destroy(ugu_gpu_context* ctx);

@@ -118,6 +118,13 @@ def load():
         lib.oracle_texture_mapping.argtypes = [C.c_int32, P, P, C.c_int32, P, P, P, P, P,
                                                C.c_int32, C.c_int32, C.c_int32, P, P]
         lib.oracle_texture_mapping.restype = C.c_int
+        lib.oracle_simple_triangles_layout.argtypes = [C.c_int32, P, C.c_int32, C.c_int32, P, P]
+        lib.oracle_simple_triangles_layout.restype = C.c_int
+        lib.oracle_simple_triangles.argtypes = [C.c_int32, C.c_int32, P, P, P, P, P, C.c_int32,
+                                                C.c_int32, P, P, P]
+        lib.oracle_simple_triangles.restype = C.c_int
+        lib.oracle_simple_tile.argtypes = [C.c_int32, P, P, P, P, C.c_int32, P, P, P, P, P]
+        lib.oracle_simple_tile.restype = C.c_int
         lib.oracle_gbuffer.argtypes = [P] * 11
         lib.oracle_gbuffer.restype = C.c_int64
         lib.oracle_test_visibility.argtypes = [P, C.c_int32, P, C.c_int32, P, C.c_int32, P, P,
@@ -319,6 +326,60 @@ def texture_mapping(uv, uv_indices, kf_colors, face_kf, face_tri, tex_w=1024, te
                                     fk.ctypes.data, ft.ctypes.data, tex_w, tex_h,
                                     padding_kernel, tex.ctypes.data, mask.ctypes.data)
     return rc, tex, mask
+
+
+def simple_triangles_layout(face_kf, tex_w, tex_h):
+    """kGenerateSimpleTriangles' layout: (status, target F x 3 x 2, uv F*3 x 2)."""
+    lib = load()
+    fk = np.ascontiguousarray(face_kf, np.int32)
+    target = np.zeros((len(fk), 3, 2), np.float32)
+    uv = np.zeros((3 * len(fk), 2), np.float32)
+    rc = lib.oracle_simple_triangles_layout(len(fk), fk.ctypes.data, tex_w, tex_h,
+                                            target.ctypes.data, uv.ctypes.data)
+    return rc, target, uv
+
+
+def _kf_arrays(kf_colors):
+    cols = [np.ascontiguousarray(c, np.uint8) for c in kf_colors]
+    kw = np.array([c.shape[1] for c in cols], np.int32)
+    kh = np.array([c.shape[0] for c in cols], np.int32)
+    ptrs = (C.c_void_p * max(1, len(cols)))(*[c.ctypes.data for c in cols])
+    return cols, kw, kh, ptrs
+
+
+def simple_triangles(kf_colors, face_kf, face_tri, tex_w, tex_h):
+    """TextureMapping with kGenerateSimpleTriangles: (status, texture, mask,
+    uv F*3 x 2); face_kf[f] indexes kf_colors (-1: none)."""
+    lib = load()
+    cols, kw, kh, ptrs = _kf_arrays(kf_colors)
+    fk = np.ascontiguousarray(face_kf, np.int32)
+    ft = np.ascontiguousarray(face_tri, np.float32)
+    tex = np.zeros((tex_h, tex_w, 3), np.uint8)
+    mask = np.zeros((tex_h, tex_w), np.uint8)
+    uv = np.zeros((3 * len(fk), 2), np.float32)
+    rc = lib.oracle_simple_triangles(len(fk), len(cols), kw.ctypes.data, kh.ctypes.data,
+                                     C.addressof(ptrs), fk.ctypes.data, ft.ctypes.data, tex_w,
+                                     tex_h, tex.ctypes.data, mask.ctypes.data, uv.ctypes.data)
+    return rc, tex, mask, uv
+
+
+def simple_tile(kf_ids, kf_colors, face_kf, face_tri):
+    """TextureMapping with kGenerateSimpleTile: (status, texture, uv F*3 x 2)."""
+    lib = load()
+    cols, kw, kh, ptrs = _kf_arrays(kf_colors)
+    ids = np.ascontiguousarray(kf_ids, np.int32)
+    fk = np.ascontiguousarray(face_kf, np.int32)
+    ft = np.ascontiguousarray(face_tri, np.float32)
+    tiles = np.zeros(2, np.int32)
+    uv = np.zeros((3 * len(fk), 2), np.float32)
+    n = len(cols)
+    xt = max(int(np.sqrt(n)), 1) if n else 1
+    tex = np.zeros(((n // xt) * (kh[0] if n else 0), xt * (kw[0] if n else 0), 3), np.uint8)
+    rc = lib.oracle_simple_tile(n, ids.ctypes.data, kw.ctypes.data, kh.ctypes.data,
+                                C.addressof(ptrs), len(fk), fk.ctypes.data, ft.ctypes.data,
+                                tiles.ctypes.data, tex.ctypes.data if tex.size else None,
+                                uv.ctypes.data)
+    return rc, tex, uv
 
 
 GBUFFER = ("pos_wld", "pos_cam", "normal_wld", "normal_cam", "bary", "uv")

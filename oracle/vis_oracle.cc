@@ -113,23 +113,21 @@ void bilinear3(float x, float y, const uint8_t* img, int32_t cols, int32_t rows,
 
 }  // namespace
 
-extern "C" int oracle_texture_mapping(int32_t num_faces, const float* uv, const int32_t* uv_idx,
-                                      int32_t num_kf, const int32_t* kf_w, const int32_t* kf_h,
-                                      const uint8_t* const* kf_color, const int32_t* face_kf,
-                                      const float* face_tri, int32_t tex_w, int32_t tex_h,
-                                      int32_t padding_kernel, uint8_t* texture, uint8_t* mask) {
-  const size_t n = (size_t)tex_w * tex_h;
-  std::fill(texture, texture + 3 * n, 0);
-  std::fill(mask, mask + n, 0);
+// RasterizeTriangle (texture_mapper.cc:234-292) for every face in order:
+// face f's target triangle (texel coordinates, tx/ty) sampled from its
+// keyframe's image at the same barycentric point of face_tri[f].
+static int draw_faces(int32_t num_faces, const float* target, int32_t num_kf,
+                      const int32_t* kf_w, const int32_t* kf_h, const uint8_t* const* kf_color,
+                      const int32_t* face_kf, const float* face_tri, int32_t tex_w,
+                      int32_t tex_h, uint8_t* texture, uint8_t* mask) {
   for (int32_t f = 0; f < num_faces; ++f) {
     const int32_t k = face_kf[f];
     if (k < 0) continue;
     if (k >= num_kf) return -1;
     float tx[3], ty[3];
     for (int j = 0; j < 3; ++j) {
-      const float* t = uv + 2 * (size_t)uv_idx[3 * (size_t)f + j];
-      tx[j] = t[0] * (float)tex_w - 0.5f;
-      ty[j] = (1.0f - t[1]) * (float)tex_h - 0.5f;
+      tx[j] = target[6 * (size_t)f + 2 * j];
+      ty[j] = target[6 * (size_t)f + 2 * j + 1];
     }
     const float* s = face_tri + 6 * (size_t)f;
     float area = edge(tx[0], ty[0], tx[1], ty[1], tx[2], ty[2]);
@@ -156,8 +154,162 @@ extern "C" int oracle_texture_mapping(int32_t num_faces, const float* uv, const 
         mask[(size_t)y * tex_w + x] = 255;
       }
   }
-  // PaddingSimple: each empty texel away from the border takes the float
-  // mean of the valid texels of its kernel window, read before any fill
+  return 0;
+}
+
+// PaddingSimple (texture_mapper.cc:148-201): each empty texel away from
+// the border takes the float mean of the valid texels of its kernel
+// window, read before any fill.
+static void pad_simple(int32_t tex_w, int32_t tex_h, int32_t padding_kernel, uint8_t* texture,
+                       uint8_t* mask);
+
+// GenerateTextureOnOriginalUv (texture_mapper.cc:294-345): the target
+// triangles from the mesh's uv.
+extern "C" int oracle_texture_mapping(int32_t num_faces, const float* uv, const int32_t* uv_idx,
+                                      int32_t num_kf, const int32_t* kf_w, const int32_t* kf_h,
+                                      const uint8_t* const* kf_color, const int32_t* face_kf,
+                                      const float* face_tri, int32_t tex_w, int32_t tex_h,
+                                      int32_t padding_kernel, uint8_t* texture, uint8_t* mask) {
+  const size_t n = (size_t)tex_w * tex_h;
+  std::fill(texture, texture + 3 * n, 0);
+  std::fill(mask, mask + n, 0);
+  std::vector<float> target(6 * (size_t)std::max(num_faces, 0));
+  for (int32_t f = 0; f < num_faces; ++f)
+    for (int j = 0; j < 3; ++j) {
+      const float* t = uv + 2 * (size_t)uv_idx[3 * (size_t)f + j];
+      target[6 * (size_t)f + 2 * j] = t[0] * (float)tex_w - 0.5f;
+      target[6 * (size_t)f + 2 * j + 1] = (1.0f - t[1]) * (float)tex_h - 0.5f;
+    }
+  if (draw_faces(num_faces, target.data(), num_kf, kf_w, kf_h, kf_color, face_kf, face_tri,
+                 tex_w, tex_h, texture, mask))
+    return -1;
+  pad_simple(tex_w, tex_h, padding_kernel, texture, mask);
+  return 0;
+}
+
+// GenerateSimpleTrianglesTextureAndUv's layout (texture_mapper.cc:347-440):
+// the faces' target triangles (texel coordinates) and uv, zeros for faces
+// without a keyframe; -1 where the reference returns false.
+extern "C" int oracle_simple_triangles_layout(int32_t num_faces, const int32_t* face_kf,
+                                              int32_t tex_w, int32_t tex_h, float* target,
+                                              float* uv) {
+  const int padding_tri = 2;
+  const int rect_num = (num_faces + 1) / 2;
+  std::fill(target, target + 6 * (size_t)num_faces, 0.0f);
+  std::fill(uv, uv + 6 * (size_t)num_faces, 0.0f);
+  if (rect_num == 0) return 0;
+  const int pix_per_rect = tex_h * tex_w / rect_num;
+  if (pix_per_rect < 6) return -1;
+  const int max_rect_edge_len = 100;
+  int sq_len = std::min(static_cast<int>(std::sqrt(pix_per_rect)), max_rect_edge_len);
+  int max_rect_num = (tex_w / (sq_len + 2 + padding_tri)) * (tex_h / (sq_len + 1 + padding_tri));
+  while (max_rect_num < rect_num) {
+    sq_len--;
+    if (sq_len < 3) return -1;
+    max_rect_num = (tex_w / (sq_len + 2 + padding_tri)) * (tex_h / (sq_len + 1 + padding_tri));
+  }
+  const int rect_w = sq_len + 2, rect_h = sq_len + 1;
+  const int rect_w_num = tex_w / (rect_w + padding_tri);
+  for (int i = 0; i < num_faces; ++i) {
+    if (face_kf[i] < 0) continue;
+    const int rect_id = i / 2, rect_x = rect_id % rect_w_num, rect_y = rect_id / rect_w_num;
+    float tx[3], ty[3];
+    if (i % 2 == 0) {
+      const int x0 = (rect_w + padding_tri) * rect_x + 2, x1 = x0 + sq_len - 1;
+      const int y0 = (rect_h + padding_tri) * rect_y, y1 = y0 + sq_len - 1;
+      tx[0] = (float)x0; ty[0] = (float)y0;
+      tx[1] = (float)x1; ty[1] = (float)y0;
+      tx[2] = (float)x1; ty[2] = (float)y1;
+    } else {
+      const int x0 = (rect_w + padding_tri) * rect_x, x1 = x0 + sq_len - 1;
+      const int y0 = (rect_h + padding_tri) * rect_y + 1, y1 = y0 + sq_len - 1;
+      tx[0] = (float)x0; ty[0] = (float)y0;
+      tx[1] = (float)x0; ty[1] = (float)y1;
+      tx[2] = (float)x1; ty[2] = (float)y1;
+    }
+    for (int j = 0; j < 3; ++j) {
+      target[6 * (size_t)i + 2 * j] = tx[j];
+      target[6 * (size_t)i + 2 * j + 1] = ty[j];
+      uv[6 * (size_t)i + 2 * j] = (tx[j] + 0.5f) / tex_w;
+      uv[6 * (size_t)i + 2 * j + 1] = 1.0f - ((ty[j] + 0.5f) / tex_h);
+    }
+  }
+  return 0;
+}
+
+// kGenerateSimpleTriangles end to end: the layout, the faces drawn into it,
+// a 3-texel padding (:430).
+extern "C" int oracle_simple_triangles(int32_t num_faces, int32_t num_kf, const int32_t* kf_w,
+                                       const int32_t* kf_h, const uint8_t* const* kf_color,
+                                       const int32_t* face_kf, const float* face_tri,
+                                       int32_t tex_w, int32_t tex_h, uint8_t* texture,
+                                       uint8_t* mask, float* uv) {
+  const size_t n = (size_t)tex_w * tex_h;
+  std::fill(texture, texture + 3 * n, 0);
+  std::fill(mask, mask + n, 0);
+  std::vector<float> target(6 * (size_t)std::max(num_faces, 0));
+  if (oracle_simple_triangles_layout(num_faces, face_kf, tex_w, tex_h, target.data(), uv))
+    return -1;
+  if (draw_faces(num_faces, target.data(), num_kf, kf_w, kf_h, kf_color, face_kf, face_tri,
+                 tex_w, tex_h, texture, mask))
+    return -1;
+  pad_simple(tex_w, tex_h, 3, texture, mask);
+  return 0;
+}
+
+// GenerateSimpleTileTextureAndUv (texture_mapper.cc:62-146) with
+// MakeTiledImage (:29-60): the keyframe images tiled (int)sqrt(n) wide, and
+// the faces' uv on their keyframe's tile (an unknown keyframe id maps to
+// tile 0); -1 where the images differ in size or do not fill whole rows.
+extern "C" int oracle_simple_tile(int32_t num_kf, const int32_t* kf_id, const int32_t* kf_w,
+                                  const int32_t* kf_h, const uint8_t* const* kf_color,
+                                  int32_t num_faces, const int32_t* face_kf,
+                                  const float* face_tri, int32_t* tiles, uint8_t* texture,
+                                  float* uv) {
+  if (num_kf <= 0) return -1;
+  const int default_x = static_cast<int>(std::sqrt(num_kf));
+  const int x_tile_num = num_kf < default_x ? num_kf : default_x;
+  const int y_tile_num = num_kf / x_tile_num;
+  const int org_w = kf_w[0], org_h = kf_h[0];
+  for (int i = 0; i < num_kf; ++i)
+    if (kf_w[i] != org_w || kf_h[i] != org_h) return -1;
+  if (num_kf % x_tile_num) return -1;
+  tiles[0] = x_tile_num;
+  tiles[1] = y_tile_num;
+  const int tex_w = x_tile_num * org_w, tex_h = y_tile_num * org_h;
+  if (texture)
+    for (int i = 0; i < num_kf; ++i) {
+      const int tpx = (i % x_tile_num) * org_w, tpy = (i / x_tile_num) * org_h;
+      for (int j = 0; j < org_h; ++j)
+        std::copy(kf_color[i] + (size_t)org_w * 3 * j, kf_color[i] + (size_t)org_w * 3 * (j + 1),
+                  texture + ((size_t)(tpy + j) * tex_w + tpx) * 3);
+    }
+  for (int f = 0; f < num_faces; ++f) {
+    float* u = uv + 6 * (size_t)f;
+    if (face_kf[f] < 0) {
+      std::fill(u, u + 6, 0.0f);
+      continue;
+    }
+    int index = 0;  // the first position of the id (emplace keeps it)
+    for (int i = 0; i < num_kf; ++i)
+      if (kf_id[i] == face_kf[f]) {
+        index = i;
+        break;
+      }
+    const int tpx = (index % x_tile_num) * org_w, tpy = (index / x_tile_num) * org_h;
+    for (int j = 0; j < 3; ++j) {
+      const float x = face_tri[6 * (size_t)f + 2 * j] + tpx;
+      const float y = face_tri[6 * (size_t)f + 2 * j + 1] + tpy;
+      u[2 * j] = (x + 0.5f) / tex_w;
+      u[2 * j + 1] = 1.0f - ((y + 0.5f) / tex_h);
+    }
+  }
+  return 0;
+}
+
+static void pad_simple(int32_t tex_w, int32_t tex_h, int32_t padding_kernel, uint8_t* texture,
+                       uint8_t* mask) {
+  const size_t n = (size_t)tex_w * tex_h;
   std::vector<uint8_t> org_t(texture, texture + 3 * n), org_m(mask, mask + n);
   const int32_t hk = padding_kernel / 2;
   for (int32_t j = hk; j < tex_h - hk; ++j)
@@ -177,5 +329,4 @@ extern "C" int oracle_texture_mapping(int32_t num_faces, const float* uv, const 
       mask[p] = 255;
       for (int c = 0; c < 3; ++c) texture[3 * p + c] = f2u8(sum[c] / (float)cnt);
     }
-  return 0;
 }

@@ -1,8 +1,11 @@
-"""TextureMapping on the mesh's own uv (src/texturing/texture_mapper.cc:
-TextureMappingSimple :924-1006 with kUseOriginalMeshUv, RasterizeTriangle
-:234-292, PaddingSimple :148-201) through ugu_gpu_texture_mapping, against
-the oracle's restatement (oracle/vis_oracle.cc: oracle_texture_mapping):
-texture and mask bit for bit.  The face arrays are seeded: uv triangles that
+"""TextureMapping (src/texturing/texture_mapper.cc: TextureMappingSimple
+:924-1006, RasterizeTriangle :234-292, PaddingSimple :148-201) against the
+oracle's restatement (oracle/vis_oracle.cc), texture, mask and uv bit for
+bit, for three uv types: the mesh's own uv (kUseOriginalMeshUv, through
+ugu_gpu_texture_mapping), the tiled keyframe images (kGenerateSimpleTile,
+the reference's default, :62-146, through ugu_gpu_tile_images) and one
+rectangle half per face (kGenerateSimpleTriangles, :347-440, through
+ugu_gpu_texture_mapping_targets).  The face arrays are seeded: uv triangles that
 overlap heavily (a later face overwrites an earlier one), source triangles
 reaching outside their keyframe images, faces without a keyframe."""
 import numpy as np
@@ -70,10 +73,68 @@ def test_best_keyframes_by_criteria():
         vis.best_keyframes(info, 3)
 
 
-def test_texture_mapping_uv_types_not_built_return_false():
+def test_texture_mapping_unbuilt_or_rejected_layouts_return_false():
     m = scenes.icosphere_textured(1, 8)
-    opt = vis.TextureMappingOption()  # kGenerateSimpleTile, the reference's default
-    assert vis.TextureMapping([], vis.VisibilityInfo(m.num_vertices, m.num_faces), m, opt) is False
+    info = vis.VisibilityInfo(m.num_vertices, m.num_faces)
+    charts = vis.TextureMappingOption(uv_type=vis.TexturingOutputUvType.kGenerateSimpleCharts)
+    assert vis.TextureMapping([], info, m, charts) is False
+    tile = vis.TextureMappingOption()  # kGenerateSimpleTile, the reference's default
+    assert vis.TextureMapping([], info, m, tile) is False  # no keyframe to tile
+
+
+@pytest.mark.parametrize("faces,size", [(5, (64, 64)), (1, (16, 16)), (2000, (512, 384)),
+                                        (301, (97, 53)), (40000, (256, 256)), (9, (7, 7)),
+                                        (0, (32, 32)), (3000, (1024, 16))])
+def test_simple_triangles_layout_matches_oracle(oracle_lib, faces, size):
+    """The layout arithmetic of the mirror (ugu_gb300/visibility.py) and of
+    the oracle agree bit for bit, including where the reference returns
+    false (fewer than 6 texels per rectangle, or sq_len under 3)."""
+    rng = np.random.default_rng(faces)
+    face_kf = rng.integers(-1, 3, faces).astype(np.int32)
+    tw, th = size
+    rc, target, uv = oracle_lib.simple_triangles_layout(face_kf, tw, th)
+    lay = vis.simple_triangles_layout(face_kf, tw, th)
+    assert (rc == -1) == (lay is None)
+    if lay is None:
+        return
+    assert np.array_equal(lay[0], target)
+    assert np.array_equal(lay[1].view(np.uint32), uv.view(np.uint32))
+    # visible faces' triangles stay inside the texture and never share a texel
+    cover = np.zeros((th, tw), np.int32)
+    for f in np.flatnonzero(face_kf >= 0):
+        t = target[f]
+        assert t.min() >= 0 and t[:, 0].max() < tw and t[:, 1].max() < th
+        (x0, y0), (x1, y1) = t.min(0).astype(int), t.max(0).astype(int)
+        ys, xs = np.mgrid[y0:y1 + 1, x0:x1 + 1]
+        upper = f % 2 == 0  # the even face: x - x0 >= y - y0 (upper right)
+        inside = (xs - x0) >= (ys - y0) if upper else (xs - x0) <= (ys - y0)
+        cover[ys[inside], xs[inside]] += 1
+    assert cover.max() <= 1
+
+
+def test_simple_tile_layout_matches_oracle(oracle_lib):
+    """The tile layout's uv (each face's projected triangle moved to its
+    keyframe's tile) in the mirror and the oracle, bit for bit; an unknown
+    keyframe id maps to tile 0 and a duplicated id to its first position,
+    as the reference's map does; 5 keyframes (not whole rows of
+    int(sqrt(5)) = 2) or images of two sizes are rejected."""
+    rng = np.random.default_rng(3)
+    imgs = [rng.integers(0, 256, (30, 40, 3)).astype(np.uint8) for _ in range(6)]
+    ids = [7, 3, 9, 3, 12, 1]
+    F = 500
+    face_kf = rng.choice(ids + [-1, 99], F).astype(np.int32)
+    face_tri = rng.uniform(-5, 45, (F, 3, 2)).astype(np.float32)
+    kfs = [vis.Keyframe(i, None, im) for i, im in zip(ids, imgs)]
+    rc, tex, uv = oracle_lib.simple_tile(ids, imgs, face_kf, face_tri)
+    assert rc == 0 and tex.shape == (90, 80, 3)  # 2 x 3 tiles
+    assert np.array_equal(tex[30:60, 40:80], imgs[3])
+    x_tiles, y_tiles, uv2 = vis.simple_tile_layout(kfs, face_kf, face_tri)
+    assert (x_tiles, y_tiles) == (2, 3)
+    assert np.array_equal(uv.view(np.uint32), uv2.view(np.uint32))
+    assert vis.simple_tile_layout(kfs[:5], face_kf, face_tri) is None
+    assert oracle_lib.simple_tile(ids[:5], imgs[:5], face_kf, face_tri)[0] == -1
+    odd = [vis.Keyframe(0, None, imgs[0]), vis.Keyframe(1, None, imgs[1][:, :20])]
+    assert vis.simple_tile_layout(odd, face_kf, face_tri) is None
 
 
 @pytest.mark.gpu
@@ -139,3 +200,92 @@ def test_gpu_texture_mapping_pipeline(gpu_lib, oracle_lib):
     assert np.array_equal(m.texture_mask, want_m)
     assert np.array_equal(m.textures[0], want_t)
     assert list(np.unique(m.material_ids)) == [0]
+
+
+def _descs(imgs):
+    descs = []
+    for k, img in enumerate(imgs):
+        d = capi.KeyframeDesc()
+        d.id = k
+        d.camera = capi.camera_struct(scenes.camera_desc(img.shape[1], img.shape[0], 50.0, 50.0,
+                                                         20.0, 20.0))
+        d.color = img.ctypes.data
+        descs.append(d)
+    return descs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("size", [(256, 192), (512, 512)])
+def test_gpu_simple_triangles_matches_oracle(gpu_lib, oracle_lib, size):
+    """Every visible face drawn into its half-rectangle on the GPU: texture
+    and mask equal the oracle's (seeded faces whose projected triangles reach
+    outside their keyframe images, faces without a keyframe)."""
+    from ugu_gb300.rasterizer import Context
+    _, _, imgs, face_kf, face_tri = overlapping_faces()
+    tw, th = size
+    rc, want_t, want_m, want_uv = oracle_lib.simple_triangles(imgs, face_kf, face_tri, tw, th)
+    assert rc == 0
+    target, uv = vis.simple_triangles_layout(face_kf, tw, th)
+    assert np.array_equal(uv.view(np.uint32), want_uv.view(np.uint32))
+    ctx = Context(0)
+    try:
+        tex = np.zeros((th, tw, 3), np.uint8)
+        mask = np.zeros((th, tw), np.uint8)
+        ctx.check(ctx.texture_mapping_targets(target.reshape(-1, 6), _descs(imgs), face_kf,
+                                              face_tri.reshape(-1, 6),
+                                              capi.TextureOption(tw, th, 3), tex, mask))
+        assert np.array_equal(mask, want_m)
+        assert np.array_equal(tex, want_t)
+        assert (want_m == 255).mean() > 0.2
+    finally:
+        ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("uv_type", [vis.TexturingOutputUvType.kGenerateSimpleTile,
+                                     vis.TexturingOutputUvType.kGenerateSimpleTriangles])
+def test_gpu_texture_mapping_atlas_pipeline(gpu_lib, oracle_lib, uv_type):
+    """VisibilityTester, then TextureMapping with a generated atlas through
+    the mirror: texture and uv equal the oracle's; the re-textured mesh then
+    renders on the GPU bit for bit as the oracle renders it."""
+    from gpu_helpers import compare, gpu_render
+    from test_visibility import keyframes, option
+    from ugu_gb300.rasterizer import Context, RendererCpuOption
+    m = scenes.icosphere_textured(3, 64)
+    base = 10 if uv_type == vis.TexturingOutputUvType.kGenerateSimpleTile else 0
+    kfs = [(base + i, cam, im) for i, (_, cam, im) in enumerate(keyframes(oracle_lib, m, n=4))]
+    vt = vis.VisibilityTester(option())
+    vt.set_data(m.vertices, m.normals, m.vertex_indices)
+    assert vt.PrepareData()
+    info = vis.VisibilityInfo(m.num_vertices, m.num_faces)
+    frames = [vis.Keyframe(kid, cam, im["color"], im["depth"], im["mask"]) for kid, cam, im in kfs]
+    assert vt.Test(info, facewise=False, keyframes=frames)
+    opt = vis.TextureMappingOption(uv_type=uv_type, tex_w=512, tex_h=512)
+    face_kf, face_tri = vis.best_keyframes(info, opt.criteria)
+    assert (face_kf >= 0).mean() > 0.3
+    if uv_type == vis.TexturingOutputUvType.kGenerateSimpleTile:
+        rc, want_t, want_uv = oracle_lib.simple_tile([f.id for f in frames],
+                                                     [f.color for f in frames], face_kf, face_tri)
+        want_m = None
+    else:
+        rc, want_t, want_m, want_uv = oracle_lib.simple_triangles(
+            [f.color for f in frames], face_kf, face_tri, 512, 512)
+    assert rc == 0
+    assert vis.TextureMapping(frames, info, m, opt, ctx=vt._ctx, slot=1)
+    assert np.array_equal(m.textures[0], want_t)
+    assert np.array_equal(m.uv.view(np.uint32), want_uv.view(np.uint32))
+    if want_m is not None:
+        assert np.array_equal(m.texture_mask, want_m)
+    assert list(np.unique(m.material_ids)) == [0]
+    # the atlas in use: render the re-textured mesh
+    ropt = RendererCpuOption(diffuse_color=1, interp=1, shading_normal=1, backface_culling=True)
+    cam = frames[0].camera
+    rc, ref, _ = oracle_lib.render(m, cam, ropt)
+    assert rc == 0
+    ctx = Context(0)
+    try:
+        rc, got = gpu_render(ctx, m, cam, ropt)
+        assert rc == 0, ctx.last_error()
+        compare(ref, got, "atlas render")
+    finally:
+        ctx.close()

@@ -98,7 +98,8 @@ EXPORTS = [
     "ugu_gpu_set_tuning", "ugu_gpu_get_tuning", "ugu_gpu_autotune", "ugu_gpu_get_stats",
     "ugu_gpu_synchronize", "ugu_gpu_set_stream", "ugu_gpu_render_noalloc",
     "ugu_gpu_get_device_mesh", "ugu_gpu_visualize", "ugu_gpu_render_gbuffer",
-    "ugu_gpu_test_visibility", "ugu_gpu_texture_mapping",
+    "ugu_gpu_test_visibility", "ugu_gpu_texture_mapping", "ugu_gpu_texture_mapping_targets",
+    "ugu_gpu_tile_images",
 ]
 
 NOALLOC_MAX_PIXELS = 2097152
@@ -157,6 +158,9 @@ def load(path: str | None = None):
                                             C.c_uint32]
     lib.ugu_gpu_texture_mapping.argtypes = [P, C.c_int32, C.c_int32, P, P, P, P, P, P,
                                             C.c_uint32]
+    lib.ugu_gpu_texture_mapping_targets.argtypes = [P, C.c_int32, P, C.c_int32, P, P, P, P,
+                                                    P, P, C.c_uint32]
+    lib.ugu_gpu_tile_images.argtypes = [P, C.c_int32, P, C.c_int32, P, C.c_uint32]
     for name in EXPORTS:
         if name != "ugu_gpu_last_error":
             getattr(lib, name).restype = C.c_int

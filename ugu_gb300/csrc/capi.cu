@@ -1371,23 +1371,16 @@ int ugu_gpu_plan_destroy(ugu_gpu_plan* plan) {
 
 // TextureMapping with kUseOriginalMeshUv (texture_mapper.cc:924-1006,
 // :294-345); texmap.cu draws the texture.
-int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
-                            const ugu_gpu_keyframe* keyframes, const int32_t* face_kf,
-                            const float* face_tri, const ugu_gpu_texture_option* option,
-                            uint8_t* texture, uint8_t* mask, uint32_t flags) {
-  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
-  cudaSetDevice(ctx->device);
-  if (n < 0 || (n > 0 && !keyframes) || !face_kf || !face_tri || !option || !texture || !mask)
-    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad keyframes, face arrays, option or output");
-  if (option->tex_w <= 0 || option->tex_h <= 0 || option->padding_kernel < 0)
-    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad texture size or padding kernel");
-  if (mesh < 0 || mesh >= kMaxMeshes || !ctx->meshes[mesh].present)
-    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh has not been initialized");
-  MeshSlot& ms = ctx->meshes[mesh];
-  const int F = ms.dev.num_faces;
-  if (!ms.dev.uv || !ms.dev.uvidx)  // :986-993
-    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
-                     "OutputUvType kUseOriginalMeshUv is specified but UV on mesh is invalid");
+namespace {
+
+// The texture of TextureMapping for F faces: target triangles from the
+// mesh slot's uv (uv, uvidx) or given per face (face_target, texel
+// coordinates, host or device as the flags say).
+int texture_mapping_impl(ugu_gpu_context* ctx, int F, const float2* uv, const int4* uvidx,
+                         const float* face_target, int32_t n, const ugu_gpu_keyframe* keyframes,
+                         const int32_t* face_kf, const float* face_tri,
+                         const ugu_gpu_texture_option* option, uint8_t* texture, uint8_t* mask,
+                         uint32_t flags) {
   const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
   for (int k = 0; k < n; ++k)
     if (!keyframes[k].color || keyframes[k].camera.width <= 0 || keyframes[k].camera.height <= 0)
@@ -1405,6 +1398,7 @@ int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
       img_bytes += align256(3 * (size_t)keyframes[k].camera.width * keyframes[k].camera.height);
   const size_t total = align256(sizeof(DevKeyframe) * (size_t)std::max(n, 1)) + img_bytes +
                        (dev ? 0 : align256(4 * (size_t)F) + align256(24 * (size_t)F)) +
+                       (dev || !face_target ? 0 : align256(24 * (size_t)F)) +
                        align256(4 * texels) + align256(3 * texels) + align256(texels) +
                        (dev ? 0 : align256(3 * texels) + align256(texels));
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
@@ -1442,8 +1436,9 @@ int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
                           cudaMemcpyHostToDevice, ctx->stream),
      "cudaMemcpyAsync(keyframes)");
   TexMapParams p{};
-  p.uv = ms.dev.uv;
-  p.uvidx = ms.dev.uvidx;
+  p.uv = uv;
+  p.uvidx = uvidx;
+  p.face_target = face_target;
   p.num_faces = F;
   p.kf = d_kfs;
   p.tex_w = option->tex_w;
@@ -1461,6 +1456,13 @@ int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
        "cudaMemcpyAsync(face triangles)");
     p.face_kf = fk;
     p.face_tri = ft;
+    if (face_target) {
+      float* tt = reinterpret_cast<float*>(take(24 * (size_t)F));
+      CK(ctx, cudaMemcpyAsync(tt, face_target, 24 * (size_t)F, cudaMemcpyHostToDevice,
+                              ctx->stream),
+         "cudaMemcpyAsync(face targets)");
+      p.face_target = tt;
+    }
   }
   p.owner = reinterpret_cast<int32_t*>(take(4 * texels));
   p.tex0 = take(3 * texels);
@@ -1477,6 +1479,87 @@ int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
        "cudaMemcpyAsync(texture mask)");
   }
   CK(ctx, cudaStreamSynchronize(ctx->stream), "texture mapping");
+  return UGU_GPU_OK;
+}
+
+bool texmap_args_ok(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_keyframe* keyframes,
+                    const int32_t* face_kf, const float* face_tri,
+                    const ugu_gpu_texture_option* option, const uint8_t* texture,
+                    const uint8_t* mask) {
+  if (n < 0 || (n > 0 && !keyframes) || !face_kf || !face_tri || !option || !texture || !mask) {
+    set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad keyframes, face arrays, option or output");
+    return false;
+  }
+  if (option->tex_w <= 0 || option->tex_h <= 0 || option->padding_kernel < 0) {
+    set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad texture size or padding kernel");
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
+                            const ugu_gpu_keyframe* keyframes, const int32_t* face_kf,
+                            const float* face_tri, const ugu_gpu_texture_option* option,
+                            uint8_t* texture, uint8_t* mask, uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  cudaSetDevice(ctx->device);
+  if (!texmap_args_ok(ctx, n, keyframes, face_kf, face_tri, option, texture, mask))
+    return UGU_GPU_ERR_INVALID_ARGUMENT;
+  if (mesh < 0 || mesh >= kMaxMeshes || !ctx->meshes[mesh].present)
+    return set_error(ctx, UGU_GPU_ERR_NOT_PREPARED, "mesh has not been initialized");
+  MeshSlot& ms = ctx->meshes[mesh];
+  if (!ms.dev.uv || !ms.dev.uvidx)  // :986-993
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                     "OutputUvType kUseOriginalMeshUv is specified but UV on mesh is invalid");
+  return texture_mapping_impl(ctx, ms.dev.num_faces, ms.dev.uv, ms.dev.uvidx, nullptr, n,
+                              keyframes, face_kf, face_tri, option, texture, mask, flags);
+}
+
+// GenerateSimpleTrianglesTextureAndUv (texture_mapper.cc:347-440): the
+// faces' target triangles come from the caller's layout.
+int ugu_gpu_texture_mapping_targets(ugu_gpu_context* ctx, int32_t num_faces,
+                                    const float* face_target, int32_t n,
+                                    const ugu_gpu_keyframe* keyframes, const int32_t* face_kf,
+                                    const float* face_tri, const ugu_gpu_texture_option* option,
+                                    uint8_t* texture, uint8_t* mask, uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  cudaSetDevice(ctx->device);
+  if (num_faces < 0 || (num_faces > 0 && !face_target))
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad face count or target triangles");
+  if (!texmap_args_ok(ctx, n, keyframes, face_kf, face_tri, option, texture, mask))
+    return UGU_GPU_ERR_INVALID_ARGUMENT;
+  return texture_mapping_impl(ctx, num_faces, nullptr, nullptr, face_target, n, keyframes,
+                              face_kf, face_tri, option, texture, mask, flags);
+}
+
+// MakeTiledImage (texture_mapper.cc:29-60): keyframe image i is copied to
+// tile (i % x_tiles, i / x_tiles) of a texture x_tiles images wide, one
+// two-dimensional copy per keyframe.  Every image must have the first
+// one's size, and the n images must fill whole rows of tiles (elsewhere the
+// reference writes past its texture).
+int ugu_gpu_tile_images(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_keyframe* keyframes,
+                        int32_t x_tiles, uint8_t* texture, uint32_t flags) {
+  if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
+  cudaSetDevice(ctx->device);
+  if (n <= 0 || !keyframes || !texture || x_tiles <= 0 || n % x_tiles != 0)
+    return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                     "tiling needs keyframes that fill whole rows of %d tiles", x_tiles);
+  const int w = keyframes[0].camera.width, h = keyframes[0].camera.height;
+  for (int k = 0; k < n; ++k)
+    if (!keyframes[k].color || keyframes[k].camera.width != w || keyframes[k].camera.height != h)
+      return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
+                       "keyframe %d: every tiled image must have the first one's size", k);
+  const bool dev = (flags & UGU_GPU_DEVICE_POINTERS) != 0;
+  const size_t row = 3 * (size_t)w, pitch = row * (size_t)x_tiles;
+  for (int k = 0; k < n; ++k) {
+    uint8_t* dst = texture + (size_t)(k / x_tiles) * h * pitch + (size_t)(k % x_tiles) * row;
+    CK(ctx, cudaMemcpy2DAsync(dst, pitch, keyframes[k].color, row, row, h,
+                              dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToHost, ctx->stream),
+       "cudaMemcpy2DAsync(tile)");
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "tiling");
   return UGU_GPU_OK;
 }
 

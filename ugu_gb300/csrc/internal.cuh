@@ -233,6 +233,8 @@ void launch_visibility(const VisParams& p, cudaStream_t s);
 struct TexMapParams {
   const float2* uv;
   const int4* uvidx;
+  const float* face_target; // per face: its triangle in texel coordinates, 6 floats, or NULL
+                            // (then it comes from uv and uvidx)
   int num_faces;
   const int32_t* face_kf;   // per face: its keyframe (an index of kf), or -1
   const float* face_tri;    // per face: projected triangle in that keyframe, 6 floats

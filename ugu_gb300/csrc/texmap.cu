@@ -1,6 +1,9 @@
 // texmap.cu -- TextureMapping's texture on the mesh's own uv
 // (src/texturing/texture_mapper.cc: TextureMappingSimple :924-1006 with
-// kUseOriginalMeshUv, GenerateTextureOnOriginalUv :294-345).
+// kUseOriginalMeshUv, GenerateTextureOnOriginalUv :294-345), or on the
+// triangles of a generated layout (kGenerateSimpleTriangles,
+// GenerateSimpleTrianglesTextureAndUv :347-440: the host lays the faces
+// out and passes their target triangles).
 //
 // The reference walks the faces in order and rasterizes each face's uv
 // triangle into the texture (RasterizeTriangle, :234-292), sampling its
@@ -32,9 +35,18 @@ struct UvTri {
 };
 
 __device__ __forceinline__ UvTri uv_tri(const TexMapParams& p, int f) {
+  UvTri t;
+  if (p.face_target) {  // a layout's own triangle (the atlas uv types)
+    const float* q = p.face_target + 6 * (int64_t)f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      t.x[j] = __ldg(&q[2 * j]);
+      t.y[j] = __ldg(&q[2 * j + 1]);
+    }
+    return t;
+  }
   const int4 ti = __ldg(&p.uvidx[f]);
   const int idx[3] = {ti.x, ti.y, ti.z};
-  UvTri t;
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     const float2 u = __ldg(&p.uv[idx[j]]);

@@ -206,6 +206,24 @@ class Context:
                                                 fk.ctypes.data, ft.ctypes.data, C.byref(option),
                                                 texture.ctypes.data, mask.ctypes.data, 0)
 
+    def texture_mapping_targets(self, face_target, kf_descs, face_kf, face_tri, option,
+                                texture: np.ndarray, mask: np.ndarray) -> int:
+        """ugu_gpu_texture_mapping_targets with host buffers: faces drawn into
+        the given target triangles (F x 6 texel coordinates)."""
+        arr = (capi.KeyframeDesc * max(1, len(kf_descs)))(*kf_descs)
+        tg = np.ascontiguousarray(face_target, np.float32)
+        fk = np.ascontiguousarray(face_kf, np.int32)
+        ft = np.ascontiguousarray(face_tri, np.float32)
+        return self.lib.ugu_gpu_texture_mapping_targets(
+            self.h, len(fk), tg.ctypes.data, len(kf_descs), C.addressof(arr), fk.ctypes.data,
+            ft.ctypes.data, C.byref(option), texture.ctypes.data, mask.ctypes.data, 0)
+
+    def tile_images(self, kf_descs, x_tiles: int, texture: np.ndarray) -> int:
+        """ugu_gpu_tile_images with host buffers."""
+        arr = (capi.KeyframeDesc * max(1, len(kf_descs)))(*kf_descs)
+        return self.lib.ugu_gpu_tile_images(self.h, len(kf_descs), C.addressof(arr), int(x_tiles),
+                                            texture.ctypes.data, 0)
+
     def stats(self) -> capi.Stats:
         s = capi.Stats()
         self.check(self.lib.ugu_gpu_get_stats(self.h, C.byref(s)))

@@ -484,23 +484,97 @@ def best_keyframes(info: VisibilityInfo, criteria: int):
     return face_kf, face_tri
 
 
-def TextureMapping(keyframes, info: VisibilityInfo, mesh, option: TextureMappingOption,
-                   ctx: Context | None = None, slot: int = 0) -> bool:
-    """TextureMapping (texture_mapper.cc:1009-1017) with kSimpleProjection and
-    kUseOriginalMeshUv, drawn on the GPU (ugu_gpu_texture_mapping): sets the
-    mesh's one material to the texture and every face's material id to 0,
-    as GenerateTextureOnOriginalUv (:336-343) does; the texture's mask (255
-    where a face or the padding wrote) is left in mesh.texture_mask.  The
-    atlas-generating uv types are not built (False, like an unimplemented
-    type)."""
-    if option.type != 0 or option.uv_type != TexturingOutputUvType.kUseOriginalMeshUv:
-        return False
-    if (mesh.uv is None or len(mesh.uv) == 0 or mesh.uv_indices is None
-            or len(mesh.uv_indices) != len(mesh.vertex_indices)):
-        return False  # :986-993
-    face_kf, face_tri = best_keyframes(info, option.criteria)
-    ctx = ctx or Context(0)
-    ctx.check(ctx.set_mesh(slot, mesh))
+def simple_tile_layout(keyframes, face_kf, face_tri):
+    """GenerateSimpleTileTextureAndUv's layout (texture_mapper.cc:62-146):
+    the keyframe images tiled x_tiles = (int)sqrt(n) wide and n / x_tiles
+    high, and each face's uv: its projected triangle moved to its best
+    keyframe's tile, (x + 0.5) / tex_w and 1 - (y + 0.5) / tex_h, in float.
+    A keyframe id maps to its position in the list (an unknown id to 0, as
+    the reference's std::unordered_map::operator[] does); faces seen by no
+    keyframe get zero uv.  Returns (x_tiles, y_tiles, uv F*3 x 2), or None
+    when the images would not fill whole rows of tiles or differ in size
+    (the reference then writes past its texture)."""
+    n = len(keyframes)
+    if n == 0:
+        return None
+    x_tiles = int(math.sqrt(float(n)))
+    x_tiles = n if n < x_tiles else x_tiles
+    y_tiles = n // x_tiles
+    h, w = keyframes[0].color.shape[:2]
+    if n % x_tiles or any(k.color.shape[:2] != (h, w) for k in keyframes):
+        return None
+    tex_w, tex_h = F32(x_tiles * w), F32(y_tiles * h)
+    index = {}
+    for i, k in enumerate(keyframes):
+        index.setdefault(int(k.id), i)  # std::unordered_map::emplace keeps the first
+    F = len(face_kf)
+    uv = np.zeros((F, 3, 2), F32)
+    for f in range(F):
+        if face_kf[f] < 0:
+            continue
+        i = index.get(int(face_kf[f]), 0)
+        tx, ty = F32((i % x_tiles) * w), F32((i // x_tiles) * h)
+        for j in range(3):
+            x = F32(face_tri[f, j, 0]) + tx
+            y = F32(face_tri[f, j, 1]) + ty
+            uv[f, j, 0] = (x + F32(0.5)) / tex_w
+            uv[f, j, 1] = F32(1.0) - ((y + F32(0.5)) / tex_h)
+    return x_tiles, y_tiles, uv.reshape(-1, 2)
+
+
+def simple_triangles_layout(face_kf, tex_w: int, tex_h: int):
+    """GenerateSimpleTrianglesTextureAndUv's layout (texture_mapper.cc:
+    347-440): faces 2r and 2r + 1 share rectangle r of sq_len + 2 by
+    sq_len + 1 texels (2 texels apart), the largest sq_len <= 100 for which
+    all fit; the even face takes the upper-right triangle shifted right by
+    2, the odd one the lower-left shifted down by 1.  Returns (target
+    triangles F x 3 x 2 in texel coordinates, uv F*3 x 2: (t + 0.5) / size,
+    flipped in y; zeros for faces seen by no keyframe), or None where the
+    reference returns false (fewer than 6 texels per rectangle, sq_len
+    under 3)."""
+    pad = 2
+    F = len(face_kf)
+    rect_num = (F + 1) // 2
+    if rect_num == 0:
+        return np.zeros((0, 3, 2), F32), np.zeros((0, 2), F32)
+    pix_per_rect = tex_h * tex_w // rect_num
+    if pix_per_rect < 6:
+        return None
+    sq_len = min(int(math.sqrt(float(pix_per_rect))), 100)
+
+    def fits(q):
+        return (tex_w // (q + 2 + pad)) * (tex_h // (q + 1 + pad))
+    while fits(sq_len) < rect_num:
+        sq_len -= 1
+        if sq_len < 3:
+            return None
+    rect_w, rect_h = sq_len + 2, sq_len + 1
+    rect_w_num = tex_w // (rect_w + pad)
+    target = np.zeros((F, 3, 2), F32)
+    uv = np.zeros((F, 3, 2), F32)
+    for i in range(F):
+        if face_kf[i] < 0:
+            continue
+        rid = i // 2
+        rx, ry = rid % rect_w_num, rid // rect_w_num
+        if i % 2 == 0:
+            x0 = (rect_w + pad) * rx + 2
+            y0 = (rect_h + pad) * ry
+            x1, y1 = x0 + sq_len - 1, y0 + sq_len - 1
+            t = [(x0, y0), (x1, y0), (x1, y1)]
+        else:
+            x0 = (rect_w + pad) * rx
+            y0 = (rect_h + pad) * ry + 1
+            x1, y1 = x0 + sq_len - 1, y0 + sq_len - 1
+            t = [(x0, y0), (x0, y1), (x1, y1)]
+        for j, (x, y) in enumerate(t):
+            target[i, j] = (x, y)
+            uv[i, j, 0] = (F32(x) + F32(0.5)) / F32(tex_w)
+            uv[i, j, 1] = F32(1.0) - ((F32(y) + F32(0.5)) / F32(tex_h))
+    return target, uv.reshape(-1, 2)
+
+
+def _keyframe_descs(keyframes):
     descs, keep = [], []
     for kf in keyframes:
         d = capi.KeyframeDesc()
@@ -510,6 +584,76 @@ def TextureMapping(keyframes, info: VisibilityInfo, mesh, option: TextureMapping
         keep.append(c)
         d.color = c.ctypes.data
         descs.append(d)
+    return descs, keep
+
+
+def TextureMapping(keyframes, info: VisibilityInfo, mesh, option: TextureMappingOption,
+                   ctx: Context | None = None, slot: int = 0) -> bool:
+    """TextureMapping (texture_mapper.cc:1009-1017) with kSimpleProjection,
+    each face textured from its best keyframe (:924-970), for three uv
+    types:
+      kGenerateSimpleTile (the default): the keyframe images tiled into one
+        texture on the GPU (ugu_gpu_tile_images), the faces' uv moved to
+        their keyframe's tile (simple_tile_layout);
+      kUseOriginalMeshUv: a tex_h x tex_w texture drawn on the GPU on the
+        mesh's own uv (ugu_gpu_texture_mapping), then padded;
+      kGenerateSimpleTriangles: every visible face drawn on the GPU into
+        its own half-rectangle of a tex_h x tex_w texture
+        (simple_triangles_layout, ugu_gpu_texture_mapping_targets), padded
+        with a 3-texel window; new uv and uv indices.
+    Like the reference, it sets the mesh's one material to the texture and
+    every face's material id to 0; the texture's mask (255 where a face or
+    the padding wrote; all 255 for tiles) is left in mesh.texture_mask.
+    kGenerateSimpleCharts is not built (False, like an unimplemented type),
+    and neither is a layout the reference rejects or would overrun."""
+    if option.type != 0 or option.uv_type not in (TexturingOutputUvType.kGenerateSimpleTile,
+                                                  TexturingOutputUvType.kUseOriginalMeshUv,
+                                                  TexturingOutputUvType.kGenerateSimpleTriangles):
+        return False
+    face_kf, face_tri = best_keyframes(info, option.criteria)
+    F = len(mesh.vertex_indices)
+    if option.uv_type == TexturingOutputUvType.kGenerateSimpleTile:
+        lay = simple_tile_layout(keyframes, face_kf, face_tri)
+        if lay is None:
+            return False
+        x_tiles, y_tiles, uv = lay
+        ctx = ctx or Context(0)
+        descs, keep = _keyframe_descs(keyframes)
+        h, w = keyframes[0].color.shape[:2]
+        tex = np.zeros((y_tiles * h, x_tiles * w, 3), np.uint8)
+        ctx.check(ctx.tile_images(descs, x_tiles, tex))
+        mesh.uv = uv
+        mesh.uv_indices = np.arange(3 * F, dtype=np.int32).reshape(-1, 3)
+        mesh.textures = [tex]
+        mesh.textures_f32 = [None]
+        mesh.material_ids = np.zeros(F, np.int32)
+        mesh.texture_mask = np.full(tex.shape[:2], 255, np.uint8)
+        return True
+    if option.uv_type == TexturingOutputUvType.kGenerateSimpleTriangles:
+        lay = simple_triangles_layout(face_kf, int(option.tex_w), int(option.tex_h))
+        if lay is None:
+            return False
+        target, uv = lay
+        ctx = ctx or Context(0)
+        descs, keep = _keyframe_descs(keyframes)
+        tex = np.zeros((option.tex_h, option.tex_w, 3), np.uint8)
+        mask = np.zeros((option.tex_h, option.tex_w), np.uint8)
+        opt = capi.TextureOption(int(option.tex_w), int(option.tex_h), 3)  # :430
+        ctx.check(ctx.texture_mapping_targets(target.reshape(-1, 6), descs, face_kf,
+                                              face_tri.reshape(-1, 6), opt, tex, mask))
+        mesh.uv = uv
+        mesh.uv_indices = np.arange(3 * F, dtype=np.int32).reshape(-1, 3)
+        mesh.textures = [tex]
+        mesh.textures_f32 = [None]
+        mesh.material_ids = np.zeros(F, np.int32)
+        mesh.texture_mask = mask
+        return True
+    if (mesh.uv is None or len(mesh.uv) == 0 or mesh.uv_indices is None
+            or len(mesh.uv_indices) != len(mesh.vertex_indices)):
+        return False  # :986-993
+    ctx = ctx or Context(0)
+    ctx.check(ctx.set_mesh(slot, mesh))
+    descs, keep = _keyframe_descs(keyframes)
     tex = np.zeros((option.tex_h, option.tex_w, 3), np.uint8)
     mask = np.zeros((option.tex_h, option.tex_w), np.uint8)
     opt = capi.TextureOption(int(option.tex_w), int(option.tex_h), int(option.padding_kernel))
