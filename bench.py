@@ -154,7 +154,7 @@ def measured_peak_hbm():
 
 # The sources the tile kernel is compiled from: a committed ncu figure is
 # used only while their content hash equals the one it was measured on.
-TILE_SOURCES = ("tile.cu", "shade.cuh", "span.cuh", "exact.cuh", "internal.cuh")
+TILE_SOURCES = ("tile.cu", "tilecommon.cuh", "shade.cuh", "span.cuh", "exact.cuh", "internal.cuh")
 
 
 def tile_source_hash():
@@ -717,6 +717,7 @@ def main():
     tuning = {"path": ["tiled", "global"][tuned.path], "tile": 1 << tuned.tile_log2,
               "ctas_per_sm": tuned.ctas_per_sm or "occupancy limit",
               "split_class": tuned.split_class, "agg_per_face": tuned.agg_per_face,
+              "small_view_pixels_on_16px_tiles": tuned.small_view_pixels,
               "small_bbox_max": tuned.small_bbox_max, "group_pixels": tuned.group_pixels,
               "chosen_by": "ugu_gpu_autotune (coordinate search, timed on these views)"
               if not args.no_autotune else "defaults"}

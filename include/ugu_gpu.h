@@ -260,6 +260,8 @@ typedef struct {
   int32_t agg_per_face;     /* tiled binning: faces touching at most this many tiles
                                rank their entries by warp aggregation, others by
                                per-tile cursors (1, 2 or 4; 0 = 2) */
+  int32_t small_view_pixels; /* tiled: views of at most this many pixels use 16-pixel
+                               tiles whatever tile_log2 says (0 = none) */
 } ugu_gpu_tuning;
 
 enum {
@@ -366,8 +368,9 @@ UGU_GPU_API int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_
 UGU_GPU_API int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* tuning);
 UGU_GPU_API int ugu_gpu_get_tuning(const ugu_gpu_context* ctx, ugu_gpu_tuning* tuning);
 /* Times candidate tunings on the given views (device pointers) and keeps the
- * fastest: the path and tile size, then the persistent grid's blocks per
- * SM and the draw and binning thresholds (split_class, agg_per_face), or
+ * fastest: the path and tile size, then the size below which views use
+ * 16-pixel tiles, the persistent grid's blocks per SM and the draw and
+ * binning thresholds (split_class, agg_per_face), or
  * the global path's small_bbox_max and group_pixels; every candidate gives
  * the same images.  The result is cached per workload shape (view sizes,
  * meshes, options), so a repeated call returns at once; when the

@@ -143,6 +143,8 @@ TUNINGS = [  # (path, tile_log2, entry_capacity, small_bbox_max, group_pixels, c
     (capi.PATH_TILED, 5, 0, 256, 1 << 22, 6, 1, 1),     # the autotuner's other candidates
     (capi.PATH_TILED, 5, 0, 256, 1 << 22, 7, 256, 4),
     (capi.PATH_TILED, 4, 0, 256, 1 << 22, 0, 4096, 4),
+    (capi.PATH_TILED, 5, 0, 256, 1 << 22, 0, 64, 2, 200 * 150),  # small views: 16-px tiles
+    (capi.PATH_TILED, 5, 0, 256, 1 << 22, 0, 64, 2, 100 * 100),
     (capi.PATH_GLOBAL, 3, 2048, 0, 1 << 22, 0, 0, 0),  # every face split into tile items
     (capi.PATH_GLOBAL, 4, 2048, 0, 1 << 22, 0, 0, 0),
     (capi.PATH_GLOBAL, 5, 2048, 16, 1 << 22, 0, 0, 0),
@@ -156,7 +158,7 @@ def with_tuning(ctx, tup):
 
 @pytest.mark.parametrize("tup", TUNINGS,
                          ids=[f"p{t[0]}_t{t[1]}_c{t[2]}_s{t[3]}_k{t[5]}_sc{t[6]}_a{t[7]}"
-                              for t in TUNINGS])
+                              f"_v{t[8] if len(t) > 8 else 0}" for t in TUNINGS])
 def test_tuning_does_not_change_results(ctx, oracle_lib, tup):
     cam = adv.identity_camera(W=200, H=150, f=120.0)
     m = adv.triangle_soup(cam, n_faces=800, seed=9)
@@ -441,3 +443,30 @@ def test_autotune_caches_per_workload(gpu_lib, oracle_lib, torch_cuda, tmp_path,
     assert chosen[0] == chosen[1]
     lines = cache.read_text().split("\n")
     assert len([x for x in lines if x.strip()]) == 1  # the second context read it back
+
+
+def test_views_on_two_tile_sizes(ctx, oracle_lib, torch_cuda):
+    """One batch whose small views use 16-pixel tiles and whose larger ones
+    use 32-pixel tiles (small_view_pixels): every view bit for bit."""
+    torch = torch_cuda
+    from gpu_helpers import to_option
+    m0, cams = _ring(5, 8)
+    opt = adv.option(1, 1, 1, 0, True)
+    ctx.check(ctx.set_mesh(0, m0))
+    ctx.check(ctx.set_option(to_option(opt)))
+    t0 = ctx.tuning()
+    ctx.check(ctx.set_tuning(capi.Tuning(capi.PATH_TILED, 5, 0, 256, 1 << 22, 0, 64, 2, 320 * 240)))
+    try:
+        assert len({c.width * c.height <= 320 * 240 for c in cams}) == 2
+        tensors, views = device_views(torch, cams, [0] * len(cams))
+        for flags in (capi.DEVICE_POINTERS, capi.DEVICE_POINTERS | capi.PER_VIEW):
+            for t in tensors:
+                for x in t.values():
+                    x.fill_(3)
+            ctx.check(ctx.render_views(views, flags))
+            torch.cuda.synchronize()
+            for i, cam in enumerate(cams):
+                ref, _ = oracle_render(oracle_lib, m0, cam, opt)
+                compare(ref, {k: v.cpu().numpy() for k, v in tensors[i].items()}, f"view{i}")
+    finally:
+        ctx.check(ctx.set_tuning(t0))

@@ -22,7 +22,7 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-fvisibility=hidden", "-I" + os.path.join(ROOT, "include")]
 
-SOURCES = ["capi.cu", "raster.cu", "tile.cu", "backward.cu", "noalloc.cu", "ray.cu", "bvh.cu",
+SOURCES = ["capi.cu", "raster.cu", "tile.cu", "bin.cu", "backward.cu", "noalloc.cu", "ray.cu", "bvh.cu",
            "vis.cu", "texmap.cu"]
 
 

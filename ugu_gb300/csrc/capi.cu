@@ -398,6 +398,14 @@ int64_t tiles_of(const ugu_gpu_camera& c, int tlog) {
   return ((c.width + T - 1) / T) * ((c.height + T - 1) / T);
 }
 
+// The tile edge (log2) of one view on the tiled path: 16 pixels for views
+// of at most small_view_pixels pixels, else the tuning's.
+int view_tile_log2(const ugu_gpu_tuning& t, const ugu_gpu_camera& c) {
+  return t.small_view_pixels > 0 && (int64_t)c.width * c.height <= t.small_view_pixels
+             ? 4
+             : t.tile_log2;
+}
+
 // Views split into launch groups: per view (the baseline), by z-buffer
 // pixels (global path) or all together (tiled path).  Renders into host
 // buffers are cut into groups of at most kHostChunkPixels so that each
@@ -427,7 +435,7 @@ std::vector<Group> make_groups(ugu_gpu_context* ctx, int n, const ugu_gpu_view* 
     cur.max_faces = std::max(cur.max_faces, F);
     cur.max_vertices = std::max(cur.max_vertices, V);
     cur.max_pixels = std::max(cur.max_pixels, px);
-    cur.tiles += tiles_of(views[i].camera, t.tile_log2);
+    cur.tiles += tiles_of(views[i].camera, view_tile_log2(t, views[i].camera));
     cur.ray_tiles = std::max(cur.ray_tiles,
                              (int64_t)((views[i].camera.width + kRayTileW - 1) / kRayTileW) *
                                  ((views[i].camera.height + kRayTileH - 1) / kRayTileH));
@@ -619,7 +627,6 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.num_views = gr.count;
   p.shade = shade_opts(o);
   p.backface_culling = o.backface_culling ? 1 : 0;
-  p.tile_log2 = ctx->tuning.tile_log2;
   p.total_tiles = (int32_t)gr.tiles;
   p.max_vertices = gr.max_vertices;
   p.split_class = ctx->tuning.split_class > 0 ? ctx->tuning.split_class : 64;
@@ -698,7 +705,6 @@ int size_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& group
 void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& groups,
                 const ugu_gpu_view* views, bool device_ptrs) {
   size_t off = 0;
-  const int tlog = ctx->tuning.tile_log2;
   for (const Group& gr : groups) {
     int64_t key_off = 0, tile_base = 0, proj_off = 0;
     for (int i = gr.first; i < gr.first + gr.count; ++i) {
@@ -710,7 +716,9 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
       d.key_offset = key_off;
       int64_t px = (int64_t)v.camera.width * v.camera.height;
       key_off += px;
+      const int tlog = view_tile_log2(ctx->tuning, v.camera);
       const int T = 1 << tlog;
+      d.tile_log2 = tlog;
       d.tiles_x = (v.camera.width + T - 1) / T;
       d.tile_base = (int32_t)tile_base;
       tile_base += tiles_of(v.camera, tlog);
@@ -1090,6 +1098,7 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->tuning.ctas_per_sm = 0;
   ctx->tuning.split_class = 64;
   ctx->tuning.agg_per_face = 2;
+  ctx->tuning.small_view_pixels = 0;
   *out = ctx;
   return UGU_GPU_OK;
 }
@@ -1611,8 +1620,9 @@ int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
       (tiled && (t->tile_log2 < 4 || t->tile_log2 > 5)) ||
       (!tiled && (t->tile_log2 < 3 || t->tile_log2 > 6)) || t->entry_capacity < 0 ||
       t->small_bbox_max < 0 || t->group_pixels < 1 || t->ctas_per_sm < 0 ||
-      t->split_class < 0 || !(t->agg_per_face == 0 || t->agg_per_face == 1 ||
-                              t->agg_per_face == 2 || t->agg_per_face == 4))
+      t->split_class < 0 || t->small_view_pixels < 0 ||
+      !(t->agg_per_face == 0 || t->agg_per_face == 1 || t->agg_per_face == 2 ||
+        t->agg_per_face == 4))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "tuning out of range");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   if (t->tile_log2 != ctx->tuning.tile_log2 || t->entry_capacity != ctx->tuning.entry_capacity) {
@@ -1667,7 +1677,7 @@ const char* tuning_cache_file() {
   return (f && *f) ? f : nullptr;
 }
 
-// One line per entry: the shape key in hex, then the tuning's nine fields.
+// One line per entry: the shape key in hex, then the tuning's ten fields.
 bool read_cached_tuning(uint64_t key, ugu_gpu_tuning* t) {
   const char* fn = tuning_cache_file();
   if (!fn) return false;
@@ -1676,9 +1686,9 @@ bool read_cached_tuning(uint64_t key, ugu_gpu_tuning* t) {
   bool found = false;
   unsigned long long k = 0;
   ugu_gpu_tuning r{};
-  while (std::fscanf(f, "%llx %d %d %d %d %d %d %d %d", &k, &r.path, &r.tile_log2,
+  while (std::fscanf(f, "%llx %d %d %d %d %d %d %d %d %d", &k, &r.path, &r.tile_log2,
                      &r.entry_capacity, &r.small_bbox_max, &r.group_pixels, &r.ctas_per_sm,
-                     &r.split_class, &r.agg_per_face) == 9)
+                     &r.split_class, &r.agg_per_face, &r.small_view_pixels) == 10)
     if (k == key) {
       *t = r;  // the last entry for a key wins
       found = true;
@@ -1692,9 +1702,9 @@ void write_cached_tuning(uint64_t key, const ugu_gpu_tuning& t) {
   if (!fn) return;
   FILE* f = std::fopen(fn, "a");
   if (!f) return;
-  std::fprintf(f, "%llx %d %d %d %d %d %d %d %d\n", (unsigned long long)key, t.path, t.tile_log2,
-               t.entry_capacity, t.small_bbox_max, t.group_pixels, t.ctas_per_sm, t.split_class,
-               t.agg_per_face);
+  std::fprintf(f, "%llx %d %d %d %d %d %d %d %d %d\n", (unsigned long long)key, t.path,
+               t.tile_log2, t.entry_capacity, t.small_bbox_max, t.group_pixels, t.ctas_per_sm,
+               t.split_class, t.agg_per_face, t.small_view_pixels);
   std::fclose(f);
 }
 
@@ -1758,6 +1768,7 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   base.ctas_per_sm = 0;
   base.split_class = 64;
   base.agg_per_face = 2;
+  base.small_view_pixels = 0;
   base.small_bbox_max = 256;
   base.group_pixels = 8 << 20;
   for (int tl : {4, 5}) {
@@ -1774,6 +1785,14 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   }
   // Stage 2: each threshold of the chosen path in turn, the others held.
   if (any && best_t.path == UGU_GPU_PATH_TILED) {
+    if (best_t.tile_log2 == 5) {  // small views on 16-pixel tiles
+      const ugu_gpu_tuning s0 = best_t;
+      for (int v : {320 * 240, 640 * 480, 1280 * 720}) {
+        ugu_gpu_tuning t = s0;
+        t.small_view_pixels = v;
+        consider(t);
+      }
+    }
     const ugu_gpu_tuning s1 = best_t;
     for (int v : {6, 7}) {
       ugu_gpu_tuning t = s1;

@@ -71,7 +71,8 @@ struct DevView {
   int64_t proj_offset; // tiled path: first projected vertex of this view
   int32_t tile_base;   // tiled path: first global tile of this view
   float split_z;       // tiled path: faces wholly deeper than this are drawn last
-  int64_t pad_;
+  int32_t tile_log2;   // tiled path: this view's tile edge is 1 << tile_log2 pixels
+  int32_t pad_;
   uint8_t* color;
   float* depth;
   float* normal;
@@ -152,7 +153,6 @@ struct TileParams {
   int32_t num_views;
   ShadeOpts shade;
   int32_t backface_culling;
-  int32_t tile_log2;
   int32_t total_tiles;
   int32_t max_vertices;
   int32_t split_class;  // draw classes of at most this many entries are shared over the warps
