@@ -716,7 +716,7 @@ def main():
     tuned = ctx.autotune(views) if not args.no_autotune else ctx.tuning()
     tuning = {"path": ["tiled", "global"][tuned.path], "tile": 1 << tuned.tile_log2,
               "ctas_per_sm": tuned.ctas_per_sm or "occupancy limit",
-              "split_class": tuned.split_class, "agg_per_face": tuned.agg_per_face,
+              "split_class": tuned.split_class, "bin_faces_per_thread": tuned.bin_faces,
               "small_view_pixels_on_16px_tiles": tuned.small_view_pixels,
               "small_bbox_max": tuned.small_bbox_max, "group_pixels": tuned.group_pixels,
               "chosen_by": "ugu_gpu_autotune (coordinate search, timed on these views)"

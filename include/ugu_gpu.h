@@ -257,9 +257,8 @@ typedef struct {
   int32_t split_class;      /* tiled: a draw class of at most this many (face, tile)
                                entries is shared out evenly over a tile's warps
                                (0 = 64; 1 = never) */
-  int32_t agg_per_face;     /* tiled binning: faces touching at most this many tiles
-                               rank their entries by warp aggregation, others by
-                               per-tile cursors (1, 2 or 4; 0 = 2) */
+  int32_t bin_faces;        /* tiled binning: faces per thread of the counting and
+                               placing passes (1, 2 or 4; 0 = 2) */
   int32_t small_view_pixels; /* tiled: views of at most this many pixels use 16-pixel
                                tiles whatever tile_log2 says (0 = none) */
 } ugu_gpu_tuning;
@@ -370,7 +369,7 @@ UGU_GPU_API int ugu_gpu_get_tuning(const ugu_gpu_context* ctx, ugu_gpu_tuning* t
 /* Times candidate tunings on the given views (device pointers) and keeps the
  * fastest: the path and tile size, then the size below which views use
  * 16-pixel tiles, the persistent grid's blocks per SM and the draw and
- * binning thresholds (split_class, agg_per_face), or
+ * binning settings (split_class, bin_faces), or
  * the global path's small_bbox_max and group_pixels; every candidate gives
  * the same images.  The result is cached per workload shape (view sizes,
  * meshes, options), so a repeated call returns at once; when the

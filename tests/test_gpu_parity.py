@@ -135,7 +135,7 @@ def test_icosphere7_textured_1080p(ctx, oracle_lib):
 
 
 TUNINGS = [  # (path, tile_log2, entry_capacity, small_bbox_max, group_pixels, ctas_per_sm,
-             #  split_class, agg_per_face)
+             #  split_class, bin_faces[, small_view_pixels])
     (capi.PATH_TILED, 5, 0, 256, 1 << 22, 0, 64, 2),
     (capi.PATH_TILED, 4, 0, 256, 1 << 22, 0, 64, 2),
     (capi.PATH_TILED, 5, 16, 256, 1 << 22, 0, 64, 2),   # entries overflow: the render is retried

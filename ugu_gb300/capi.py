@@ -82,7 +82,7 @@ class Tuning(C.Structure):
     _fields_ = [("path", C.c_int32), ("tile_log2", C.c_int32), ("entry_capacity", C.c_int32),
                 ("small_bbox_max", C.c_int32), ("group_pixels", C.c_int32),
                 ("ctas_per_sm", C.c_int32), ("split_class", C.c_int32),
-                ("agg_per_face", C.c_int32), ("small_view_pixels", C.c_int32)]
+                ("bin_faces", C.c_int32), ("small_view_pixels", C.c_int32)]
 
 
 class Stats(C.Structure):

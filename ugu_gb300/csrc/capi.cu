@@ -66,12 +66,9 @@ struct Scratch {
   // tiled path
   int32_t* tile_count = nullptr;  // 4 arrays: count, offsets (+1), lo cursor, hi cursor
   size_t tiles_cap = 0;
-  int2* entries = nullptr;  // entries_cap in tile order, then entries_cap staged
+  int2* entries = nullptr;  // entries_cap entries in tile order
   size_t entries_cap = 0;
   size_t entries_min = 0;  // capacity asked for by the last overflow
-  int4* runs = nullptr;
-  size_t runs_cap = 0;
-  size_t runs_min = 0;
   float4* proj = nullptr;
   size_t proj_cap = 0;
   TileCounters* tcounters = nullptr;
@@ -207,7 +204,6 @@ void free_scratch(Scratch& s) {
   cudaFree(s.d_out);
   cudaFree(s.tile_count);
   cudaFree(s.entries);
-  cudaFree(s.runs);
   cudaFree(s.proj);
   cudaFree(s.tcounters);
   cudaFreeHost(s.h_tcounters);
@@ -488,19 +484,8 @@ int ensure_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& gro
     cudaFree(s.entries);
     s.entries = nullptr;
     s.entries_cap = 0;
-    CK(ctx, cudaMalloc(&s.entries, 2 * want * sizeof(int2)), "cudaMalloc(tile entries)");
+    CK(ctx, cudaMalloc(&s.entries, want * sizeof(int2)), "cudaMalloc(tile entries)");
     s.entries_cap = want;
-  }
-  // runs: one per (binning block, tile, draw class), one per entry of a face
-  // that touches many tiles
-  const size_t want_runs = std::min<size_t>(s.runs_min ? s.runs_min : faces / 32 + 4096,
-                                            (size_t)INT32_MAX);
-  if (want_runs > s.runs_cap) {
-    cudaFree(s.runs);
-    s.runs = nullptr;
-    s.runs_cap = 0;
-    CK(ctx, cudaMalloc(&s.runs, want_runs * sizeof(int4)), "cudaMalloc(tile runs)");
-    s.runs_cap = want_runs;
   }
   if (groups.size() > s.tcounters_cap) {
     cudaFree(s.tcounters);
@@ -611,12 +596,11 @@ int persistent_grid(ugu_gpu_context* ctx, int blocks_per_sm) {
   return ctx->num_sms * std::max(per_sm, 1);
 }
 
-// Entry and run capacities that hold what a render reported, with room to
-// spare; the next ensure_tiled allocates them.
+// An entry capacity that holds what a render reported, with room to spare;
+// the next ensure_tiled allocates it.
 void want_capacity(Scratch& s, const TileCounters& c) {
-  const size_t e = (size_t)c.total_entries, r = (size_t)c.total_runs;
+  const size_t e = (size_t)c.total_entries;
   s.entries_min = std::max(s.entries_min, e + e / 8 + 4096);
-  s.runs_min = std::max(s.runs_min, r + r / 8 + 4096);
 }
 
 TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) {
@@ -630,17 +614,14 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.total_tiles = (int32_t)gr.tiles;
   p.max_vertices = gr.max_vertices;
   p.split_class = ctx->tuning.split_class > 0 ? ctx->tuning.split_class : 64;
-  p.agg_per_face = ctx->tuning.agg_per_face > 0 ? ctx->tuning.agg_per_face : 2;
+  p.bin_faces = ctx->tuning.bin_faces > 0 ? ctx->tuning.bin_faces : 2;
   p.entry_cap = (int64_t)s.entries_cap;
-  p.run_cap = (int64_t)s.runs_cap;
   p.proj = s.proj;
   p.tile_count = s.tile_count;
   p.tile_off = s.tile_count + s.tiles_cap;
   p.tile_lo = p.tile_off + s.tiles_cap + 1;
   p.tile_hi = p.tile_lo + s.tiles_cap;
   p.entries = s.entries;
-  p.staged = s.entries + s.entries_cap;
-  p.runs = s.runs;
   p.counters = s.tcounters + gi;
   p.sticky = ctx->sticky_on ? ctx->d_sticky : nullptr;
   return p;
@@ -662,7 +643,7 @@ int enqueue_group(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) 
   if (ctx->tuning.path != UGU_GPU_PATH_GLOBAL) {
     TileParams p = tile_params(ctx, s, gr, gi);
     cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream);
-    launch_bin(p, gr.max_faces, ctx->num_sms * 8, ctx->stream);
+    launch_bin(p, gr.max_faces, ctx->stream);
     const bool timed = ctx->time_tile && 2 * (size_t)(gi + 1) <= ctx->tile_events.size();
     if (timed) cudaEventRecord(ctx->tile_events[2 * gi], ctx->stream);
     launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
@@ -1082,7 +1063,6 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->stream = ctx->own_stream;
   // occupancy queries happen here, never inside a stream capture
   tile_kernel_blocks_per_sm();
-  bin_kernel_blocks_per_sm();
   ctx->opt.diffuse_color = 0;
   ctx->opt.interp = 1;
   ctx->opt.shading_normal = 1;
@@ -1097,7 +1077,7 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->tuning.group_pixels = 4 << 20;
   ctx->tuning.ctas_per_sm = 0;
   ctx->tuning.split_class = 64;
-  ctx->tuning.agg_per_face = 2;
+  ctx->tuning.bin_faces = 2;
   ctx->tuning.small_view_pixels = 0;
   *out = ctx;
   return UGU_GPU_OK;
@@ -1621,8 +1601,7 @@ int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
       (!tiled && (t->tile_log2 < 3 || t->tile_log2 > 6)) || t->entry_capacity < 0 ||
       t->small_bbox_max < 0 || t->group_pixels < 1 || t->ctas_per_sm < 0 ||
       t->split_class < 0 || t->small_view_pixels < 0 ||
-      !(t->agg_per_face == 0 || t->agg_per_face == 1 || t->agg_per_face == 2 ||
-        t->agg_per_face == 4))
+      !(t->bin_faces == 0 || t->bin_faces == 1 || t->bin_faces == 2 || t->bin_faces == 4))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "tuning out of range");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   if (t->tile_log2 != ctx->tuning.tile_log2 || t->entry_capacity != ctx->tuning.entry_capacity) {
@@ -1630,12 +1609,10 @@ int ugu_gpu_set_tuning(ugu_gpu_context* ctx, const ugu_gpu_tuning* t) {
     Scratch& s = ctx->scratch;
     cudaFree(s.tile_count);
     cudaFree(s.entries);
-    cudaFree(s.runs);
-    s.tile_count = nullptr;
+      s.tile_count = nullptr;
     s.entries = nullptr;
-    s.runs = nullptr;
-    s.tiles_cap = s.entries_cap = s.runs_cap = 0;
-    s.entries_min = s.runs_min = (size_t)t->entry_capacity;
+    s.tiles_cap = s.entries_cap = 0;
+    s.entries_min = (size_t)t->entry_capacity;
   }
   ctx->tuning = *t;
   return UGU_GPU_OK;
@@ -1688,7 +1665,7 @@ bool read_cached_tuning(uint64_t key, ugu_gpu_tuning* t) {
   ugu_gpu_tuning r{};
   while (std::fscanf(f, "%llx %d %d %d %d %d %d %d %d %d", &k, &r.path, &r.tile_log2,
                      &r.entry_capacity, &r.small_bbox_max, &r.group_pixels, &r.ctas_per_sm,
-                     &r.split_class, &r.agg_per_face, &r.small_view_pixels) == 10)
+                     &r.split_class, &r.bin_faces, &r.small_view_pixels) == 10)
     if (k == key) {
       *t = r;  // the last entry for a key wins
       found = true;
@@ -1704,7 +1681,7 @@ void write_cached_tuning(uint64_t key, const ugu_gpu_tuning& t) {
   if (!f) return;
   std::fprintf(f, "%llx %d %d %d %d %d %d %d %d %d\n", (unsigned long long)key, t.path,
                t.tile_log2, t.entry_capacity, t.small_bbox_max, t.group_pixels, t.ctas_per_sm,
-               t.split_class, t.agg_per_face, t.small_view_pixels);
+               t.split_class, t.bin_faces, t.small_view_pixels);
   std::fclose(f);
 }
 
@@ -1767,7 +1744,7 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   base.entry_capacity = 0;
   base.ctas_per_sm = 0;
   base.split_class = 64;
-  base.agg_per_face = 2;
+  base.bin_faces = 2;
   base.small_view_pixels = 0;
   base.small_bbox_max = 256;
   base.group_pixels = 8 << 20;
@@ -1808,7 +1785,7 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     const ugu_gpu_tuning s3 = best_t;
     for (int v : {1, 4}) {
       ugu_gpu_tuning t = s3;
-      t.agg_per_face = v;
+      t.bin_faces = v;
       consider(t);
     }
   } else if (any) {

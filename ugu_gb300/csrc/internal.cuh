@@ -133,20 +133,19 @@ struct RenderParams {
 // Counters of one tiled render (memset before every launch).
 struct TileCounters {
   unsigned int next_tile;             // work-queue head of k_tile
-  unsigned int invalid;                // runs or entries outside their arrays (a bug)
+  unsigned int invalid;                // entries outside their arrays (a bug)
   unsigned long long special;         // covered samples with unorderable depth
-  unsigned long long dropped;         // entries or runs did not fit (0: none)
+  unsigned long long dropped;         // entries did not fit (0: none)
   unsigned long long total_entries;   // (face, tile) entries of this render
-  unsigned long long total_runs;      // staged runs of this render
 };
 
-// Tiled-path buffers.  k_bin stages the (face, tile) entries as runs, each
-// run the entries of one block for one (tile, draw class); per global tile
-// t, k_gather then copies the entries of the faces drawn first to
-// [tile_off[t], tile_lo[t]) and those drawn last to
-// [tile_lo[t], tile_off[t + 1]).  An entry is (the face's number in the
-// binning order DevMesh::order, bit pattern of a lower bound of every depth
-// the face can produce).
+// Tiled-path buffers.  k_bin_pass counts every tile's (face, tile) entries,
+// k_scan turns the counts into offsets and k_bin_pass places the entries:
+// per global tile t, those of the faces drawn first in [tile_off[t],
+// tile_lo[t]) and those of the faces drawn last in [tile_lo[t],
+// tile_off[t + 1]).  An entry is (the face's number in the binning order
+// DevMesh::order, bit pattern of a lower bound of every depth the face can
+// produce).
 struct TileParams {
   const DevMesh* meshes;
   const DevView* views;
@@ -156,16 +155,13 @@ struct TileParams {
   int32_t total_tiles;
   int32_t max_vertices;
   int32_t split_class;  // draw classes of at most this many entries are shared over the warps
-  int32_t agg_per_face; // binning: faces touching at most this many tiles aggregate by warp
-  int64_t entry_cap;    // entries (and staged entries) the buffers hold
-  int64_t run_cap;      // runs the run list holds
+  int32_t bin_faces;    // binning: faces per thread (1, 2 or 4)
+  int64_t entry_cap;    // entries the entry buffer holds
   float4* proj;         // projected vertices (x, y, camera z, 0) of every view
-  int32_t* tile_count;  // entries per tile (k_bin adds; k_scan reads and zeroes)
+  int32_t* tile_count;  // entries per tile (k_bin_pass adds; k_scan reads and zeroes)
   int32_t* tile_off;    // total_tiles + 1 offsets into entries
   int32_t* tile_lo;     // first-drawn cursor / boundary per tile
   int32_t* tile_hi;     // last-drawn cursor per tile
-  int2* staged;         // entries in k_bin's order
-  int4* runs;           // (tile, draw class, first staged entry, count)
   int2* entries;        // entries in tile order
   TileCounters* counters;
   unsigned long long* sticky;  // as RenderParams::sticky
@@ -278,15 +274,14 @@ void launch_ray(const RayParams& p, int64_t max_tiles, cudaStream_t s);
 void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices, int num_sms,
                      cudaStream_t s);
 
-// Host-side launchers (tile.cu).  launch_bin enqueues projection, binning,
-// the offset scan and the gather (launch_size all but the gather, to learn
-// a render's entry and run counts); launch_tile the per-tile raster and
-// resolve.
-void launch_bin(const TileParams& p, int max_faces, int gather_blocks, cudaStream_t s);
+// Host-side launchers of the tiled path.  launch_bin (bin.cu) enqueues
+// projection, counting, the offset scan and the placing of the entries
+// (launch_size all but the placing, to learn a render's entry count);
+// launch_tile (tile.cu) the per-tile raster and resolve.
+void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
 int tile_kernel_blocks_per_sm();
-int bin_kernel_blocks_per_sm();
 constexpr int kBinKernels = 4;
 
 // Host-side launchers (raster.cu).
