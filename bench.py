@@ -845,6 +845,10 @@ def main():
                    "sample": f"all {len(cams)} views once, largest first, on {threads} host "
                              f"threads ({dt:.2f} s wall); oracle restatement of "
                              "Rasterizer::Render (-O2 -ffp-contract=off)"}
+            # one core, the views in turn, as the reference's serial loops run
+            dt1, _ = oracle_all_views(m, cams, 1)
+            cpu["single_core"] = {"value": len(cams) / dt1, "unit": "views/s", "cores": 1,
+                                  "sample": f"all {len(cams)} views serially ({dt1:.2f} s)"}
         if ref is not None:
             bad = [mismatched_pixels(r, g) for r, g in zip(ref, replay)]
             parity = {"views": len(cams), "mismatched_px": int(sum(bad)),

@@ -7,6 +7,7 @@
 // Each builds a ugu::Mesh and a ugu::PinholeCamera from plain arrays, calls
 // Render, and copies the images out together with the camera floats Render
 // derived.
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -59,12 +60,15 @@ struct ref_option {
 }  // extern "C"
 
 // c2w: 4x4 row-major double.  cam_out: w2c_R[9], w2c_t[3], c2w_R[9] (row-major
-// floats) as Render and the ray table use them.
+// floats) as Render and the ray table use them.  times_ms, when not NULL:
+// Render is called twice on the same camera and the wall times of both calls
+// are stored, the first with the camera's ray table still to be built
+// (PinholeCamera::InitRayTable, camera.h:100-101), the second with it built.
 template <typename Renderer>
 static int render_with(const ref_mesh* m, int width, int height, float fx, float fy, float cx,
                        float cy, const double* c2w, const ref_option* o, unsigned char* color,
                        float* depth, float* normal, unsigned char* mask, int* face_id,
-                       float* cam_out) {
+                       float* cam_out, double* times_ms = nullptr) {
   ugu::set_log_level(ugu::LogLevel::kError);
   auto mesh = std::make_shared<ugu::Mesh>();
   std::vector<Eigen::Vector3f> v(m->num_vertices);
@@ -132,9 +136,15 @@ static int render_with(const ref_mesh* m, int width, int height, float fx, float
   ugu::Image3f n_img;
   ugu::Image1b m_img;
   ugu::Image1i f_img;
-  bool ok = r.Render(color ? &c_img : nullptr, depth ? &d_img : nullptr,
-                     normal ? &n_img : nullptr, mask ? &m_img : nullptr,
-                     face_id ? &f_img : nullptr);
+  bool ok = true;
+  for (int k = 0; k < (times_ms ? 2 : 1) && ok; ++k) {
+    const auto t0 = std::chrono::steady_clock::now();
+    ok = r.Render(color ? &c_img : nullptr, depth ? &d_img : nullptr,
+                  normal ? &n_img : nullptr, mask ? &m_img : nullptr,
+                  face_id ? &f_img : nullptr);
+    const auto t1 = std::chrono::steady_clock::now();
+    if (times_ms) times_ms[k] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  }
   if (!ok) return 1;
   const size_t px = (size_t)width * height;
   if (color) std::memcpy(color, c_img.data, px * 3);
@@ -164,6 +174,16 @@ int ref_render(const ref_mesh* m, int width, int height, float fx, float fy, flo
                float* cam_out) {
   return render_with<ugu::Rasterizer>(m, width, height, fx, fy, cx, cy, c2w, o, color, depth,
                                       normal, mask, face_id, cam_out);
+}
+
+// ref_render, timed: times_ms[0] the first Render on a fresh camera,
+// times_ms[1] a second Render on the same camera.
+int ref_render_timed(const ref_mesh* m, int width, int height, float fx, float fy, float cx,
+                     float cy, const double* c2w, const ref_option* o, unsigned char* color,
+                     float* depth, float* normal, unsigned char* mask, int* face_id,
+                     double* times_ms) {
+  return render_with<ugu::Rasterizer>(m, width, height, fx, fy, cx, cy, c2w, o, color, depth,
+                                      normal, mask, face_id, nullptr, times_ms);
 }
 
 int ref_raytrace(const ref_mesh* m, int width, int height, float fx, float fy, float cx,

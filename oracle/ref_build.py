@@ -1,7 +1,8 @@
 """Build and bind oracle/_ref/libugu_ref.so: the reference's own rasterizer
 sources compiled unmodified against the Eigen-compatible shim (TEST
-INFRASTRUCTURE ONLY).  Only possible where the reference checkout exists;
-everything here returns None / skips elsewhere."""
+INFRASTRUCTURE ONLY).  Only possible where the reference checkout exists
+and $UGU_REFERENCE_DIR names it; everything here returns None / skips
+elsewhere."""
 from __future__ import annotations
 
 import ctypes as C
@@ -11,12 +12,13 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("UGU_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("UGU_REFERENCE_DIR", "")
 LIB = os.path.join(HERE, "_ref", "libugu_ref.so")
 
 
 def available() -> bool:
-    return os.path.exists(os.path.join(REF, "src", "renderer", "cpu", "rasterizer.cc"))
+    return bool(REF) and os.path.exists(os.path.join(REF, "src", "renderer", "cpu",
+                                                     "rasterizer.cc"))
 
 
 def build_if_available() -> str | None:
@@ -54,7 +56,7 @@ def load():
             if build_if_available() is None:
                 return None
         lib = C.CDLL(LIB)
-        for f in (lib.ref_render, lib.ref_raytrace):
+        for f in (lib.ref_render, lib.ref_raytrace, lib.ref_render_timed):
             f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                           C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                           C.c_void_p, C.c_void_p, C.c_void_p]
@@ -70,12 +72,20 @@ def render(mesh, cam, opt):
     return _render(load().ref_render, mesh, cam, opt)
 
 
+def render_timed(mesh, cam, opt):
+    """Render twice on one camera with the reference's Rasterizer.  Returns
+    (rc, images, (first call ms, second call ms)): the first call builds the
+    camera's ray table, the second finds it built."""
+    rc, out, times = _render(load().ref_render_timed, mesh, cam, opt, timed=True)
+    return rc, out, (float(times[0]), float(times[1]))
+
+
 def raytrace(mesh, cam, opt):
     """The same through the reference's Raytracer (naive BVH)."""
     return _render(load().ref_raytrace, mesh, cam, opt)
 
 
-def _render(fn, mesh, cam, opt):
+def _render(fn, mesh, cam, opt, timed=False):
     keep = []
 
     def a(x, dt):
@@ -111,9 +121,12 @@ def _render(fn, mesh, cam, opt):
            "face_id": np.zeros((H, W), np.int32)}
     c2w = np.ascontiguousarray(cam.c2w if cam.c2w is not None else np.eye(4), np.float64)
     camf = np.zeros(21, np.float32)
+    times = np.zeros(2, np.float64)
     rc = fn(C.addressof(m), W, H, cam.fx, cam.fy, cam.cx, cam.cy, c2w.ctypes.data,
                         C.addressof(o), out["color"].ctypes.data, out["depth"].ctypes.data,
                         out["normal"].ctypes.data, out["mask"].ctypes.data,
-                        out["face_id"].ctypes.data, camf.ctypes.data)
+                        out["face_id"].ctypes.data, (times if timed else camf).ctypes.data)
+    if timed:
+        return rc, out, times
     return rc, out, {"w2c_R": camf[0:9].reshape(3, 3).copy(), "w2c_t": camf[9:12].copy(),
                      "c2w_R": camf[12:21].reshape(3, 3).copy()}

@@ -257,7 +257,7 @@ extern "C" int oracle_simple_triangles(int32_t num_faces, int32_t num_kf, const 
   return 0;
 }
 
-// GenerateSimpleTileTextureAndUv (texture_mapper.cc:62-146) with
+// GenerateSimpleTileTextureAndUv (texture_mapper.cc:62-141) with
 // MakeTiledImage (:29-60): the keyframe images tiled (int)sqrt(n) wide, and
 // the faces' uv on their keyframe's tile (an unknown keyframe id maps to
 // tile 0); -1 where the images differ in size or do not fill whole rows.

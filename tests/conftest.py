@@ -6,6 +6,11 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
+# The reference checkout that the pinning and drop-in tests compile from:
+# $UGU_REFERENCE_DIR, else the build machine's checkout when it is there;
+# those tests skip without one.
+if not os.environ.get("UGU_REFERENCE_DIR") and os.path.isdir("/root/reference/src"):
+    os.environ["UGU_REFERENCE_DIR"] = "/root/reference"
 
 
 def pytest_configure(config):

@@ -3,7 +3,7 @@
 oracle's restatement (oracle/vis_oracle.cc), texture, mask and uv bit for
 bit, for three uv types: the mesh's own uv (kUseOriginalMeshUv, through
 ugu_gpu_texture_mapping), the tiled keyframe images (kGenerateSimpleTile,
-the reference's default, :62-146, through ugu_gpu_tile_images) and one
+the reference's default, :62-141, through ugu_gpu_tile_images) and one
 rectangle half per face (kGenerateSimpleTriangles, :347-440, through
 ugu_gpu_texture_mapping_targets).  The face arrays are seeded: uv triangles that
 overlap heavily (a later face overwrites an earlier one), source triangles

@@ -81,36 +81,6 @@ struct alignas(16) ProjHL {
   float iz, pad_[3];
 };
 
-// The pinhole projection of every vertex of one view (blockIdx.y) in
-// double, from the float vertices and camera (camera.h:380-387), split
-// into hi + lo floats.
-__global__ void __launch_bounds__(kThreads) k_proj64(BackwardParams p) {
-  const DevView& V = p.views[blockIdx.y];
-  const DevMesh& M = p.meshes[V.mesh];
-  const int i = blockIdx.x * kThreads + threadIdx.x;
-  if (i >= M.num_vertices) return;
-  const Cam& c = V.cam;
-  const float4 P = __ldg(&M.vertices[i]);
-  double cc[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j)
-    cc[j] = (double)c.R[3 * j] * P.x + (double)c.R[3 * j + 1] * P.y +
-            (double)c.R[3 * j + 2] * P.z + (double)c.t[j];
-  const double iz = 1.0 / cc[2];
-  const double x = (double)c.fx * cc[0] * iz + (double)c.cx;
-  const double y = (double)c.fy * cc[1] * iz + (double)c.cy;
-  ProjHL o;
-  o.xh = (float)x;
-  o.yh = (float)y;
-  o.xl = (float)(x - (double)o.xh);
-  o.yl = (float)(y - (double)o.yh);
-  o.iz = (float)iz;
-  o.pad_[0] = o.pad_[1] = o.pad_[2] = 0.0f;
-  float4* dst = reinterpret_cast<float4*>(reinterpret_cast<ProjHL*>(p.proj64) + V.proj_offset + i);
-  dst[0] = make_float4(o.xh, o.yh, o.xl, o.yl);
-  dst[1] = make_float4(o.iz, 0.0f, 0.0f, 0.0f);
-}
-
 // Error-free transformations (Knuth's TwoSum, and the FMA product error):
 // a + b = s + e and a * b = p + e exactly.  The library is compiled without
 // FMA contraction, so the separate roundings these rely on are kept.
@@ -118,6 +88,81 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   const float bb = s - a;
   e = (a - (s - bb)) + (b - bb);
+}
+
+// Float-float arithmetic (Dekker 1971; Shewchuk 1997): a value is the
+// unevaluated sum hi + lo of two floats with |lo| <= ulp(hi) / 2, about 48
+// significant bits.  Sums use TwoSum, products the FMA product error; a
+// quotient is refined from the float quotient of the high parts by two
+// correction steps against the float-float remainder.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_norm(float s, float e) {  // s + e, renormalised
+  FF r;
+  two_sum(s, e, r.hi, r.lo);
+  return r;
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  return ff_norm(s, e + (a.lo + b.lo));
+}
+
+__device__ __forceinline__ FF ff_prod(float a, float b) {  // exact
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_mul(FF a, float b) {
+  const float p = a.hi * b;
+  return ff_norm(p, fmaf(a.lo, b, fmaf(a.hi, b, -p)));
+}
+
+__device__ __forceinline__ FF ff_sub_mul(FF r, FF b, float q) {  // r - b q
+  const FF bq = ff_mul(b, q);
+  return ff_add(r, {-bq.hi, -bq.lo});
+}
+
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+  const float q1 = a.hi / b.hi;
+  const FF r1 = ff_sub_mul(a, b, q1);
+  const float q2 = r1.hi / b.hi;
+  const FF r2 = ff_sub_mul(r1, b, q2);
+  const float q3 = r2.hi / b.hi;
+  const FF q = ff_norm(q1, q2);
+  return ff_add(q, {q3, 0.0f});
+}
+
+// The pinhole projection of every vertex of one view (blockIdx.y)
+// (camera.h:380-387) from the float vertices and camera, in float-float:
+// the camera coordinates R p + t from exact products, then
+// x = fx x_c / z_c + cx and y likewise, each split into hi + lo floats, and
+// 1 / z_c.  Accurate to a few units of 2^-46 relative, which the hi + lo
+// pair stores; GB300 issues float-float several times faster than FP64.
+__global__ void __launch_bounds__(kThreads) k_proj64(BackwardParams p) {
+  const DevView& V = p.views[blockIdx.y];
+  const DevMesh& M = p.meshes[V.mesh];
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= M.num_vertices) return;
+  const Cam& c = V.cam;
+  const float4 P = __ldg(&M.vertices[i]);
+  FF cc[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    FF acc = ff_prod(c.R[3 * j], P.x);
+    acc = ff_add(acc, ff_prod(c.R[3 * j + 1], P.y));
+    acc = ff_add(acc, ff_prod(c.R[3 * j + 2], P.z));
+    cc[j] = ff_add(acc, {c.t[j], 0.0f});
+  }
+  const FF x = ff_add(ff_div(ff_mul(cc[0], c.fx), cc[2]), {c.cx, 0.0f});
+  const FF y = ff_add(ff_div(ff_mul(cc[1], c.fy), cc[2]), {c.cy, 0.0f});
+  const FF iz = ff_div({1.0f, 0.0f}, cc[2]);
+  float4* dst = reinterpret_cast<float4*>(reinterpret_cast<ProjHL*>(p.proj64) + V.proj_offset + i);
+  dst[0] = make_float4(x.hi, y.hi, x.lo, y.lo);
+  dst[1] = make_float4(iz.hi + iz.lo, 0.0f, 0.0f, 0.0f);
 }
 
 // Texel coordinate base + t (t small: the offset of the pixel's texture

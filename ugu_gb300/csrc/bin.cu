@@ -125,7 +125,7 @@ __device__ __forceinline__ int tile_of(const BinShared& sb, const FaceBins& b, i
 // faces' tiles together; lanes whose current tile (and, when placing, draw
 // class) agree take one atomic between them, made by the lowest of them.
 template <int kFaces, bool kPlace>
-__global__ void __launch_bounds__(kBinThreads) k_bin_pass(TileParams p) {
+__device__ __forceinline__ void bin_pass(const TileParams& p) {
   __shared__ BinShared sb;
   if (kPlace && p.counters->dropped) return;  // entries do not fit: the host retries
   load_bin_view(p, sb);
@@ -159,6 +159,16 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_pass(TileParams p) {
         atomicAdd(&p.counters->invalid, 1u);
     }
   }
+}
+
+template <int kFaces>
+__global__ void __launch_bounds__(kBinThreads) k_count(TileParams p) {
+  bin_pass<kFaces, false>(p);
+}
+
+template <int kFaces>
+__global__ void __launch_bounds__(kBinThreads) k_place(TileParams p) {
+  bin_pass<kFaces, true>(p);
 }
 
 // Exclusive scan of the per-tile counts (one block, kScanItems consecutive
@@ -236,16 +246,23 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
 
 }  // namespace
 
-template <bool kPlace>
-void launch_pass(const TileParams& p, int max_faces, cudaStream_t s) {
+template <int kFaces>
+void launch_pass(const TileParams& p, dim3 grid, bool place, cudaStream_t s) {
+  if (place)
+    k_place<kFaces><<<grid, kBinThreads, 0, s>>>(p);
+  else
+    k_count<kFaces><<<grid, kBinThreads, 0, s>>>(p);
+}
+
+void launch_pass(const TileParams& p, int max_faces, bool place, cudaStream_t s) {
   const int faces = p.bin_faces == 1 || p.bin_faces == 4 ? p.bin_faces : 2;
   const dim3 grid((max_faces + kBinThreads * faces - 1) / (kBinThreads * faces), p.num_views);
   if (faces == 1)
-    k_bin_pass<1, kPlace><<<grid, kBinThreads, 0, s>>>(p);
+    launch_pass<1>(p, grid, place, s);
   else if (faces == 4)
-    k_bin_pass<4, kPlace><<<grid, kBinThreads, 0, s>>>(p);
+    launch_pass<4>(p, grid, place, s);
   else
-    k_bin_pass<2, kPlace><<<grid, kBinThreads, 0, s>>>(p);
+    launch_pass<2>(p, grid, place, s);
 }
 
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
@@ -255,13 +272,13 @@ void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
     k_proj<<<dim3((p.max_vertices + kProjVerts * kBinThreads - 1) / (kProjVerts * kBinThreads),
                   p.num_views),
              kBinThreads, 0, s>>>(p);
-  if (max_faces > 0) launch_pass<false>(p, max_faces, s);
+  if (max_faces > 0) launch_pass(p, max_faces, false, s);
   k_scan<<<1, kScanThreads, 0, s>>>(p);
 }
 
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {
   launch_size(p, max_faces, s);
-  if (max_faces > 0) launch_pass<true>(p, max_faces, s);
+  if (max_faces > 0) launch_pass(p, max_faces, true, s);
 }
 
 }  // namespace ugu_gpu

@@ -139,8 +139,8 @@ struct TileCounters {
   unsigned long long total_entries;   // (face, tile) entries of this render
 };
 
-// Tiled-path buffers.  k_bin_pass counts every tile's (face, tile) entries,
-// k_scan turns the counts into offsets and k_bin_pass places the entries:
+// Tiled-path buffers.  k_count counts every tile's (face, tile) entries,
+// k_scan turns the counts into offsets and k_place places the entries:
 // per global tile t, those of the faces drawn first in [tile_off[t],
 // tile_lo[t]) and those of the faces drawn last in [tile_lo[t],
 // tile_off[t + 1]).  An entry is (the face's number in the binning order
@@ -158,7 +158,7 @@ struct TileParams {
   int32_t bin_faces;    // binning: faces per thread (1, 2 or 4)
   int64_t entry_cap;    // entries the entry buffer holds
   float4* proj;         // projected vertices (x, y, camera z, 0) of every view
-  int32_t* tile_count;  // entries per tile (k_bin_pass adds; k_scan reads and zeroes)
+  int32_t* tile_count;  // entries per tile (k_count adds; k_scan reads and zeroes)
   int32_t* tile_off;    // total_tiles + 1 offsets into entries
   int32_t* tile_lo;     // first-drawn cursor / boundary per tile
   int32_t* tile_hi;     // last-drawn cursor per tile

@@ -9,9 +9,10 @@
 // triangle into the texture (RasterizeTriangle, :234-292), sampling its
 // best keyframe's colour image at the same barycentric point of the face's
 // projected triangle; a later face overwrites an earlier one.  Here:
-//   k_tm_cover  one thread per face: every texel its uv triangle covers
-//               takes the face number by atomicMax, so the last face in
-//               order wins, as in the sequential loop;
+//   k_tm_cover  one warp per face, its lanes over the texels of the face's
+//               box: every texel its uv triangle covers takes the face
+//               number by atomicMax, so the last face in order wins, as in
+//               the sequential loop;
 //   k_tm_fill   one thread per texel: the winning face's weights at the
 //               texel (the same float operations) and the bilinear sample
 //               (BilinearInterpolation, include/ugu/util/image_util.h:156-192);
@@ -72,9 +73,14 @@ __device__ __forceinline__ bool tm_weights(const UvTri& t, float ia, int x, int 
   return !(w[0] < 0.0f || w[1] < 0.0f || w[2] < 0.0f);
 }
 
+// One warp per face (kTmThreads / 32 faces per block); the lanes take the
+// box's texels in row-major order, 32 at a time.
 __global__ void __launch_bounds__(kTmThreads) k_tm_cover(TexMapParams p) {
-  const int f = blockIdx.x * kTmThreads + threadIdx.x;
-  if (f >= p.num_faces || __ldg(&p.face_kf[f]) < 0) return;
+  const int64_t fw = (int64_t)blockIdx.x * (kTmThreads / 32) + threadIdx.x / 32;
+  if (fw >= p.num_faces) return;
+  const int f = (int)fw;
+  if (__ldg(&p.face_kf[f]) < 0) return;
+  const int lane = threadIdx.x & 31;
   const UvTri t = uv_tri(p, f);
   const float ia = inv_area(t);
   // the bounding box: int casts of min - 1 and max + 1, clamped (:245-256)
@@ -83,11 +89,13 @@ __global__ void __launch_bounds__(kTmThreads) k_tm_cover(TexMapParams p) {
   const int x1 = clampi(f2i_sat(fadd(max3_std(t.x[0], t.x[1], t.x[2]), 1.0f)), p.tex_w - 1);
   const int y0 = clampi(f2i_sat(fsub(min3_std(t.y[0], t.y[1], t.y[2]), 1.0f)), p.tex_h - 1);
   const int y1 = clampi(f2i_sat(fadd(max3_std(t.y[0], t.y[1], t.y[2]), 1.0f)), p.tex_h - 1);
-  for (int y = y0; y <= y1; ++y)
-    for (int x = x0; x <= x1; ++x) {
-      float w[3];
-      if (tm_weights(t, ia, x, y, w)) atomicMax(&p.owner[(int64_t)y * p.tex_w + x], f);
-    }
+  const int bw = x1 - x0 + 1;
+  const int64_t n = (int64_t)bw * (y1 - y0 + 1);
+  for (int64_t k = lane; k < n; k += 32) {
+    const int y = y0 + (int)(k / bw), x = x0 + (int)(k % bw);
+    float w[3];
+    if (tm_weights(t, ia, x, y, w)) atomicMax(&p.owner[(int64_t)y * p.tex_w + x], f);
+  }
 }
 
 // BilinearInterpolation<Vec3b>: floor, the lower corner clamped at 0 and
@@ -181,7 +189,8 @@ void launch_texture_mapping(const TexMapParams& p, cudaStream_t s) {
   const int64_t n = (int64_t)p.tex_w * p.tex_h;
   cudaMemsetAsync(p.owner, 0xff, sizeof(int32_t) * (size_t)n, s);  // -1: no face
   if (p.num_faces > 0)
-    k_tm_cover<<<(p.num_faces + kTmThreads - 1) / kTmThreads, kTmThreads, 0, s>>>(p);
+    k_tm_cover<<<(unsigned)(((int64_t)p.num_faces + kTmThreads / 32 - 1) / (kTmThreads / 32)),
+                 kTmThreads, 0, s>>>(p);
   const unsigned blocks = (unsigned)((n + kTmThreads - 1) / kTmThreads);
   k_tm_fill<<<blocks, kTmThreads, 0, s>>>(p);
   k_tm_pad<<<blocks, kTmThreads, 0, s>>>(p);

@@ -339,14 +339,14 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
         if (lane < m) do {  // `continue` leaves the slot empty
           const int2 e = p.entries[cs + lane];
           const float zlb = __int_as_float(e.y);
-          if ((unsigned)e.x >= (unsigned)sm.mesh.num_faces) {  // never for k_bin's entries
+          if ((unsigned)e.x >= (unsigned)sm.mesh.num_faces) {  // never for the binning's entries
             atomicAdd(&p.counters->invalid, 1u);
             continue;
           }
           if (zlb > zmax) continue;  // behind every key of a covered tile: cannot win
           const int f = __ldg(&sm.mesh.order[e.x]);  // the entry holds the binning number
           FaceSetup s;
-          setup_proj(proj, sm.mesh.vidx_morton, e.x, c, s);  // succeeded in k_bin: same arithmetic
+          setup_proj(proj, sm.mesh.vidx_morton, e.x, c, s);  // succeeded in k_count: same arithmetic
           const int bx0 = max(s.x0, tx0), bx1 = min(s.x1, tx0 + tw - 1);
           const int by0 = max(s.y0, ty0), by1 = min(s.y1, ty0 + th - 1);
           const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;

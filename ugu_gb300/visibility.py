@@ -485,7 +485,7 @@ def best_keyframes(info: VisibilityInfo, criteria: int):
 
 
 def simple_tile_layout(keyframes, face_kf, face_tri):
-    """GenerateSimpleTileTextureAndUv's layout (texture_mapper.cc:62-146):
+    """GenerateSimpleTileTextureAndUv's layout (texture_mapper.cc:62-141):
     the keyframe images tiled x_tiles = (int)sqrt(n) wide and n / x_tiles
     high, and each face's uv: its projected triangle moved to its best
     keyframe's tile, (x + 0.5) / tex_w and 1 - (y + 0.5) / tex_h, in float.
