@@ -67,3 +67,16 @@ def test_python_mirror_without_gpu_raises():
     with pytest.raises(capi.GpuError) as e:
         Context(0)
     assert e.value.code == capi.ERR_NO_DEVICE
+
+
+def test_kernel_cases_lists_every_kernel_family():
+    """The profiling cases cover every kernel family of the library, and
+    without a device the runner stops with a message instead of running."""
+    import pytest as _pytest
+    from ugu_gb300 import kernel_cases
+    assert set(kernel_cases.CASES) == {"tiled", "global", "noalloc", "visualize", "gbuffer",
+                                       "visibility", "texmap", "backward", "raytrace"}
+    torch = _pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        with _pytest.raises(SystemExit):
+            kernel_cases.main(["--case", "tiled", "--repeat", "1"])

@@ -29,7 +29,8 @@ using tiled::setup_proj;
 
 constexpr int kBinThreads = 256;
 constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 8;    // tile counts per scan thread and round
+constexpr int kScanItems = 32;   // tile counts per scan thread and round
+constexpr int kScanRound = kScanThreads * kScanItems;
 
 // A lower bound of the depth Loop B computes for the face at any covered
 // pixel: the three edge functions carry rounding errors of at most
@@ -81,8 +82,18 @@ struct BinShared {
   DevMesh mesh;
 };
 
+// Binning blocks run view-fastest: block b takes face block b / num_views of
+// view b % num_views, so that the blocks resident together spread over all
+// views' tiles rather than crowd one view's tile counters with atomics.
+__device__ __forceinline__ int bin_block_view(const TileParams& p) {
+  return (int)(blockIdx.x % (unsigned)p.num_views);
+}
+__device__ __forceinline__ int bin_block_faces(const TileParams& p) {
+  return (int)(blockIdx.x / (unsigned)p.num_views);
+}
+
 __device__ __forceinline__ void load_bin_view(const TileParams& p, BinShared& sb) {
-  copy_words(sb.view, p.views[blockIdx.y]);
+  copy_words(sb.view, p.views[bin_block_view(p)]);
   __syncthreads();
   copy_words(sb.mesh, p.meshes[sb.view.mesh]);
   __syncthreads();
@@ -131,7 +142,7 @@ __device__ __forceinline__ void bin_pass(const TileParams& p) {
   load_bin_view(p, sb);
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
-  const int f0 = blockIdx.x * (kBinThreads * kFaces) + threadIdx.x;
+  const int f0 = bin_block_faces(p) * (kBinThreads * kFaces) + threadIdx.x;
 #pragma unroll
   for (int u = 0; u < kFaces; ++u) {
     const FaceBins b = bin_face(p, sb, f0 + u * kBinThreads);
@@ -173,19 +184,21 @@ __global__ void __launch_bounds__(kBinThreads) k_place(TileParams p) {
 
 // Exclusive scan of the per-tile counts (one block, kScanItems consecutive
 // tiles per thread and round, staged through shared memory so that global
-// accesses coalesce); zeroes the counts for the next render and flags a
-// render whose entries exceed the buffer.
+// accesses coalesce; the staging index skips one word in 33 so that a
+// thread's run of 32 sits in 32 different banks); zeroes the counts for the
+// next render and flags a render whose entries exceed the buffer.
+__device__ __forceinline__ int skew(int i) { return i + (i >> 5); }
+
 __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
-  __shared__ int stage[kScanThreads * kScanItems];
+  extern __shared__ int stage[];  // skew(kScanRound) words
   __shared__ long long warp_sum[kScanThreads / 32];
   const int T = p.total_tiles;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int kRound = kScanThreads * kScanItems;
   long long carry = 0;
-  for (int r0 = 0; r0 < T; r0 += kRound) {
-    for (int i = tid; i < kRound; i += kScanThreads) {
+  for (int r0 = 0; r0 < T; r0 += kScanRound) {
+    for (int i = tid; i < kScanRound; i += kScanThreads) {
       const int t = r0 + i;
-      stage[i] = t < T ? p.tile_count[t] : 0;
+      stage[skew(i)] = t < T ? p.tile_count[t] : 0;
       if (t < T) p.tile_count[t] = 0;
     }
     __syncthreads();
@@ -193,7 +206,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
     long long own = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-      v[k] = stage[tid * kScanItems + k];
+      v[k] = stage[skew(tid * kScanItems + k)];
       own += v[k];
     }
     long long x = own;
@@ -218,15 +231,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
     const long long round_total = warp_sum[kScanThreads / 32 - 1];
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-      stage[tid * kScanItems + k] = (int)run;  // offsets stay below the entry capacity
+      stage[skew(tid * kScanItems + k)] = (int)run;  // offsets stay below the entry capacity
       run += v[k];
     }
     __syncthreads();
-    for (int i = tid; i < kRound; i += kScanThreads) {
+    for (int i = tid; i < kScanRound; i += kScanThreads) {
       const int t = r0 + i;
       if (t >= T) break;
-      const int off = stage[i];
-      const int nxt = i + 1 < kRound ? stage[i + 1] : (int)(carry + round_total);
+      const int off = stage[skew(i)];
+      const int nxt = i + 1 < kScanRound ? stage[skew(i + 1)] : (int)(carry + round_total);
       p.tile_off[t] = off;
       p.tile_lo[t] = off;
       p.tile_hi[t] = nxt;
@@ -244,6 +257,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
   }
 }
 
+constexpr size_t kScanSmem = sizeof(int) * (kScanRound + kScanRound / 32);
+
 }  // namespace
 
 template <int kFaces>
@@ -256,7 +271,8 @@ void launch_pass(const TileParams& p, dim3 grid, bool place, cudaStream_t s) {
 
 void launch_pass(const TileParams& p, int max_faces, bool place, cudaStream_t s) {
   const int faces = p.bin_faces == 1 || p.bin_faces == 4 ? p.bin_faces : 2;
-  const dim3 grid((max_faces + kBinThreads * faces - 1) / (kBinThreads * faces), p.num_views);
+  const dim3 grid((unsigned)(((int64_t)max_faces + kBinThreads * faces - 1) /
+                             (kBinThreads * faces) * p.num_views));
   if (faces == 1)
     launch_pass<1>(p, grid, place, s);
   else if (faces == 4)
@@ -273,7 +289,11 @@ void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
                   p.num_views),
              kBinThreads, 0, s>>>(p);
   if (max_faces > 0) launch_pass(p, max_faces, false, s);
-  k_scan<<<1, kScanThreads, 0, s>>>(p);
+  k_scan<<<1, kScanThreads, kScanSmem, s>>>(p);
+}
+
+void bin_kernels_init() {
+  cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanSmem);
 }
 
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {

@@ -1063,6 +1063,7 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->stream = ctx->own_stream;
   // occupancy queries happen here, never inside a stream capture
   tile_kernel_blocks_per_sm();
+  bin_kernels_init();
   ctx->opt.diffuse_color = 0;
   ctx->opt.interp = 1;
   ctx->opt.shading_normal = 1;

@@ -282,6 +282,9 @@ void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
 int tile_kernel_blocks_per_sm();
+// One-time kernel attributes of the binning kernels (the scan's shared
+// memory); called when a context is created.
+void bin_kernels_init();
 constexpr int kBinKernels = 4;
 
 // Host-side launchers (raster.cu).
