@@ -249,6 +249,37 @@ def oracle_all_views(m, cams, threads, keep=False):
     return time.perf_counter() - t0, (res if keep else None)
 
 
+def fp64_errors(m, cams, outs, threads):
+    """The largest error of the GPU's float outputs against an FP64
+    recomputation of the interpolation at the GPU's own face ids (the
+    oracle's interp_f64), over all views: depth relative, camera-frame
+    normal absolute, and the 8-bit colour's distance from the FP64 colour
+    (truncation included)."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    import oracle
+    opt = option()
+
+    def one(i):
+        o = outs[i]
+        d64, n64, c64 = oracle.interp_f64(m, cams[i], opt, o["face_id"])
+        vis, shaded = o["face_id"] >= 0, o["face_id"] > 0
+        dr = float(np.max(np.abs(o["depth"][vis] - d64[vis]) / d64[vis])) if vis.any() else 0.0
+        na = float(np.max(np.abs(o["normal"][shaded] - n64[shaded]))) if shaded.any() else 0.0
+        ca = (float(np.max(np.abs(o["color"][shaded].astype(np.float64) - c64[shaded])))
+              if shaded.any() else 0.0)
+        return dr, na, ca
+
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        errs = list(ex.map(one, range(len(cams))))
+    return {"views": len(cams), "depth_max_rel": max(e[0] for e in errs),
+            "normal_max_abs": max(e[1] for e in errs),
+            "color_u8_max_abs": max(e[2] for e in errs),
+            "against": "FP64 recomputation of the interpolation at the GPU's face ids"}
+
+
 def view_digest(outs):
     import hashlib
     h = hashlib.blake2b(digest_size=16)
@@ -857,6 +888,7 @@ def main():
                       "checked": "the last timed graph replay",
                       "identical_to_replay": same_as_replay}
             del ref
+            parity["fp64_error"] = fp64_errors(m, cams, replay, threads)
     del replay
 
     peak, peak_kind = measured_peak_hbm()
