@@ -280,6 +280,17 @@ def fp64_errors(m, cams, outs, threads):
             "against": "FP64 recomputation of the interpolation at the GPU's face ids"}
 
 
+def tuning_record(tuned, autotuned):
+    """The bench line's record of a ugu_gpu_tuning."""
+    return {"path": ["tiled", "global"][tuned.path], "tile": 1 << tuned.tile_log2,
+            "ctas_per_sm": tuned.ctas_per_sm or "occupancy limit",
+            "split_class": tuned.split_class, "bin_faces_per_thread": tuned.bin_faces,
+            "small_view_pixels_on_16px_tiles": tuned.small_view_pixels,
+            "small_bbox_max": tuned.small_bbox_max, "group_pixels": tuned.group_pixels,
+            "chosen_by": "ugu_gpu_autotune (coordinate search, timed on these views)"
+            if autotuned else "defaults"}
+
+
 def view_digest(outs):
     import hashlib
     h = hashlib.blake2b(digest_size=16)
@@ -336,6 +347,7 @@ def measure_fwd_bwd(ctx, torch, dev, stream, flush, timed, args, n_views=16, siz
     tgt, tviews = views_for(2, ("color_f32",))
     ctx.check(ctx.render_views(tviews, capi.DEVICE_POINTERS))
     fw, fviews = views_for(1, ("face_id", "color_f32"))
+    tuned = ctx.autotune(fviews) if not args.no_autotune else ctx.tuning()
     plan = ctx.plan_create(fviews, capi.DEVICE_POINTERS)
     gtex = torch.zeros(m.textures_f32[0].size, dtype=torch.float32, device=dev)
     gpos = torch.zeros(3 * m.num_vertices, dtype=torch.float32, device=dev)
@@ -356,7 +368,8 @@ def measure_fwd_bwd(ctx, torch, dev, stream, flush, timed, args, n_views=16, siz
     ms_step = sum(ms) / len(ms)
     return {"views_per_s": n_views / (ms_step / 1e3), "ms_per_step": ms_step,
             "workload": f"icosphere7_tex2048_f32_{n_views}x{size[0]}x{size[1]}",
-            "grads": "texels + vertex positions"}
+            "grads": "texels + vertex positions",
+            "tuning": tuning_record(tuned, not args.no_autotune)}
 
 
 def run_reference(args):
@@ -497,7 +510,7 @@ class _DeviceArray:
                                          "data": (int(ptr), False), "version": 3}
 
 
-def measure_texdescent(warmup, n_views=256, iters=20, lr=0.1):
+def measure_texdescent(warmup, n_views=256, iters=20, lr=0.1, autotune=True):
     """The large forward+backward: icosphere-8 (1,310,720 faces, radial noise
     0.01), a 4096^2 float texture, 256 Fibonacci-sphere cameras at distance
     3, 1280x720, fx = 1000; 20 iterations of texture gradient descent
@@ -546,6 +559,7 @@ def measure_texdescent(warmup, n_views=256, iters=20, lr=0.1):
     grad = torch.zeros_like(tex)
     loss = torch.zeros(n_views, dtype=torch.float32, device=dev)
     fw, fviews = views_for(0, ("face_id", "color_f32"))
+    tuned = ctx.autotune(fviews) if autotune else ctx.tuning()
     plan = ctx.plan_create(fviews, capi.DEVICE_POINTERS)
     tptr = [x["color_f32"].data_ptr() for x in tgt]
     setup_s = time.perf_counter() - t_setup
@@ -599,11 +613,11 @@ def measure_texdescent(warmup, n_views=256, iters=20, lr=0.1):
                    "step": "one graph-replayed forward (face_id + float colour), one "
                            "backward (texel gradient), one texel update per iteration"},
         "loss_iter0": losses[0], "loss_iter20": losses[iters], "loss_curve": losses,
-        "setup_s": setup_s, "clocks": clocks}
+        "setup_s": setup_s, "clocks": clocks, "tuning": tuning_record(tuned, autotune)}
 
 
 def run_texdescent(args):
-    print(json.dumps(measure_texdescent(args.warmup)), flush=True)
+    print(json.dumps(measure_texdescent(args.warmup, autotune=not args.no_autotune)), flush=True)
 
 
 def run_raytrace(args):
@@ -745,13 +759,7 @@ def main():
         outs.append(t)
         views.append(v)
     tuned = ctx.autotune(views) if not args.no_autotune else ctx.tuning()
-    tuning = {"path": ["tiled", "global"][tuned.path], "tile": 1 << tuned.tile_log2,
-              "ctas_per_sm": tuned.ctas_per_sm or "occupancy limit",
-              "split_class": tuned.split_class, "bin_faces_per_thread": tuned.bin_faces,
-              "small_view_pixels_on_16px_tiles": tuned.small_view_pixels,
-              "small_bbox_max": tuned.small_bbox_max, "group_pixels": tuned.group_pixels,
-              "chosen_by": "ugu_gpu_autotune (coordinate search, timed on these views)"
-              if not args.no_autotune else "defaults"}
+    tuning = tuning_record(tuned, not args.no_autotune)
     plan = ctx.plan_create(views, capi.DEVICE_POINTERS)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
@@ -936,7 +944,7 @@ def main():
         line["extra"] = {
             "c1_uvsphere_640x480": measure_single("uvsphere", args.steps, args.warmup),
             "c2_icosphere7_1920x1080": measure_single("single1080", args.steps, args.warmup),
-            "c5_texdescent256": measure_texdescent(args.warmup),
+            "c5_texdescent256": measure_texdescent(args.warmup, autotune=not args.no_autotune),
         }
     if rank == 0:
         print(json.dumps(line), flush=True)
