@@ -436,9 +436,8 @@ UGU_GPU_API int ugu_gpu_set_stream(ugu_gpu_context* ctx, void* stream);
  * whenever the mesh has faces: the reference's z pass reads them at every
  * pixel of every face (rasterizer.cc:199).  The first call on a device
  * looks up the array's device address for that device and keeps it for the
- * life of the process; make that first call before any stream capture, and
- * do not cudaDeviceReset a device while this library is in use there (the
- * kept address would be stale).  All calls share the array and it keeps
+ * life of the process; do not cudaDeviceReset a device while this library
+ * is in use there (the kept address would be stale).  All calls share the array and it keeps
  * the last call's contents (each call clears what it needs first), so
  * calls whose GPU work overlaps -- on different streams or from different
  * host threads -- race and must be serialised by the caller.  Runs on the

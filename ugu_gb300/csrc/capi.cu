@@ -1709,14 +1709,16 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   cudaEvent_t e0, e1;
   CK(ctx, cudaEventCreate(&e0), "cudaEventCreate");
   CK(ctx, cudaEventCreate(&e1), "cudaEventCreate");
-  // The median of three timed renders of the views on one candidate, after
+  // The median of five timed renders of the views on one candidate, after
   // an untimed one that sizes its lists; a failed candidate is skipped.
+  // (Candidates often differ by about 1 %, within the spread of three.)
+  constexpr int kTimed = 5;
   auto time_of = [&](const ugu_gpu_tuning& t, float* ms_out) -> int {
     int r = ugu_gpu_set_tuning(ctx, &t);
     if (!r) r = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS | UGU_GPU_ASYNC);
     if (!r) r = ugu_gpu_synchronize(ctx);
-    float ms[3];
-    for (int k = 0; k < 3 && !r; ++k) {
+    float ms[kTimed];
+    for (int k = 0; k < kTimed && !r; ++k) {
       cudaEventRecord(e0, ctx->stream);
       r = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS | UGU_GPU_ASYNC);
       cudaEventRecord(e1, ctx->stream);
@@ -1725,8 +1727,8 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
       cudaEventElapsedTime(&ms[k], e0, e1);
     }
     if (r) return r;
-    std::sort(ms, ms + 3);
-    *ms_out = ms[1];
+    std::sort(ms, ms + kTimed);
+    *ms_out = ms[kTimed / 2];
     return UGU_GPU_OK;
   };
   float best = 1e30f;
