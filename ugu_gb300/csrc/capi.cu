@@ -17,10 +17,26 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "internal.cuh"
 #include "ugu_gpu.h"
 
 using namespace ugu_gpu;
+
+namespace {
+
+// An NVTX range over a scope (NVTX 3 is header-only: without a tool attached
+// the calls return at once).  Profilers group the kernels an entry point
+// launches under its range, e.g. `ncu --nvtx --nvtx-include "ugu_gpu tile/"`.
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
+
+}  // namespace
 
 namespace {
 
@@ -643,10 +659,16 @@ int enqueue_group(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t gi) 
   if (ctx->tuning.path != UGU_GPU_PATH_GLOBAL) {
     TileParams p = tile_params(ctx, s, gr, gi);
     cudaMemsetAsync(p.counters, 0, sizeof(TileCounters), ctx->stream);
-    launch_bin(p, gr.max_faces, ctx->stream);
+    {
+      Range r("ugu_gpu bin");
+      launch_bin(p, gr.max_faces, ctx->stream);
+    }
     const bool timed = ctx->time_tile && 2 * (size_t)(gi + 1) <= ctx->tile_events.size();
     if (timed) cudaEventRecord(ctx->tile_events[2 * gi], ctx->stream);
-    launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
+    {
+      Range r("ugu_gpu tile");
+      launch_tile(p, persistent_grid(ctx, tile_kernel_blocks_per_sm()), ctx->stream);
+    }
     if (timed) {
       cudaEventRecord(ctx->tile_events[2 * gi + 1], ctx->stream);
       ctx->timed_groups = (int)gi + 1;
@@ -933,6 +955,7 @@ uint64_t view_list_signature(const ugu_gpu_context* ctx, int n, const ugu_gpu_vi
 }
 
 int render_impl(ugu_gpu_context* ctx, int n, const ugu_gpu_view* views, uint32_t flags) {
+  Range range("ugu_gpu render");
   if (n < 0 || (n > 0 && !views))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view list");
   if (n == 0) return UGU_GPU_OK;
@@ -1282,6 +1305,7 @@ int ugu_gpu_render_views(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vi
 
 int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                         uint32_t flags, ugu_gpu_plan** out) {
+  Range range("ugu_gpu plan create");
   if (!ctx || !out || n <= 0 || !views)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad plan arguments");
   *out = nullptr;
@@ -1337,6 +1361,7 @@ int ugu_gpu_plan_create(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* vie
 }
 
 int ugu_gpu_plan_launch(ugu_gpu_plan* plan) {
+  Range range("ugu_gpu plan launch");
   if (!plan) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL plan");
   ugu_gpu_context* ctx = plan->ctx;
   CK(ctx, cudaGraphLaunch(plan->exec, ctx->stream), "cudaGraphLaunch");
@@ -1493,6 +1518,7 @@ int ugu_gpu_texture_mapping(ugu_gpu_context* ctx, int32_t mesh, int32_t n,
                             const ugu_gpu_keyframe* keyframes, const int32_t* face_kf,
                             const float* face_tri, const ugu_gpu_texture_option* option,
                             uint8_t* texture, uint8_t* mask, uint32_t flags) {
+  Range range("ugu_gpu texture mapping");
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   cudaSetDevice(ctx->device);
   if (!texmap_args_ok(ctx, n, keyframes, face_kf, face_tri, option, texture, mask))
@@ -1514,6 +1540,7 @@ int ugu_gpu_texture_mapping_targets(ugu_gpu_context* ctx, int32_t num_faces,
                                     const ugu_gpu_keyframe* keyframes, const int32_t* face_kf,
                                     const float* face_tri, const ugu_gpu_texture_option* option,
                                     uint8_t* texture, uint8_t* mask, uint32_t flags) {
+  Range range("ugu_gpu texture mapping");
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   cudaSetDevice(ctx->device);
   if (num_faces < 0 || (num_faces > 0 && !face_target))
@@ -1531,6 +1558,7 @@ int ugu_gpu_texture_mapping_targets(ugu_gpu_context* ctx, int32_t num_faces,
 // reference writes past its texture).
 int ugu_gpu_tile_images(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_keyframe* keyframes,
                         int32_t x_tiles, uint8_t* texture, uint32_t flags) {
+  Range range("ugu_gpu tile images");
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   cudaSetDevice(ctx->device);
   if (n <= 0 || !keyframes || !texture || x_tiles <= 0 || n % x_tiles != 0)
@@ -1690,6 +1718,7 @@ void write_cached_tuning(uint64_t key, const ugu_gpu_tuning& t) {
 
 int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                      ugu_gpu_tuning* chosen) {
+  Range range("ugu_gpu autotune");
   if (!ctx || n <= 0 || !views)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad autotune arguments");
   cudaSetDevice(ctx->device);
@@ -1824,6 +1853,7 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
                      const float* const* targets, float* grad_texels,
                      float* grad_vertex_colors, float* grad_vertices, float* loss_out,
                      uint32_t flags) {
+  Range range("ugu_gpu backward");
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   if (n <= 0 || !views || !targets)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view or target list");
@@ -1946,6 +1976,7 @@ int ugu_gpu_get_device_mesh(ugu_gpu_context* ctx, int32_t slot, ugu_gpu_device_m
 
 int ugu_gpu_visualize(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_vis* items,
                       uint32_t flags) {
+  Range range("ugu_gpu visualize");
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   if (n < 0 || (n > 0 && !items))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad item list");
@@ -2020,6 +2051,7 @@ int ugu_gpu_visualize(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_vis* items,
 
 int ugu_gpu_render_gbuffer(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_gbuffer* views,
                            uint32_t flags) {
+  Range range("ugu_gpu gbuffer");
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   if (n < 0 || (n > 0 && !views))
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT, "bad view list");
@@ -2118,6 +2150,7 @@ int ugu_gpu_test_visibility(ugu_gpu_context* ctx, int32_t mesh, const float* nor
                             const ugu_gpu_keyframe* keyframes,
                             const ugu_gpu_visibility_option* option, int32_t facewise,
                             const ugu_gpu_visibility_out* out, uint32_t flags) {
+  Range range("ugu_gpu visibility");
   if (!ctx) return set_error(nullptr, UGU_GPU_ERR_INVALID_ARGUMENT, "NULL context");
   cudaSetDevice(ctx->device);
   if (n <= 0 || !keyframes || !option || !out)
