@@ -28,7 +28,8 @@ namespace {
 
 // An NVTX range over a scope (NVTX 3 is header-only: without a tool attached
 // the calls return at once).  Profilers group the kernels an entry point
-// launches under its range, e.g. `ncu --nvtx --nvtx-include "ugu_gpu tile/"`.
+// launches under its range, e.g. `ncu --nvtx --nvtx-include "ugu_gpu tile/"`
+// for a direct render's tile kernels (a plan replays under its launch range).
 struct Range {
   explicit Range(const char* name) { nvtxRangePushA(name); }
   ~Range() { nvtxRangePop(); }
