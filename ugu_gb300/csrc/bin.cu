@@ -177,8 +177,10 @@ __global__ void __launch_bounds__(kBinThreads) k_count(TileParams p) {
   bin_pass<kFaces, false>(p);
 }
 
+// Eight blocks per SM (32 registers, a few spilled) rather than the six that
+// 40 registers allow: the placing atomics' latency wants the warps.
 template <int kFaces>
-__global__ void __launch_bounds__(kBinThreads) k_place(TileParams p) {
+__global__ void __launch_bounds__(kBinThreads, 8) k_place(TileParams p) {
   bin_pass<kFaces, true>(p);
 }
 
