@@ -126,11 +126,6 @@ __device__ __forceinline__ FaceBins bin_face(const TileParams& p, const BinShare
   return b;
 }
 
-// The global tile of the face's k-th tile (row-major over its tile range).
-__device__ __forceinline__ int tile_of(const BinShared& sb, const FaceBins& b, int k) {
-  return sb.view.tile_base + (b.ty0 + k / b.ntx) * sb.view.tiles_x + b.tx0 + k % b.ntx;
-}
-
 // kPlace false: count every (face, tile) entry of kFaces faces per thread;
 // true: write each entry to its place.  The lanes of a warp walk their
 // faces' tiles together; lanes whose current tile (and, when placing, draw
@@ -148,11 +143,18 @@ __device__ __forceinline__ void bin_pass(const TileParams& p) {
     const FaceBins b = bin_face(p, sb, f0 + u * kBinThreads);
     const int nmax = __reduce_max_sync(0xffffffffu, b.n);
     const int2 e = make_int2(b.i, __float_as_int(b.zlb));
+    // the face's tiles in row-major order over its tile range, walked
+    // without a division per tile
+    int cx = 0, row = sb.view.tile_base + b.ty0 * sb.view.tiles_x + b.tx0;
     for (int k = 0; k < nmax; ++k) {
       const bool act = k < b.n;
       const unsigned am = __ballot_sync(0xffffffffu, act);
       if (!act) continue;
-      const int t = tile_of(sb, b, k);
+      const int t = row + cx;
+      if (++cx == b.ntx) {
+        cx = 0;
+        row += sb.view.tiles_x;
+      }
       const unsigned peers = __match_any_sync(am, kPlace ? 2 * t + b.cls : t);
       const int leader = __ffs(peers) - 1, cnt = __popc(peers);
       if (!kPlace) {
