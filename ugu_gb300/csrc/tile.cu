@@ -69,9 +69,12 @@ struct Region {
 
 // A face's bbox-in-tile in 32 bits: tile-local x0 and y0, width - 1 (5 bits
 // each) and m = ceil(2^16 / width) (17 bits), so that row = (k * m) >> 16
-// for every pixel number k < width * height <= 1024 of the box.
-__device__ __forceinline__ float pack_box(int x0, int y0, int w) {
-  const unsigned m = (65536u + (unsigned)w - 1u) / (unsigned)w;
+// for every pixel number k < width * height <= 1024 of the box.  m comes
+// from a table of the 32 widths in shared memory (box_recip).
+__device__ __forceinline__ unsigned box_recip_of(int w) {
+  return (65536u + (unsigned)w - 1u) / (unsigned)w;
+}
+__device__ __forceinline__ float pack_box(int x0, int y0, int w, unsigned m) {
   return __uint_as_float((unsigned)x0 | ((unsigned)y0 << 5) | ((unsigned)(w - 1) << 10) |
                          (m << 15));
 }
@@ -86,6 +89,7 @@ struct TileSmem {
   int item;
   unsigned zmax_bits;
   int cursor[2];  // next entry of each draw class: warps take 32 at a time
+  unsigned box_recip[kMaxTile];  // ceil(2^16 / w) for box widths w = 1 .. 32
 };
 // Eight blocks (with the 1 KB each block reserves) within the 196 KB
 // shared-memory carve-out, which leaves 60 KB of L1 for the setup and
@@ -161,7 +165,9 @@ __device__ __forceinline__ void raster_pass(TileSmem& sm, Region& R, const TileP
     if (cnt > 0) {
       const float4 a = R.r0[j], b = R.r1[j];
       const unsigned box = __float_as_uint(b.w);
-      const int bw = (int)((box >> 10) & 31u) + 1, bh = cnt / bw;
+      // bh = cnt / bw through the box's reciprocal m = ceil(2^16 / bw):
+      // exact, since bh (bw - 1) < 2^16 for boxes of at most 32 x 32
+      const int bw = (int)((box >> 10) & 31u) + 1, bh = (cnt * (int)(box >> 15)) >> 16;
       const int bx0 = tx0 + (int)(box & 31u), by0 = ty0 + (int)((box >> 5) & 31u);
       FaceSpans sp;
       if (face_spans(a.x, a.y, a.z, a.w, b.x, b.y, b.z, bx0, bx0 + bw - 1, by0, by0 + bh - 1,
@@ -255,6 +261,7 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
   if (p.counters->dropped) return;  // entries were not written: the host retries
   int v_begin = 0, v_end = 0;  // global tiles of the view in shared memory
   Region& R = sm.reg;
+  if (tid < kMaxTile) sm.box_recip[tid] = box_recip_of(tid + 1);  // read after the next barrier
   for (;;) {
     if (tid == 0) sm.item = (int)atomicAdd(&p.counters->next_tile, 1u);
     __syncthreads();
@@ -373,7 +380,8 @@ __global__ void __launch_bounds__(kTileThreads, UGU_TILE_BLOCKS) k_tile(TilePara
           const float aP = pre_ok ? fabsf(s.area) * (z0 * z1 * z2) * 0.99998474f
                                   : __int_as_float(0x7fc00000);
           R.r0[j] = make_float4(s.v0.x, s.v0.y, s.v1.x, s.v1.y);
-          R.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, pack_box(bx0 - tx0, by0 - ty0, bw));
+          R.r1[j] = make_float4(s.v2.x, s.v2.y, s.area, pack_box(bx0 - tx0, by0 - ty0, bw,
+                                                                 sm.box_recip[bw - 1]));
           R.r2[j] = make_float4(z0, z1, z2, __int_as_float(f));
           R.r3[j] = make_float4(sa, sb, sc, tol);
           R.r5[j] = make_float4(z1 * z2, z0 * z2, z0 * z1, aP);
