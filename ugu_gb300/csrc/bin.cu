@@ -36,8 +36,11 @@ constexpr int kScanRound = kScanThreads * kScanItems;
 // pixel: the three edge functions carry rounding errors of at most
 // delta = 2^-18 * bboxW * bboxH, so the interpolation weights' sum exceeds
 // the area by at most delta and the depth is at least
-// zmin * |A| / (|A| + delta), less a margin for this expression's own
-// roundings.  -1 when no bound is proven.
+// zmin * |A| / (|A| + delta), less a margin of 2^-16 for this expression's
+// own roundings: four of 2^-24 each, and the fast quotient's (at most two
+// ulp, 2^-22, for a divisor in [2^-126, 2^126]; |A| + delta >= 3 * 2^-18,
+// and past 2^126 the fast quotient is 0, which is still a lower bound).
+// -1 when no bound is proven.
 __device__ __forceinline__ float depth_lower_bound(const FaceSetup& s) {
   const float zmin = fminf(fminf(s.v0.z, s.v1.z), s.v2.z);
   const float BW = fmaxf(fmaxf(s.v0.x, s.v1.x), s.v2.x) -
@@ -46,7 +49,8 @@ __device__ __forceinline__ float depth_lower_bound(const FaceSetup& s) {
                    fminf(fminf(s.v0.y, s.v1.y), s.v2.y) + 1.0f;
   const float delta = kU64 * BW * BH;
   const float aa = fabsf(s.area);
-  return (aa > 2.0f * delta && zmin > 0.0f) ? zmin * (aa / (aa + delta)) * 0.99998474f : -1.0f;
+  return (aa > 2.0f * delta && zmin > 0.0f) ? zmin * __fdividef(aa, aa + delta) * 0.99998474f
+                                             : -1.0f;
 }
 
 // Loop A for every vertex of one view (blockIdx.y), stored by vertex rank;
