@@ -73,6 +73,17 @@ __device__ __forceinline__ void add3(float* g, int64_t tix, float g0, float g1,
   }
 }
 
+// A texel's RGB gradient: one 16-byte atomic into the RGBA scratch when
+// there is one (every texel 16-byte aligned), else add3 into the H*W*3
+// buffer.
+__device__ __forceinline__ void add_texel(const BackwardParams& p, int64_t tix, float g0,
+                                          float g1, float g2, bool aligned8) {
+  if (p.grad_texels4)
+    atomicAdd(reinterpret_cast<float4*>(p.grad_texels4) + tix, make_float4(g0, g1, g2, 0.0f));
+  else
+    add3(p.grad_texels, tix, g0, g1, g2, aligned8);
+}
+
 // One vertex of one view: its screen x and y, projected in double, as
 // unevaluated sums hi + lo of two floats (about 48 significant bits), and
 // 1 / z.  32 bytes per vertex.
@@ -423,7 +434,7 @@ __device__ __forceinline__ float backward_pixel(const BackwardParams& p, const D
 #pragma unroll
       for (int j = 0; j < 4; ++j)
         if (j < o.ntex)
-          add3(p.grad_texels, o.tix[j], o.tg[j][0], o.tg[j][1], o.tg[j][2], aligned8);
+          add_texel(p, o.tix[j], o.tg[j][0], o.tg[j][1], o.tg[j][2], aligned8);
   } else if (fid > 0) {
     // Texel and vertex-colour gradients only: the float colour equals the
     // forward's (same exact arithmetic), so the loss is the rendered one.
@@ -502,8 +513,7 @@ __device__ __forceinline__ float backward_pixel(const BackwardParams& p, const D
       }
       if (mid == 0 && p.grad_texels)
         for (int j = 0; j < nt; ++j)
-          add3(p.grad_texels, tix[j], gC[0] * tw[j], gC[1] * tw[j], gC[2] * tw[j],
-                         aligned8);
+          add_texel(p, tix[j], gC[0] * tw[j], gC[1] * tw[j], gC[2] * tw[j], aligned8);
     }
   }
 
@@ -569,6 +579,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_backward(BackwardParams p) {
   }
 }
 
+// grad_texels += the RGB of the RGBA scratch, one thread per texel.
+__global__ void __launch_bounds__(kThreads) k_fold_texels(float* g3, const float4* g4, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (t >= n) return;
+  const float4 v = g4[t];
+  g3[3 * t + 0] += v.x;
+  g3[3 * t + 1] += v.y;
+  g3[3 * t + 2] += v.z;
+}
+
 }  // namespace
 
 void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertices, int num_sms,
@@ -580,6 +600,9 @@ void launch_backward(const BackwardParams& p, int64_t max_pixels, int max_vertic
   const int64_t per_view = std::max<int64_t>(1, ((int64_t)num_sms * 16 + p.num_views - 1) / p.num_views);
   dim3 grid((unsigned)std::max<int64_t>(1, std::min(chunks, per_view)), p.num_views);
   k_backward<<<grid, kThreads, 0, s>>>(p);
+  if (p.grad_texels4 && p.num_texels4 > 0)
+    k_fold_texels<<<(unsigned)((p.num_texels4 + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+        p.grad_texels, reinterpret_cast<const float4*>(p.grad_texels4), p.num_texels4);
 }
 
 }  // namespace ugu_gpu

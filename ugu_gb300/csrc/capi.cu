@@ -99,6 +99,8 @@ struct Scratch {
   // backward: per-view target pointers, hi + lo projection table
   void* proj64 = nullptr;    // 32 bytes per vertex of every view
   size_t proj64_cap = 0;     // vertices
+  float* grad4 = nullptr;   // backward: RGBA texel-gradient scratch
+  size_t grad4_cap = 0;     // texels
   const float** d_targets = nullptr;
   const float** h_targets = nullptr;  // pinned
   size_t targets_cap = 0;
@@ -225,6 +227,7 @@ void free_scratch(Scratch& s) {
   cudaFree(s.tcounters);
   cudaFreeHost(s.h_tcounters);
   cudaFree(s.proj64);
+  cudaFree(s.grad4);
   cudaFree(s.d_targets);
   cudaFreeHost(s.h_targets);
   s = Scratch();
@@ -1868,16 +1871,19 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   if (o.diffuse_shading != 0)
     return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
                      "backward differentiates the unshaded colour (diffuse_shading = kNone)");
-  int64_t max_px = 0, sum_v = 0;
+  int64_t max_px = 0, sum_v = 0, texels = 0, sum_px = 0;
   int max_v = 0;
   for (int i = 0; i < n; ++i) {
     ugu_gpu_view v = views[i];
+    if (grad_texels && o.diffuse_color == 1 && v.mesh >= 0 && v.mesh < kMaxMeshes)
+      texels = std::max(texels, (int64_t)ctx->meshes[v.mesh].tex0_w * ctx->meshes[v.mesh].tex0_h);
     if (!v.images.face_id || !targets[i])
       return set_error(ctx, UGU_GPU_ERR_INVALID_ARGUMENT,
                        "view %d needs the forward's face_id image and a target", i);
     int rc = validate_view(ctx, v, true);
     if (rc) return rc;
     max_px = std::max(max_px, (int64_t)v.camera.width * v.camera.height);
+    sum_px += (int64_t)v.camera.width * v.camera.height;
     const int nv = ctx->meshes[v.mesh].dev.num_vertices;
     max_v = std::max(max_v, nv);
     sum_v += nv;
@@ -1902,6 +1908,19 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     CK(ctx, cudaMalloc(&s.proj64, (size_t)sum_v * 32),
        "cudaMalloc(projection table)");
     s.proj64_cap = (size_t)sum_v;
+  }
+  // texel gradients through an RGBA scratch: one 16-byte atomic per texel
+  // instead of an 8- and a 4-byte one, then added into grad_texels.  The
+  // scratch costs a clear and a pass over the texture, about what the
+  // atomics of 1.5 pixels per texel save (measured), so it is used from 2.
+  if (sum_px < 2 * texels) texels = 0;
+  if (texels > 0 && (size_t)texels > s.grad4_cap) {
+    cudaFree(s.grad4);
+    s.grad4 = nullptr;
+    s.grad4_cap = 0;
+    CK(ctx, cudaMalloc(&s.grad4, (size_t)texels * 4 * sizeof(float)),
+       "cudaMalloc(texel gradient scratch)");
+    s.grad4_cap = (size_t)texels;
   }
   CK(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   int64_t proj_off = 0;
@@ -1934,11 +1953,17 @@ int ugu_gpu_backward(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   p.loss = loss_out;
   p.bad_ids = &s.counters[0].pad;
   p.proj64 = s.proj64;
+  if (texels > 0) {
+    p.grad_texels4 = s.grad4;
+    p.num_texels4 = texels;
+    CK(ctx, cudaMemsetAsync(s.grad4, 0, (size_t)texels * 4 * sizeof(float), ctx->stream),
+       "cudaMemsetAsync(texel gradient scratch)");
+  }
   CK(ctx, cudaMemsetAsync(s.counters, 0, sizeof(DevCounters), ctx->stream),
      "cudaMemsetAsync(counters)");
   launch_backward(p, max_px, max_v, ctx->num_sms, ctx->stream);
   CK(ctx, cudaGetLastError(), "backward launch");
-  ctx->launches += grad_vertices ? 2 : 1;
+  ctx->launches += 1 + (grad_vertices ? 1 : 0) + (texels > 0 ? 1 : 0);
   CK(ctx, cudaMemcpyAsync(s.h_counters, s.counters, sizeof(DevCounters), cudaMemcpyDeviceToHost,
                           ctx->stream),
      "cudaMemcpyAsync(counters)");

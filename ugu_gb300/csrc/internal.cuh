@@ -174,12 +174,16 @@ struct BackwardParams {
   int32_t diffuse_color, interp;
   const float* const* targets;  // device array of per-view H*W*3 targets
   float* grad_texels;           // material 0, H*W*3 (or NULL)
+  // texel gradients gathered first as RGBA (one 16-byte atomic per texel)
+  // and then added into grad_texels, or NULL to scatter into it directly
+  float* grad_texels4;
+  int64_t num_texels4;
   float* grad_vertex_colors;    // V*3 (or NULL)
   float* grad_vertices;         // V*3 (or NULL)
   float* loss;                  // one per view (or NULL)
   unsigned long long* bad_ids;  // counts face ids outside [-1, num_faces)
   void* proj64;                 // per view (DevView::proj_offset), 32 bytes per vertex: screen
-                                // x, y projected in double as hi + lo floats, and 1/z
+                                // x, y as hi + lo floats, and 1/z
 };
 
 // Image helpers of ugu_gpu_visualize (vis.cu): one item, device pointers.
