@@ -245,7 +245,9 @@ typedef struct {
   int32_t padding_kernel;   /* PaddingSimple's window (3) */
 } ugu_gpu_texture_option;
 
-/* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune). */
+/* GPU tunables (no reference counterpart; chosen by ugu_gpu_autotune).  A
+ * new context starts on the tiled path with tile_log2 5, split_class 256,
+ * bin_faces 4 and small_view_pixels 307200 (640 x 480). */
 typedef struct {
   int32_t path;             /* UGU_GPU_PATH_TILED (default) or UGU_GPU_PATH_GLOBAL */
   int32_t tile_log2;        /* screen tile edge = 1 << tile_log2 pixels (4 or 5) */

@@ -1104,9 +1104,10 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->tuning.small_bbox_max = 256;
   ctx->tuning.group_pixels = 4 << 20;
   ctx->tuning.ctas_per_sm = 0;
-  ctx->tuning.split_class = 64;
-  ctx->tuning.bin_faces = 2;
-  ctx->tuning.small_view_pixels = 0;
+  // the thresholds the autotuner most often keeps on large view batches
+  ctx->tuning.split_class = 256;
+  ctx->tuning.bin_faces = 4;
+  ctx->tuning.small_view_pixels = 640 * 480;
   *out = ctx;
   return UGU_GPU_OK;
 }
@@ -1742,10 +1743,10 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   cudaEvent_t e0, e1;
   CK(ctx, cudaEventCreate(&e0), "cudaEventCreate");
   CK(ctx, cudaEventCreate(&e1), "cudaEventCreate");
-  // The median of five timed renders of the views on one candidate, after
+  // The median of seven timed renders of the views on one candidate, after
   // an untimed one that sizes its lists; a failed candidate is skipped.
   // (Candidates often differ by about 1 %, within the spread of three.)
-  constexpr int kTimed = 5;
+  constexpr int kTimed = 7;
   auto time_of = [&](const ugu_gpu_tuning& t, float* ms_out) -> int {
     int r = ugu_gpu_set_tuning(ctx, &t);
     if (!r) r = render_impl(ctx, n, views, UGU_GPU_DEVICE_POINTERS | UGU_GPU_ASYNC);
@@ -1767,21 +1768,26 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
   float best = 1e30f;
   ugu_gpu_tuning best_t = start;
   bool any = false;
+  // in stage 2 a threshold moves off its current value only for a gain above
+  // the timing noise, so that noise does not walk the search away from the
+  // base values
+  float margin = 1.0f;
   auto consider = [&](const ugu_gpu_tuning& t) {
     float ms = 0.0f;
-    if (time_of(t, &ms) == UGU_GPU_OK && ms < best) {
+    if (time_of(t, &ms) == UGU_GPU_OK && ms < best * margin) {
       best = ms;
       best_t = t;
       any = true;
     }
   };
-  // Stage 1: the path and the tile size, each at its default thresholds.
+  // Stage 1: the path and the tile size, each at the base thresholds (a new
+  // context's).
   ugu_gpu_tuning base = start;
   base.entry_capacity = 0;
   base.ctas_per_sm = 0;
-  base.split_class = 64;
-  base.bin_faces = 2;
-  base.small_view_pixels = 0;
+  base.split_class = 256;
+  base.bin_faces = 4;
+  base.small_view_pixels = 640 * 480;
   base.small_bbox_max = 256;
   base.group_pixels = 8 << 20;
   for (int tl : {4, 5}) {
@@ -1797,10 +1803,11 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
     consider(t);
   }
   // Stage 2: each threshold of the chosen path in turn, the others held.
+  margin = 0.997f;
   if (any && best_t.path == UGU_GPU_PATH_TILED) {
     if (best_t.tile_log2 == 5) {  // small views on 16-pixel tiles
       const ugu_gpu_tuning s0 = best_t;
-      for (int v : {320 * 240, 640 * 480, 1280 * 720}) {
+      for (int v : {0, 320 * 240, 1280 * 720}) {
         ugu_gpu_tuning t = s0;
         t.small_view_pixels = v;
         consider(t);
@@ -1813,13 +1820,13 @@ int ugu_gpu_autotune(ugu_gpu_context* ctx, int32_t n, const ugu_gpu_view* views,
       consider(t);
     }
     const ugu_gpu_tuning s2 = best_t;
-    for (int v : {1, 256}) {
+    for (int v : {1, 64}) {
       ugu_gpu_tuning t = s2;
       t.split_class = v;
       consider(t);
     }
     const ugu_gpu_tuning s3 = best_t;
-    for (int v : {1, 4}) {
+    for (int v : {1, 2}) {
       ugu_gpu_tuning t = s3;
       t.bin_faces = v;
       consider(t);
