@@ -80,3 +80,17 @@ def test_kernel_cases_lists_every_kernel_family():
     if not torch.cuda.is_available():
         with _pytest.raises(SystemExit):
             kernel_cases.main(["--case", "tiled", "--repeat", "1"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["tiled", "global", "noalloc", "visualize", "gbuffer",
+                                  "visibility", "texmap", "backward", "raytrace"])
+def test_kernel_cases_run_on_the_gpu(case, capsys):
+    """Every profiling case runs once on the device and reports its timing."""
+    import json
+    from ugu_gb300 import kernel_cases
+    views = {"tiled": 2, "global": 2, "visualize": 2, "gbuffer": 2, "visibility": 2,
+             "texmap": 2, "backward": 2, "raytrace": 1}.get(case, 0)
+    kernel_cases.main(["--case", case, "--repeat", "1", "--views", str(views)])
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["case"] == case and line["ms_per_call"] > 0.0
