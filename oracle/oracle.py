@@ -125,6 +125,9 @@ def load():
         lib.oracle_simple_triangles.restype = C.c_int
         lib.oracle_simple_tile.argtypes = [C.c_int32, P, P, P, P, C.c_int32, P, P, P, P, P]
         lib.oracle_simple_tile.restype = C.c_int
+        lib.oracle_simple_charts.argtypes = [C.c_int32, P, P, P, C.c_int32, P, P, P, C.c_int32,
+                                             C.c_int32, P, P, P, P]
+        lib.oracle_simple_charts.restype = C.c_int
         lib.oracle_gbuffer.argtypes = [P] * 11
         lib.oracle_gbuffer.restype = C.c_int64
         lib.oracle_test_visibility.argtypes = [P, C.c_int32, P, C.c_int32, P, C.c_int32, P, P,
@@ -380,6 +383,27 @@ def simple_tile(kf_ids, kf_colors, face_kf, face_tri):
                                 tiles.ctypes.data, tex.ctypes.data if tex.size else None,
                                 uv.ctypes.data)
     return rc, tex, uv
+
+
+def simple_charts(vertex_indices, kf_colors, face_kf, face_tri, tex_w, tex_h):
+    """TextureMapping with kGenerateSimpleCharts: (status, texture, uv,
+    uv_indices F x 3); face_kf[f] indexes kf_colors (-1: none)."""
+    lib = load()
+    cols, kw, kh, ptrs = _kf_arrays(kf_colors)
+    vi = np.ascontiguousarray(vertex_indices, np.int32)
+    fk = np.ascontiguousarray(face_kf, np.int32)
+    ft = np.ascontiguousarray(face_tri, np.float32)
+    dims = np.zeros(3, np.int32)
+    args = (len(fk), vi.ctypes.data, fk.ctypes.data, ft.ctypes.data, len(cols), kw.ctypes.data,
+            kh.ctypes.data, C.addressof(ptrs), int(tex_w), int(tex_h), dims.ctypes.data)
+    rc = lib.oracle_simple_charts(*args, None, None, None)
+    if rc:
+        return rc, None, None, None
+    tex = np.zeros((dims[1], dims[0], 3), np.uint8)
+    uv = np.zeros((dims[2], 2), np.float32)
+    uvi = np.zeros((len(fk), 3), np.int32)
+    rc = lib.oracle_simple_charts(*args, tex.ctypes.data, uv.ctypes.data, uvi.ctypes.data)
+    return rc, tex, uv, uvi
 
 
 GBUFFER = ("pos_wld", "pos_cam", "normal_wld", "normal_cam", "bary", "uv")

@@ -13,9 +13,13 @@
  * the low bits of the truncated int32 value, as the GPU does.
  */
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
+#include <deque>
+#include <map>
 #include <random>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -329,4 +333,218 @@ static void pad_simple(int32_t tex_w, int32_t tex_h, int32_t padding_kernel, uin
       mask[p] = 255;
       for (int c = 0; c < 3; ++c) texture[3 * p + c] = f2u8(sum[c] / (float)cnt);
     }
+}
+
+// GenerateSimpleChartsTextureAndUv with GenerateAtlas (texture_mapper.cc:
+// 476-922), BinPacking2D (src/discrete/bin_packer_2d.cc:14-113), the
+// FaceAdjacency edge lookups (include/ugu/face_adjacency.h:49-151, 194-209)
+// and PaddingBorderSimple (texture_mapper.cc:203-231).  Charts of equal
+// patch area keep their chart order (std::stable_sort; libstdc++'s
+// std::sort leaves it unspecified).  Called with texture == NULL it only
+// reports the texture size (dims[0], dims[1]) and the uv count (dims[2]).
+// Returns 0, -1 when nothing packs within 8192, -2 for a patch outside its
+// keyframe image, -3 for an edge sum that names no face (the reference then
+// reads past its arrays).
+namespace {
+
+struct ORect {
+  int x, y, w, h;
+};
+
+bool bin_packing(const std::vector<ORect>& rects, std::vector<ORect>* packed,
+                 std::vector<ORect>* avail, int x_min, int x_max, int y_min, int y_max) {
+  avail->assign(1, ORect{x_min, y_min, x_max, y_max});
+  packed->clear();
+  for (const ORect& r : rects) {
+    for (;;) {
+      int best = -1, best_diff = 2147483647;
+      for (int i = 0; i < (int)avail->size(); ++i) {
+        const ORect& a = (*avail)[i];
+        if (r.h <= a.h && r.w <= a.w && a.w * a.h - r.w * r.h < best_diff) {
+          best_diff = a.w * a.h - r.w * r.h;
+          best = i;
+        }
+      }
+      if (best < 0 || (*avail)[best].w * (*avail)[best].h < r.w * r.h) return false;
+      const ORect b = (*avail)[best];
+      if (b.w == r.w && b.h == r.h) {
+        packed->push_back(b);
+        avail->erase(avail->begin() + best);
+        break;
+      }
+      ORect c1, c2;
+      if (b.h - r.h > b.w - r.w) {
+        c1 = ORect{b.x, b.y, b.w, r.h};
+        c2 = ORect{b.x, b.y + r.h, b.w, b.h - r.h};
+      } else {
+        c1 = ORect{b.x, b.y, r.w, b.h};
+        c2 = ORect{b.x + r.w, b.y, b.w - r.w, b.h};
+      }
+      avail->erase(avail->begin() + best);
+      avail->push_back(c2);
+      avail->push_back(c1);
+    }
+  }
+  return true;
+}
+
+struct OChart {
+  int w = 0, h = 0;
+  std::vector<uint8_t> patch;
+  std::vector<std::pair<float, float>> pos;       // per chart vertex, vertex-id order
+  std::vector<std::pair<int, std::array<int, 3>>> face_idx;
+};
+
+}  // namespace
+
+extern "C" int oracle_simple_charts(int32_t num_faces, const int32_t* vidx, const int32_t* face_kf,
+                                    const float* face_tri, int32_t num_kf, const int32_t* kf_w,
+                                    const int32_t* kf_h, const uint8_t* const* kf_color,
+                                    int32_t tex_w, int32_t tex_h, int32_t* dims,
+                                    uint8_t* texture, float* uv, int32_t* uv_indices) {
+  const int F = num_faces;
+  std::map<std::pair<int, int>, long long> edges;
+  for (int f = 0; f < F; ++f) {
+    const int* v = vidx + 3 * (size_t)f;
+    edges[{v[0], v[1]}] += f + 1;
+    edges[{v[1], v[2]}] += f + 1;
+    edges[{v[2], v[0]}] += f + 1;
+  }
+  auto lookup = [&](int a, int b) -> long long {
+    auto it = edges.find({a, b});
+    return it == edges.end() ? 0 : it->second;
+  };
+  std::vector<char> selected(F, 0);
+  std::vector<OChart> valid;
+  std::vector<int> invalid_faces;
+  for (int seed = 0; seed < F; ++seed) {
+    if (selected[seed]) continue;
+    const int kf = face_kf[seed];
+    std::vector<int> faces{seed};
+    selected[seed] = 1;
+    std::deque<int> queue{seed};
+    while (!queue.empty()) {
+      const int fid = queue.front();
+      queue.pop_front();
+      const int* v = vidx + 3 * (size_t)fid;
+      std::vector<long long> adj;
+      for (auto e : {std::make_pair(v[1], v[0]), std::make_pair(v[2], v[1]),
+                     std::make_pair(v[0], v[2])}) {
+        const long long m = lookup(e.first, e.second);
+        if (m > 0) adj.push_back(m - 1);
+      }
+      for (auto e : {std::make_pair(v[0], v[1]), std::make_pair(v[1], v[2]),
+                     std::make_pair(v[2], v[0])}) {
+        auto it = edges.find(e);
+        if (it != edges.end()) it->second = 0;
+      }
+      for (long long g : adj)
+        if (g >= F) return -3;
+      std::vector<int> add;
+      for (long long g : adj)
+        if (face_kf[g] == kf && !selected[g]) add.push_back((int)g);
+      for (int g : add) {
+        queue.push_back(g);
+        faces.push_back(g);
+        selected[g] = 1;
+      }
+    }
+    if (kf < 0) {
+      invalid_faces.insert(invalid_faces.end(), faces.begin(), faces.end());
+      continue;
+    }
+    if (kf >= num_kf) return -2;
+    float xminf = 1e30f, xmaxf = -1e30f, yminf = 1e30f, ymaxf = -1e30f;
+    for (int f : faces)
+      for (int j = 0; j < 3; ++j) {
+        xminf = std::min(xminf, face_tri[6 * (size_t)f + 2 * j]);
+        xmaxf = std::max(xmaxf, face_tri[6 * (size_t)f + 2 * j]);
+        yminf = std::min(yminf, face_tri[6 * (size_t)f + 2 * j + 1]);
+        ymaxf = std::max(ymaxf, face_tri[6 * (size_t)f + 2 * j + 1]);
+      }
+    const int xmin = (int)std::floor(xminf), ymin = (int)std::floor(yminf);
+    const int xmax = (int)std::ceil(xmaxf), ymax = (int)std::ceil(ymaxf);
+    if (xmin < 0 || ymin < 0 || xmax >= kf_w[kf] || ymax >= kf_h[kf]) return -2;
+    const int pad = 1;
+    OChart c;
+    c.w = xmax - xmin + 1 + 2 * pad;
+    c.h = ymax - ymin + 1 + 2 * pad;
+    c.patch.assign((size_t)c.w * c.h * 3, 0);
+    for (int y = ymin; y <= ymax; ++y)
+      std::copy(kf_color[kf] + ((size_t)kf_w[kf] * y + xmin) * 3,
+                kf_color[kf] + ((size_t)kf_w[kf] * y + xmax + 1) * 3,
+                c.patch.begin() + ((size_t)c.w * (y - ymin + pad) + pad) * 3);
+    auto px = [&](int y, int x) { return c.patch.begin() + ((size_t)c.w * y + x) * 3; };
+    for (int y = 0; y < pad; ++y)
+      for (int x = 0; x < c.w; ++x) std::copy(px(pad, x), px(pad, x) + 3, px(y, x));
+    for (int y = c.h - pad; y < c.h; ++y)
+      for (int x = 0; x < c.w; ++x) std::copy(px(c.h - pad - 1, x), px(c.h - pad - 1, x) + 3, px(y, x));
+    for (int y = 0; y < c.h; ++y)
+      for (int x = 0; x < pad; ++x) std::copy(px(y, pad), px(y, pad) + 3, px(y, x));
+    for (int y = 0; y < c.h; ++y)
+      for (int x = c.w - pad; x < c.w; ++x) std::copy(px(y, c.w - pad - 1), px(y, c.w - pad - 1) + 3, px(y, x));
+    std::map<int, std::pair<float, float>> vpos;
+    for (int f : faces)
+      for (int j = 0; j < 3; ++j) {
+        const float lx = face_tri[6 * (size_t)f + 2 * j] - xmin + pad;
+        const float ly = face_tri[6 * (size_t)f + 2 * j + 1] - ymin + pad;
+        vpos.insert({vidx[3 * (size_t)f + j], {lx, ly}});
+      }
+    std::map<int, int> renum;
+    for (const auto& kv : vpos) {
+      renum[kv.first] = (int)c.pos.size();
+      c.pos.push_back(kv.second);
+    }
+    for (int f : faces)
+      c.face_idx.push_back({f, {renum[vidx[3 * (size_t)f]], renum[vidx[3 * (size_t)f + 1]],
+                                renum[vidx[3 * (size_t)f + 2]]}});
+    valid.push_back(std::move(c));
+  }
+  std::stable_sort(valid.begin(), valid.end(),
+                   [](const OChart& a, const OChart& b) { return a.w * a.h > b.w * b.h; });
+  std::vector<ORect> rects, packed, avail;
+  for (const OChart& c : valid) rects.push_back(ORect{0, 0, c.w, c.h});
+  int cur_w = tex_w, cur_h = tex_h, tries = 0;
+  const float ratio = std::sqrt(2.0f);
+  while (!bin_packing(rects, &packed, &avail, 1, cur_w - 1, 1, cur_h - 1)) {
+    ++tries;
+    cur_w = (int)(tex_w * std::pow(ratio, tries));
+    cur_h = (int)(tex_h * std::pow(ratio, tries));
+    if (8192 < cur_w || 8192 < cur_h) return -1;
+  }
+  int nuv = 3;
+  for (const OChart& c : valid) nuv += (int)c.pos.size();
+  dims[0] = cur_w;
+  dims[1] = cur_h;
+  dims[2] = nuv;
+  if (!texture) return 0;
+  std::fill(texture, texture + (size_t)cur_w * cur_h * 3, 0);
+  const float cols = (float)cur_w, rows = (float)cur_h;
+  int off = 0;
+  for (size_t k = 0; k < valid.size(); ++k) {
+    const OChart& c = valid[k];
+    const ORect& r = packed[k];
+    for (int y = 0; y < c.h; ++y)
+      std::copy(c.patch.begin() + (size_t)c.w * y * 3, c.patch.begin() + (size_t)c.w * (y + 1) * 3,
+                texture + ((size_t)cur_w * (y + r.y) + r.x) * 3);
+    for (size_t i = 0; i < c.pos.size(); ++i) {
+      uv[2 * (off + i)] = (c.pos[i].first + r.x + 0.5f) / cols;
+      uv[2 * (off + i) + 1] = 1.0f - ((c.pos[i].second + r.y + 0.5f) / rows);
+    }
+    for (const auto& fi : c.face_idx)
+      for (int j = 0; j < 3; ++j) uv_indices[3 * (size_t)fi.first + j] = off + fi.second[j];
+    off += (int)c.pos.size();
+  }
+  float iu = 0.0f, iv = 0.0f;
+  if (!avail.empty()) {
+    iu = (avail[0].x + 0.5f) / cols;
+    iv = 1.0f - ((avail[0].y + 0.5f) / rows);
+  }
+  for (int j = 0; j < 3; ++j) {
+    uv[2 * (off + j)] = iu;
+    uv[2 * (off + j) + 1] = iv;
+  }
+  for (int f : invalid_faces)
+    for (int j = 0; j < 3; ++j) uv_indices[3 * (size_t)f + j] = off + j;
+  return 0;
 }

@@ -1,11 +1,13 @@
 """TextureMapping (src/texturing/texture_mapper.cc: TextureMappingSimple
 :924-1006, RasterizeTriangle :234-292, PaddingSimple :148-201) against the
 oracle's restatement (oracle/vis_oracle.cc), texture, mask and uv bit for
-bit, for three uv types: the mesh's own uv (kUseOriginalMeshUv, through
+bit, for the four uv types: the mesh's own uv (kUseOriginalMeshUv, through
 ugu_gpu_texture_mapping), the tiled keyframe images (kGenerateSimpleTile,
-the reference's default, :62-141, through ugu_gpu_tile_images) and one
+the reference's default, :62-141, through ugu_gpu_tile_images), one
 rectangle half per face (kGenerateSimpleTriangles, :347-440, through
-ugu_gpu_texture_mapping_targets).  The face arrays are seeded: uv triangles that
+ugu_gpu_texture_mapping_targets) and bin-packed charts of keyframe patches
+(kGenerateSimpleCharts, :476-922, host layout and copies, as in the
+reference).  The face arrays are seeded: uv triangles that
 overlap heavily (a later face overwrites an earlier one), source triangles
 reaching outside their keyframe images, faces without a keyframe."""
 import numpy as np
@@ -73,13 +75,90 @@ def test_best_keyframes_by_criteria():
         vis.best_keyframes(info, 3)
 
 
-def test_texture_mapping_unbuilt_or_rejected_layouts_return_false():
+def test_texture_mapping_rejected_layouts_return_false():
     m = scenes.icosphere_textured(1, 8)
     info = vis.VisibilityInfo(m.num_vertices, m.num_faces)
-    charts = vis.TextureMappingOption(uv_type=vis.TexturingOutputUvType.kGenerateSimpleCharts)
-    assert vis.TextureMapping([], info, m, charts) is False
     tile = vis.TextureMappingOption()  # kGenerateSimpleTile, the reference's default
     assert vis.TextureMapping([], info, m, tile) is False  # no keyframe to tile
+    other = vis.TextureMappingOption(type=1)  # a mapping type the reference does not implement
+    assert vis.TextureMapping([], info, m, other) is False
+
+
+def test_bin_packing_2d_known_answer():
+    """BinPacking2D's guillotine cuts worked by hand: a 3x3 then a 2x2
+    rectangle into the 8x8 free rectangle at (1, 1); the 3x3 leaves a
+    5-wide strip (cut across the wider leftover: a 3-wide column first, then
+    its 3-high top), and the 2x2 takes the 3x5 piece under it."""
+    packed, free = vis.bin_packing_2d([(3, 3), (2, 2)], 1, 8, 1, 8)
+    assert packed == [(1, 1, 3, 3), (1, 4, 2, 2)]
+    assert free == [(4, 1, 5, 8), (1, 6, 3, 3), (3, 4, 1, 2)]
+    assert vis.bin_packing_2d([(9, 2)], 1, 8, 1, 8) is None  # wider than the space
+
+
+class _Kf:
+    def __init__(self, i, color):
+        self.id, self.color = i, color
+
+
+def _chart_case(subdiv, n_kf, size, seed, unseen=0.2):
+    """Faces of an icosphere given seeded best keyframes by region (some
+    unseen) and orthographic projected triangles inside size-sized images."""
+    m = scenes.icosphere_textured(subdiv, 8)
+    rng = np.random.default_rng(seed)
+    cen = m.vertices[m.vertex_indices].mean(1)
+    ang = np.arctan2(cen[:, 1], cen[:, 0])
+    face_kf = (((ang + np.pi) / (2 * np.pi)) * n_kf).astype(np.int32) % n_kf
+    face_kf[np.abs(cen[:, 2]) > 1.0 - unseen] = -1
+    w, h = size
+    tri = m.vertices[m.vertex_indices][:, :, :2]
+    face_tri = np.stack([(w - 1) * 0.5 * (1 + 0.98 * tri[..., 0]),
+                         (h - 1) * 0.5 * (1 + 0.98 * tri[..., 1])], -1).astype(np.float32)
+    imgs = [rng.integers(0, 256, (h, w, 3), dtype=np.uint8) for _ in range(n_kf)]
+    return m, face_kf, face_tri, imgs
+
+
+@pytest.mark.parametrize("subdiv,n_kf,size,tex,seed", [
+    (2, 3, (64, 48), 128, 1), (3, 4, (160, 120), 256, 2), (3, 2, (96, 96), 16, 3),
+    (4, 6, (200, 150), 512, 4), (1, 1, (32, 32), 64, 5)])
+def test_simple_charts_layout_matches_oracle(oracle_lib, subdiv, n_kf, size, tex, seed):
+    """kGenerateSimpleCharts in the mirror and the oracle agree bit for bit:
+    the atlas texture (patches with their replicated border, packed largest
+    first, the texture grown in sqrt(2) steps when tex x tex is too small),
+    the uv of every chart vertex and every face's uv indices, unseen faces on
+    the shared invalid uv."""
+    m, face_kf, face_tri, imgs = _chart_case(subdiv, n_kf, size, seed)
+    kfs = [_Kf(i, im) for i, im in enumerate(imgs)]
+    lay = vis.simple_charts_layout(m.vertex_indices, face_kf, face_tri, kfs, tex, tex)
+    rc, want_t, want_uv, want_uvi = oracle_lib.simple_charts(m.vertex_indices, imgs, face_kf,
+                                                             face_tri, tex, tex)
+    assert rc == 0 and lay is not None
+    t, uv, uvi, mask = lay
+    assert np.array_equal(t, want_t)
+    assert np.array_equal(uv.view(np.uint32), want_uv.view(np.uint32))
+    assert np.array_equal(uvi, want_uvi)
+    # every visible face's uv triangle lies on its chart's patch, unseen
+    # faces all on the last three (invalid) uv
+    unseen = face_kf < 0
+    if unseen.any():
+        assert (uvi[unseen] == np.arange(len(uv) - 3, len(uv))).all()
+    seen = uvi[~unseen]
+    assert seen.max() < len(uv) - 3
+    H, W = t.shape[:2]
+    px = np.rint(uv[seen][..., 0] * W - 0.5).astype(int)
+    py = np.rint((1.0 - uv[seen][..., 1]) * H - 0.5).astype(int)
+    assert (mask[py, px] == 255).all()
+
+
+def test_simple_charts_rejects_what_the_reference_overruns(oracle_lib):
+    """A chart whose projected triangles reach outside its keyframe image
+    would make the reference copy from outside the image: both refuse."""
+    m, face_kf, face_tri, imgs = _chart_case(2, 2, (64, 48), 7)
+    face_tri = face_tri.copy()
+    face_tri[np.flatnonzero(face_kf >= 0)[0], 0, 0] = 70.0
+    kfs = [_Kf(i, im) for i, im in enumerate(imgs)]
+    assert vis.simple_charts_layout(m.vertex_indices, face_kf, face_tri, kfs, 128, 128) is None
+    rc, *_ = oracle_lib.simple_charts(m.vertex_indices, imgs, face_kf, face_tri, 128, 128)
+    assert rc == -2
 
 
 @pytest.mark.parametrize("faces,size", [(5, (64, 64)), (1, (16, 16)), (2000, (512, 384)),
@@ -243,7 +322,8 @@ def test_gpu_simple_triangles_matches_oracle(gpu_lib, oracle_lib, size):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("uv_type", [vis.TexturingOutputUvType.kGenerateSimpleTile,
-                                     vis.TexturingOutputUvType.kGenerateSimpleTriangles])
+                                     vis.TexturingOutputUvType.kGenerateSimpleTriangles,
+                                     vis.TexturingOutputUvType.kGenerateSimpleCharts])
 def test_gpu_texture_mapping_atlas_pipeline(gpu_lib, oracle_lib, uv_type):
     """VisibilityTester, then TextureMapping with a generated atlas through
     the mirror: texture and uv equal the oracle's; the re-textured mesh then
@@ -263,9 +343,14 @@ def test_gpu_texture_mapping_atlas_pipeline(gpu_lib, oracle_lib, uv_type):
     opt = vis.TextureMappingOption(uv_type=uv_type, tex_w=512, tex_h=512)
     face_kf, face_tri = vis.best_keyframes(info, opt.criteria)
     assert (face_kf >= 0).mean() > 0.3
+    want_uvi = None
     if uv_type == vis.TexturingOutputUvType.kGenerateSimpleTile:
         rc, want_t, want_uv = oracle_lib.simple_tile([f.id for f in frames],
                                                      [f.color for f in frames], face_kf, face_tri)
+        want_m = None
+    elif uv_type == vis.TexturingOutputUvType.kGenerateSimpleCharts:
+        rc, want_t, want_uv, want_uvi = oracle_lib.simple_charts(
+            m.vertex_indices, [f.color for f in frames], face_kf, face_tri, 512, 512)
         want_m = None
     else:
         rc, want_t, want_m, want_uv = oracle_lib.simple_triangles(
@@ -276,6 +361,8 @@ def test_gpu_texture_mapping_atlas_pipeline(gpu_lib, oracle_lib, uv_type):
     assert np.array_equal(m.uv.view(np.uint32), want_uv.view(np.uint32))
     if want_m is not None:
         assert np.array_equal(m.texture_mask, want_m)
+    if want_uvi is not None:
+        assert np.array_equal(m.uv_indices, want_uvi)
     assert list(np.unique(m.material_ids)) == [0]
     # the atlas in use: render the re-textured mesh
     ropt = RendererCpuOption(diffuse_color=1, interp=1, shading_normal=1, backface_culling=True)

@@ -574,6 +574,162 @@ def simple_triangles_layout(face_kf, tex_w: int, tex_h: int):
     return target, uv.reshape(-1, 2)
 
 
+def bin_packing_2d(rects, x_min: int, x_max: int, y_min: int, y_max: int):
+    """BinPacking2D (src/discrete/bin_packer_2d.cc:14-113): guillotine
+    packing of (width, height) rectangles in the given order into the free
+    rectangle (x_min, y_min, x_max, y_max) (x, y, width, height).  Each
+    rectangle takes the free one whose area exceeds its own the least
+    (the first of equals); a larger one is cut across the longer leftover
+    side, the remainder appended before the piece, until one fits exactly.
+    Returns (packed (x, y, w, h) list, free rectangles), or None when a
+    rectangle finds no room."""
+    free = [(x_min, y_min, x_max, y_max)]
+    packed = []
+    for (w, h) in rects:
+        while True:
+            best, best_i = None, -1
+            best_diff = 2 ** 31 - 1
+            for i, (fx, fy, fw, fh) in enumerate(free):
+                if h <= fh and w <= fw and fw * fh - w * h < best_diff:
+                    best_diff = fw * fh - w * h
+                    best, best_i = (fx, fy, fw, fh), i
+            if best_i < 0 or best[2] * best[3] < w * h:
+                return None
+            fx, fy, fw, fh = best
+            if fw == w and fh == h:
+                packed.append(best)
+                del free[best_i]
+                break
+            if fh - h > fw - w:  # CutRect: across the longer leftover side
+                cut1, cut2 = (fx, fy, fw, h), (fx, fy + h, fw, fh - h)
+            else:
+                cut1, cut2 = (fx, fy, w, fh), (fx + w, fy, fw - w, fh)
+            del free[best_i]
+            free.append(cut2)
+            free.append(cut1)
+    return packed, free
+
+
+def simple_charts_layout(vertex_indices, face_kf, face_tri, keyframes, tex_w: int, tex_h: int):
+    """GenerateSimpleChartsTextureAndUv with GenerateAtlas
+    (texture_mapper.cc:476-922): charts are the faces reachable from the
+    lowest unselected face over shared edges (FaceAdjacency,
+    include/ugu/face_adjacency.h: a face's neighbours own the reversed
+    directed edges; duplicate directed edges sum, as setFromTriplets does)
+    that have the seed's best keyframe.  A visible chart's patch is the
+    bounding box of its projected triangles (floor / ceil) copied from the
+    keyframe image with a 1-texel border replicated (PaddingBorderSimple);
+    its vertices keep one texture position each (the first face's, in
+    vertex order as std::map keeps them).  Visible charts are packed by
+    patch area, largest first (std::sort; the mirror's sort is stable, so
+    charts of equal area keep their chart order where libstdc++'s is
+    unspecified), with BinPacking2D into the texture less a 1-texel edge,
+    which grows by sqrt(2) steps up to 8192 until everything fits.  Faces
+    of unseen charts share one uv at the first free rectangle (or 0, 0).
+    Returns (texture H x W x 3, uv, uv_indices F x 3, mask H x W: 255 on
+    the patches), or None where the reference fails (no packing within 8192) or reads past its arrays (a
+    patch outside its keyframe image, an edge sum naming no face)."""
+    from collections import deque
+    vi = np.asarray(vertex_indices, np.int64)
+    F = len(vi)
+    edges = {}
+    for f in range(F):
+        a, b, c = (int(x) for x in vi[f])
+        for e in ((a, b), (b, c), (c, a)):
+            edges[e] = edges.get(e, 0) + f + 1
+    selected = np.zeros(F, bool)
+    charts = []  # (kf, faces) in the order of their seeds
+    for seed in range(F):
+        if selected[seed]:
+            continue
+        kf = int(face_kf[seed])
+        faces = [seed]
+        selected[seed] = True
+        queue = deque([seed])
+        while queue:
+            fid = queue.popleft()
+            a, b, c = (int(x) for x in vi[fid])
+            adjacent = [edges.get(e, 0) - 1 for e in ((b, a), (c, b), (a, c))]
+            adjacent = [g for g in adjacent if g >= 0]
+            for e in ((a, b), (b, c), (c, a)):  # RemoveFace
+                if e in edges:
+                    edges[e] = 0
+            if any(g >= F for g in adjacent):
+                return None
+            add = [g for g in adjacent if int(face_kf[g]) == kf and not selected[g]]
+            for g in add:
+                queue.append(g)
+                faces.append(g)
+                selected[g] = True
+        charts.append((kf, faces))
+    pad = 1
+    valid = []  # (area, patch, vertex ids, positions, face uv-index lists)
+    invalid_faces = []
+    for kf, faces in charts:
+        if kf < 0:
+            invalid_faces.extend(faces)
+            continue
+        tris = np.asarray(face_tri, F32)[faces]  # n x 3 x 2
+        xmin, xmax = int(math.floor(tris[:, :, 0].min())), int(math.ceil(tris[:, :, 0].max()))
+        ymin, ymax = int(math.floor(tris[:, :, 1].min())), int(math.ceil(tris[:, :, 1].max()))
+        img = keyframes[kf].color
+        if xmin < 0 or ymin < 0 or xmax >= img.shape[1] or ymax >= img.shape[0]:
+            return None
+        ph, pw = ymax - ymin + 1 + 2 * pad, xmax - xmin + 1 + 2 * pad
+        patch = np.zeros((ph, pw, 3), np.uint8)
+        patch[pad:pad + ymax - ymin + 1, pad:pad + xmax - xmin + 1] = img[ymin:ymax + 1,
+                                                                          xmin:xmax + 1]
+        patch[:pad] = patch[pad]  # PaddingBorderSimple (:203-231)
+        patch[ph - pad:] = patch[ph - pad - 1]
+        patch[:, :pad] = patch[:, pad:pad + 1]
+        patch[:, pw - pad:] = patch[:, pw - pad - 1:pw - pad]
+        pos = {}
+        for k, f in enumerate(faces):
+            for j in range(3):
+                p = (F32(tris[k, j, 0]) - F32(xmin) + F32(pad),
+                     F32(tris[k, j, 1]) - F32(ymin) + F32(pad))
+                pos.setdefault(int(vi[f, j]), p)
+        vids = sorted(pos)
+        new = {v: i for i, v in enumerate(vids)}
+        valid.append((ph * pw, patch, [pos[v] for v in vids],
+                      [(f, [new[int(vi[f, j])] for j in range(3)]) for f in faces]))
+    valid.sort(key=lambda c: -c[0])
+    rects = [(c[1].shape[1], c[1].shape[0]) for c in valid]
+    cur_w, cur_h, tries = int(tex_w), int(tex_h), 0
+    ratio = float(F32(math.sqrt(2.0)))
+    while True:
+        got = bin_packing_2d(rects, 1, cur_w - 1, 1, cur_h - 1)
+        if got is not None:
+            break
+        tries += 1
+        cur_w = int(tex_w * math.pow(ratio, tries))
+        cur_h = int(tex_h * math.pow(ratio, tries))
+        if 8192 < cur_w or 8192 < cur_h:
+            return None
+    packed, free = got
+    tex = np.zeros((cur_h, cur_w, 3), np.uint8)
+    mask = np.zeros((cur_h, cur_w), np.uint8)
+    uv = []
+    uv_indices = np.zeros((F, 3), np.int32)
+    cols, rows = F32(cur_w), F32(cur_h)
+    for (area, patch, positions, face_idx), (rx, ry, rw, rh) in zip(valid, packed):
+        tex[ry:ry + patch.shape[0], rx:rx + patch.shape[1]] = patch
+        mask[ry:ry + patch.shape[0], rx:rx + patch.shape[1]] = 255
+        off = len(uv)
+        for (px, py) in positions:
+            uv.append(((px + F32(rx) + F32(0.5)) / cols,
+                       F32(1.0) - ((py + F32(ry) + F32(0.5)) / rows)))
+        for f, idx in face_idx:
+            uv_indices[f] = [off + k for k in idx]
+    inv = (F32(0.0), F32(0.0))
+    if free:
+        inv = ((F32(free[0][0]) + F32(0.5)) / cols, F32(1.0) - ((F32(free[0][1]) + F32(0.5)) / rows))
+    uv.extend([inv, inv, inv])
+    for f in invalid_faces:
+        uv_indices[f] = [len(uv) - 3, len(uv) - 2, len(uv) - 1]
+    return tex, np.asarray(uv, F32).reshape(-1, 2), uv_indices, mask
+
+
 def _keyframe_descs(keyframes):
     descs, keep = [], []
     for kf in keyframes:
@@ -600,15 +756,21 @@ def TextureMapping(keyframes, info: VisibilityInfo, mesh, option: TextureMapping
       kGenerateSimpleTriangles: every visible face drawn on the GPU into
         its own half-rectangle of a tex_h x tex_w texture
         (simple_triangles_layout, ugu_gpu_texture_mapping_targets), padded
-        with a 3-texel window; new uv and uv indices.
+        with a 3-texel window; new uv and uv indices;
+      kGenerateSimpleCharts: charts of edge-connected faces sharing a best
+        keyframe, each a padded bounding-box patch of that keyframe's image,
+        bin-packed into a texture that grows from tex_h x tex_w as needed
+        (simple_charts_layout: host work, as in the reference); new uv and
+        uv indices.
     Like the reference, it sets the mesh's one material to the texture and
-    every face's material id to 0; the texture's mask (255 where a face or
-    the padding wrote; all 255 for tiles) is left in mesh.texture_mask.
-    kGenerateSimpleCharts is not built (False, like an unimplemented type),
-    and neither is a layout the reference rejects or would overrun."""
+    every face's material id to 0; the texture's mask (255 where a face, a
+    patch or the padding wrote; all 255 for tiles) is left in
+    mesh.texture_mask.  A layout the reference rejects or would overrun
+    returns False."""
     if option.type != 0 or option.uv_type not in (TexturingOutputUvType.kGenerateSimpleTile,
                                                   TexturingOutputUvType.kUseOriginalMeshUv,
-                                                  TexturingOutputUvType.kGenerateSimpleTriangles):
+                                                  TexturingOutputUvType.kGenerateSimpleTriangles,
+                                                  TexturingOutputUvType.kGenerateSimpleCharts):
         return False
     face_kf, face_tri = best_keyframes(info, option.criteria)
     F = len(mesh.vertex_indices)
@@ -628,6 +790,19 @@ def TextureMapping(keyframes, info: VisibilityInfo, mesh, option: TextureMapping
         mesh.textures_f32 = [None]
         mesh.material_ids = np.zeros(F, np.int32)
         mesh.texture_mask = np.full(tex.shape[:2], 255, np.uint8)
+        return True
+    if option.uv_type == TexturingOutputUvType.kGenerateSimpleCharts:
+        lay = simple_charts_layout(mesh.vertex_indices, face_kf, face_tri, keyframes,
+                                   int(option.tex_w), int(option.tex_h))
+        if lay is None:
+            return False
+        tex, uv, uv_indices, mask = lay
+        mesh.uv = uv
+        mesh.uv_indices = uv_indices
+        mesh.textures = [tex]
+        mesh.textures_f32 = [None]
+        mesh.material_ids = np.zeros(F, np.int32)
+        mesh.texture_mask = mask
         return True
     if option.uv_type == TexturingOutputUvType.kGenerateSimpleTriangles:
         lay = simple_triangles_layout(face_kf, int(option.tex_w), int(option.tex_h))
