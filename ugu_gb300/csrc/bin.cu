@@ -9,12 +9,16 @@
 //            (rasterizer.cc:163-193) from the table and the screen tiles the
 //            face's bbox touches; a warp's entries of one tile are added to
 //            the tile's count with one atomic.
-//   k_scan   exclusive scan of the per-tile counts into entry offsets, so the
-//            entry buffer holds exactly the render's (face, tile) pairs.
+//   k_scan_sum, k_scan_apply
+//            exclusive scan of the per-tile counts into entry offsets, so the
+//            entry buffer holds exactly the render's (face, tile) pairs: each
+//            chunk of 4,096 tiles summed, then scanned from the sums before it.
 //   k_place  the same pass again: each entry goes straight to its place in
 //            its tile's range, faces drawn first from the front and faces
 //            drawn last from the back, one atomic per warp, tile and class.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "internal.cuh"
 #include "tilecommon.cuh"
@@ -28,9 +32,10 @@ using tiled::kU64;
 using tiled::setup_proj;
 
 constexpr int kBinThreads = 256;
-constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 32;   // tile counts per scan thread and round
-constexpr int kScanRound = kScanThreads * kScanItems;
+constexpr int kScanThreads = 256;
+constexpr int kScanWarps = kScanThreads / 32;
+constexpr int kScanItems = 16;  // tile counts per scan thread
+constexpr int kScanChunk = kScanThreads * kScanItems;
 
 // A lower bound of the depth Loop B computes for the face at any covered
 // pixel: the three edge functions carry rounding errors of at most
@@ -190,82 +195,122 @@ __global__ void __launch_bounds__(kBinThreads, 8) k_place(TileParams p) {
   bin_pass<kFaces, true>(p);
 }
 
-// Exclusive scan of the per-tile counts (one block, kScanItems consecutive
-// tiles per thread and round, staged through shared memory so that global
-// accesses coalesce; the staging index skips one word in 33 so that a
-// thread's run of 32 sits in 32 different banks); zeroes the counts for the
-// next render and flags a render whose entries exceed the buffer.
+// Exclusive scan of the per-tile counts in chunks of kScanChunk tiles, one
+// block per chunk: k_scan_sum sums each chunk, k_scan_apply scans its chunk
+// from the sum of the chunks before it.  A block's counts are staged through
+// shared memory so that global accesses coalesce, kScanItems consecutive
+// tiles per thread (the staging index skips one word in 33, so that a
+// thread's run sits in different banks).  k_scan_apply zeroes the counts for
+// the next render, and its last block flags a render whose entries exceed
+// the buffer.
 __device__ __forceinline__ int skew(int i) { return i + (i >> 5); }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(TileParams p) {
-  extern __shared__ int stage[];  // skew(kScanRound) words
-  __shared__ long long warp_sum[kScanThreads / 32];
+// A block's sum of one value per thread (every thread gets it).
+__device__ __forceinline__ long long block_sum(long long v, long long* warp_part) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();  // warp_part may still be read from a previous use
+  if (lane == 0) warp_part[warp] = v;
+  __syncthreads();
+  long long t = 0;
+#pragma unroll
+  for (int w = 0; w < kScanWarps; ++w) t += warp_part[w];
+  return t;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_sum(TileParams p) {
+  __shared__ long long warp_part[kScanWarps];
+  const int T = p.total_tiles, tid = threadIdx.x;
+  const int r0 = blockIdx.x * kScanChunk;
+  long long v = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int t = r0 + k * kScanThreads + tid;
+    if (t < T) v += p.tile_count[t];
+  }
+  v = block_sum(v, warp_part);
+  if (tid == 0) p.chunk_sums[blockIdx.x] = v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(TileParams p) {
+  __shared__ int stage[kScanChunk + kScanChunk / 32];  // skew(kScanChunk) words
+  __shared__ long long warp_part[kScanWarps];
   const int T = p.total_tiles;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = blockIdx.x * kScanChunk;
+  // the entries of the chunks before this one
   long long carry = 0;
-  for (int r0 = 0; r0 < T; r0 += kScanRound) {
-    for (int i = tid; i < kScanRound; i += kScanThreads) {
-      const int t = r0 + i;
-      stage[skew(i)] = t < T ? p.tile_count[t] : 0;
+  for (int j = tid; j < (int)blockIdx.x; j += kScanThreads) carry += p.chunk_sums[j];
+  carry = block_sum(carry, warp_part);
+  {
+    // every load issued before the first store, so that the thread waits
+    // for one memory latency and not one per count
+    int c[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      const int t = r0 + k * kScanThreads + tid;
+      c[k] = t < T ? p.tile_count[t] : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      const int t = r0 + k * kScanThreads + tid;
+      stage[skew(k * kScanThreads + tid)] = c[k];
       if (t < T) p.tile_count[t] = 0;
     }
-    __syncthreads();
-    int v[kScanItems];
-    long long own = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-      v[k] = stage[skew(tid * kScanItems + k)];
-      own += v[k];
-    }
-    long long x = own;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sum[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      long long w = warp_sum[lane];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const long long y = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += y;
-      }
-      warp_sum[lane] = w;
-    }
-    __syncthreads();
-    long long run = carry + x - own + (warp ? warp_sum[warp - 1] : 0);
-    const long long round_total = warp_sum[kScanThreads / 32 - 1];
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-      stage[skew(tid * kScanItems + k)] = (int)run;  // offsets stay below the entry capacity
-      run += v[k];
-    }
-    __syncthreads();
-    for (int i = tid; i < kScanRound; i += kScanThreads) {
-      const int t = r0 + i;
-      if (t >= T) break;
-      const int off = stage[skew(i)];
-      const int nxt = i + 1 < kScanRound ? stage[skew(i + 1)] : (int)(carry + round_total);
-      p.tile_off[t] = off;
-      p.tile_lo[t] = off;
-      p.tile_hi[t] = nxt;
-    }
-    carry += round_total;
-    __syncthreads();
   }
-  if (tid == 0) {
-    p.tile_off[T] = (int)carry;
-    p.counters->total_entries = (unsigned long long)carry;  // the render's entry count
-    if (carry > p.entry_cap) {
+  __syncthreads();
+  int v[kScanItems];
+  long long own = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = stage[skew(tid * kScanItems + k)];
+    own += v[k];
+  }
+  long long x = own;  // inclusive scan of the threads' sums: warps, then the block
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();  // warp_part's sums above have been read
+  if (lane == 31) warp_part[warp] = x;
+  __syncthreads();
+  long long before = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < kScanWarps; ++w) {
+    const long long sw = warp_part[w];
+    if (w < warp) before += sw;
+    total += sw;
+  }
+  long long run = carry + before + x - own;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    stage[skew(tid * kScanItems + k)] = (int)run;  // offsets stay below the entry capacity
+    run += v[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int i = k * kScanThreads + tid;
+    const int t = r0 + i;
+    if (t >= T) break;
+    const int off = stage[skew(i)];
+    const int nxt = i + 1 < kScanChunk ? stage[skew(i + 1)] : (int)(carry + total);
+    p.tile_off[t] = off;
+    p.tile_lo[t] = off;
+    p.tile_hi[t] = nxt;
+  }
+  if (blockIdx.x == gridDim.x - 1 && tid == 0) {
+    const long long all = carry + total;
+    p.tile_off[T] = (int)all;
+    p.counters->total_entries = (unsigned long long)all;  // the render's entry count
+    if (all > p.entry_cap) {
       p.counters->dropped = 1ull;
       if (p.sticky) atomicOr(p.sticky, kStickyOverflow);
     }
   }
 }
-
-constexpr size_t kScanSmem = sizeof(int) * (kScanRound + kScanRound / 32);
 
 }  // namespace
 
@@ -297,12 +342,12 @@ void launch_size(const TileParams& p, int max_faces, cudaStream_t s) {
                   p.num_views),
              kBinThreads, 0, s>>>(p);
   if (max_faces > 0) launch_pass(p, max_faces, false, s);
-  k_scan<<<1, kScanThreads, kScanSmem, s>>>(p);
+  const int chunks = std::max(1, (p.total_tiles + kScanChunk - 1) / kScanChunk);
+  k_scan_sum<<<chunks, kScanThreads, 0, s>>>(p);
+  k_scan_apply<<<chunks, kScanThreads, 0, s>>>(p);
 }
 
-void bin_kernels_init() {
-  cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanSmem);
-}
+int64_t scan_chunks(int64_t tiles) { return std::max<int64_t>(1, (tiles + kScanChunk - 1) / kScanChunk); }
 
 void launch_bin(const TileParams& p, int max_faces, cudaStream_t s) {
   launch_size(p, max_faces, s);

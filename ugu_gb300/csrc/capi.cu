@@ -83,6 +83,7 @@ struct Scratch {
   // tiled path
   int32_t* tile_count = nullptr;  // 4 arrays: count, offsets (+1), lo cursor, hi cursor
   size_t tiles_cap = 0;
+  long long* chunk_sums = nullptr;  // the tile-count scan's chunk sums, for tiles_cap tiles
   int2* entries = nullptr;  // entries_cap entries in tile order
   size_t entries_cap = 0;
   size_t entries_min = 0;  // capacity asked for by the last overflow
@@ -222,6 +223,7 @@ void free_scratch(Scratch& s) {
   cudaFreeHost(s.h_views);
   cudaFree(s.d_out);
   cudaFree(s.tile_count);
+  cudaFree(s.chunk_sums);
   cudaFree(s.entries);
   cudaFree(s.proj);
   cudaFree(s.tcounters);
@@ -482,10 +484,14 @@ int ensure_tiled(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& gro
   }
   if (tiles > s.tiles_cap) {
     cudaFree(s.tile_count);
+    cudaFree(s.chunk_sums);
     s.tile_count = nullptr;
+    s.chunk_sums = nullptr;
     s.tiles_cap = 0;
     CK(ctx, cudaMalloc(&s.tile_count, (4 * tiles + 1) * sizeof(int32_t)),
        "cudaMalloc(tile offsets)");
+    CK(ctx, cudaMalloc(&s.chunk_sums, scan_chunks((int64_t)tiles) * sizeof(long long)),
+       "cudaMalloc(scan chunk sums)");
     s.tiles_cap = tiles;
     s.tiles_dirty = true;
   }
@@ -642,6 +648,7 @@ TileParams tile_params(ugu_gpu_context* ctx, Scratch& s, const Group& gr, size_t
   p.tile_lo = p.tile_off + s.tiles_cap + 1;
   p.tile_hi = p.tile_lo + s.tiles_cap;
   p.entries = s.entries;
+  p.chunk_sums = s.chunk_sums;
   p.counters = s.tcounters + gi;
   p.sticky = ctx->sticky_on ? ctx->d_sticky : nullptr;
   return p;
@@ -1090,7 +1097,6 @@ int ugu_gpu_create(int32_t device, ugu_gpu_context** out) {
   ctx->stream = ctx->own_stream;
   // occupancy queries happen here, never inside a stream capture
   tile_kernel_blocks_per_sm();
-  bin_kernels_init();
   ctx->opt.diffuse_color = 0;
   ctx->opt.interp = 1;
   ctx->opt.shading_normal = 1;

@@ -140,7 +140,8 @@ struct TileCounters {
 };
 
 // Tiled-path buffers.  k_count counts every tile's (face, tile) entries,
-// k_scan turns the counts into offsets and k_place places the entries:
+// k_scan_sum and k_scan_apply turn the counts into offsets and k_place places
+// the entries:
 // per global tile t, those of the faces drawn first in [tile_off[t],
 // tile_lo[t]) and those of the faces drawn last in [tile_lo[t],
 // tile_off[t + 1]).  An entry is (the face's number in the binning order
@@ -158,11 +159,12 @@ struct TileParams {
   int32_t bin_faces;    // binning: faces per thread (1, 2 or 4)
   int64_t entry_cap;    // entries the entry buffer holds
   float4* proj;         // projected vertices (x, y, camera z, 0) of every view
-  int32_t* tile_count;  // entries per tile (k_count adds; k_scan reads and zeroes)
+  int32_t* tile_count;  // entries per tile (k_count adds; k_scan_apply reads and zeroes)
   int32_t* tile_off;    // total_tiles + 1 offsets into entries
   int32_t* tile_lo;     // first-drawn cursor / boundary per tile
   int32_t* tile_hi;     // last-drawn cursor per tile
   int2* entries;        // entries in tile order
+  long long* chunk_sums;  // entries of each chunk of 4,096 tiles (scan_chunks(total_tiles))
   TileCounters* counters;
   unsigned long long* sticky;  // as RenderParams::sticky
 };
@@ -286,10 +288,9 @@ void launch_bin(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_size(const TileParams& p, int max_faces, cudaStream_t s);
 void launch_tile(const TileParams& p, int grid, cudaStream_t s);
 int tile_kernel_blocks_per_sm();
-// One-time kernel attributes of the binning kernels (the scan's shared
-// memory); called when a context is created.
-void bin_kernels_init();
-constexpr int kBinKernels = 4;
+constexpr int kBinKernels = 5;
+// Chunks of the tile-count scan for `tiles` tiles (TileParams::chunk_sums).
+int64_t scan_chunks(int64_t tiles);
 
 // Host-side launchers (raster.cu).
 void launch_raster(const RenderParams& p, int max_faces, int num_sms, cudaStream_t s);

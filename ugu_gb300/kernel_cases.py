@@ -5,9 +5,9 @@ times, for profiling one kernel at a time (for example under
     python -m ugu_gb300.kernel_cases --case tiled --repeat 3
 
 Cases (the kernels each one launches):
-  tiled       k_proj, k_count, k_scan, k_place, k_tile: a CUDA-graph replay of
-              `views` ring views of icosphere-7 (2048^2 RGB8 texture,
-              bilinear, vertex normals, culling on)
+  tiled       k_proj, k_count, k_scan_sum, k_scan_apply, k_place, k_tile:
+              a CUDA-graph replay of `views` ring views of icosphere-7
+              (2048^2 RGB8 texture, bilinear, vertex normals, culling on)
   global      k_raster, k_tiles, k_resolve: the same views on the global
               z-buffer path
   noalloc     the global path's kernels through ugu_gpu_render_noalloc, one
