@@ -12,6 +12,7 @@
 #include <memory>
 #include <vector>
 
+#include "ugu/discrete/bin_packer_2d.h"
 #include "ugu/renderer/cpu/rasterizer.h"
 #include "ugu/renderer/cpu/raytracer.h"
 
@@ -192,6 +193,33 @@ int ref_raytrace(const ref_mesh* m, int width, int height, float fx, float fy, f
                  float* cam_out) {
   return render_with<ugu::Raytracer>(m, width, height, fx, fy, cx, cy, c2w, o, color, depth,
                                      normal, mask, face_id, cam_out);
+}
+
+// ugu::BinPacking2D (src/discrete/bin_packer_2d.cc) on n integer rects
+// (x, y, width, height each): packed receives n rects, free_rects the
+// available rects left (at most free_cap; *n_free says how many there are).
+// Returns 1 when every rect was packed, 0 otherwise.
+int ref_bin_packing_2d(const int* rects, int n, int x_min, int x_max, int y_min, int y_max,
+                       int* packed, int* free_rects, int free_cap, int* n_free) {
+  std::vector<ugu::Rect> in;
+  for (int i = 0; i < n; ++i)
+    in.emplace_back(rects[4 * i], rects[4 * i + 1], rects[4 * i + 2], rects[4 * i + 3]);
+  std::vector<ugu::Rect> out, avail;
+  const bool ok = ugu::BinPacking2D(in, &out, &avail, x_min, x_max, y_min, y_max);
+  for (size_t i = 0; i < out.size() && (int)i < n; ++i) {
+    packed[4 * i] = out[i].x;
+    packed[4 * i + 1] = out[i].y;
+    packed[4 * i + 2] = out[i].width;
+    packed[4 * i + 3] = out[i].height;
+  }
+  *n_free = (int)avail.size();
+  for (size_t i = 0; i < avail.size() && (int)i < free_cap; ++i) {
+    free_rects[4 * i] = avail[i].x;
+    free_rects[4 * i + 1] = avail[i].y;
+    free_rects[4 * i + 2] = avail[i].width;
+    free_rects[4 * i + 3] = avail[i].height;
+  }
+  return ok ? 1 : 0;
 }
 
 }  // extern "C"

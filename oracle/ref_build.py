@@ -52,9 +52,10 @@ _lib = None
 def load():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
-            if build_if_available() is None:
-                return None
+        # make rebuilds only what changed; without the reference checkout an
+        # existing build is used as it is
+        if build_if_available() is None and not os.path.exists(LIB):
+            return None
         lib = C.CDLL(LIB)
         for f in (lib.ref_render, lib.ref_raytrace, lib.ref_render_timed):
             f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
@@ -130,3 +131,26 @@ def _render(fn, mesh, cam, opt, timed=False):
         return rc, out, times
     return rc, out, {"w2c_R": camf[0:9].reshape(3, 3).copy(), "w2c_t": camf[9:12].copy(),
                      "c2w_R": camf[12:21].reshape(3, 3).copy()}
+
+
+def bin_packing_2d(rects, x_min, x_max, y_min, y_max):
+    """ugu::BinPacking2D (src/discrete/bin_packer_2d.cc), the reference's own
+    code, on integer (x, y, width, height) rects: (ok, packed rects, free
+    rects), or None without the reference build."""
+    lib = load()
+    if lib is None:
+        return None
+    f = lib.ref_bin_packing_2d
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                  C.c_void_p, C.c_int, C.c_void_p]
+    r = np.ascontiguousarray(np.asarray(rects, np.int32).reshape(-1, 4))
+    n = len(r)
+    packed = np.zeros((n, 4), np.int32)
+    cap = 4 * n + 8  # each placement turns one free rect into at most two
+    free = np.zeros((cap, 4), np.int32)
+    n_free = C.c_int(0)
+    ok = f(r.ctypes.data, n, x_min, x_max, y_min, y_max, packed.ctypes.data, free.ctypes.data,
+           cap, C.byref(n_free))
+    return bool(ok), [tuple(int(v) for v in x) for x in packed], \
+        [tuple(int(v) for v in x) for x in free[:min(n_free.value, cap)]]

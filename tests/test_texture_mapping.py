@@ -95,6 +95,37 @@ def test_bin_packing_2d_known_answer():
     assert vis.bin_packing_2d([(9, 2)], 1, 8, 1, 8) is None  # wider than the space
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_bin_packing_2d_pinned_to_the_reference(seed):
+    """The mirror's BinPacking2D against the reference's own
+    (src/discrete/bin_packer_2d.cc, built into oracle/_ref): the same packed
+    and free rectangles, in the same order, or both failing.  Seeded
+    rectangle lists, sorted by area as the chart atlas sorts them or not,
+    into spaces from roomy to too small; runs where the reference checkout
+    is present."""
+    ref_build = pytest.importorskip("oracle.ref_build")
+    if not ref_build.available():
+        pytest.skip("reference sources not present")
+    rng = np.random.default_rng(100 + seed)
+    cases = [([(3, 3), (2, 2)], (1, 8, 1, 8)), ([(9, 2)], (1, 8, 1, 8))]
+    for space in (64, 128, 256):
+        n = int(rng.integers(5, 60))
+        rects = [(int(w), int(h)) for w, h in rng.integers(1, 40, (n, 2))]
+        if seed % 2 == 0:
+            rects.sort(key=lambda r: -r[0] * r[1])
+        cases.append((rects, (1, space - 1, 1, space - 1)))
+    for rects, (x0, x1, y0, y1) in cases:
+        ok, r_packed, r_free = ref_build.bin_packing_2d([(0, 0, w, h) for w, h in rects],
+                                                        x0, x1, y0, y1)
+        mine = vis.bin_packing_2d(rects, x0, x1, y0, y1)
+        if not ok:
+            assert mine is None, (rects, x0, x1)
+            continue
+        assert mine is not None, (rects, x0, x1)
+        assert mine[0] == r_packed
+        assert mine[1] == r_free
+
+
 class _Kf:
     def __init__(self, i, color):
         self.id, self.color = i, color
