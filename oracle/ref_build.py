@@ -154,3 +154,70 @@ def bin_packing_2d(rects, x_min, x_max, y_min, y_max):
            cap, C.byref(n_free))
     return bool(ok), [tuple(int(v) for v in x) for x in packed], \
         [tuple(int(v) for v in x) for x in free[:min(n_free.value, cap)]]
+
+
+class RefKeyframe(C.Structure):
+    _fields_ = [("id", C.c_int), ("width", C.c_int), ("height", C.c_int),
+                ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("c2w", C.c_double * 16), ("color", C.c_void_p), ("depth", C.c_void_p),
+                ("mask", C.c_void_p)]
+
+
+class RefVisOption(C.Structure):
+    _fields_ = [("backface_culling_angle_rad_th", C.c_float), ("use_mask", C.c_int),
+                ("use_depth", C.c_int), ("interp", C.c_int), ("calc_stat_vertex_info", C.c_int),
+                ("collect_face_info", C.c_int), ("calc_stat_face_info", C.c_int),
+                ("max_viewing_angle", C.c_float),
+                ("max_distance_from_camera_to_vertex", C.c_float),
+                ("max_depth_difference", C.c_float), ("eps", C.c_float),
+                ("invalid_color", C.c_float * 3)]
+
+
+def visibility(vertices, normals, faces, keyframes, option, facewise):
+    """ugu::VisibilityTester::Test(keyframes, info, facewise)
+    (src/texturing/visibility_tester.cc), the reference's own code, for
+    keyframes = [(id, camera, color, depth or None, mask or None)] and
+    option = VisibilityTesterOption fields.  Returns the VisibilityInfo as
+    arrays (see ref_visibility.cc), or None without the reference build."""
+    lib = load()
+    if lib is None:
+        return None
+    V = np.ascontiguousarray(vertices, np.float32)
+    N = np.ascontiguousarray(normals, np.float32)
+    F = np.ascontiguousarray(faces, np.int32)
+    K, nv, nf = len(keyframes), len(V), len(F)
+    keep = []
+    kfs = (RefKeyframe * K)()
+    for i, (kid, cam, color, depth, mask) in enumerate(keyframes):
+        k = kfs[i]
+        k.id, k.width, k.height = int(kid), int(cam.width), int(cam.height)
+        k.fx, k.fy, k.cx, k.cy = float(cam.fx), float(cam.fy), float(cam.cx), float(cam.cy)
+        k.c2w[:] = [float(x) for x in np.asarray(cam.c2w, np.float64).reshape(-1)]
+        for name, a, dt in (("color", color, np.uint8), ("depth", depth, np.float32),
+                            ("mask", mask, np.uint8)):
+            if a is not None:
+                a = np.ascontiguousarray(a, dt)
+                keep.append(a)
+                setattr(k, name, a.ctypes.data)
+    o = RefVisOption(float(option.backface_culling_angle_rad_th), int(option.use_mask),
+                     int(option.use_depth), int(option.interp),
+                     int(option.calc_stat_vertex_info), int(option.collect_face_info),
+                     int(option.calc_stat_face_info), float(option.max_viewing_angle),
+                     float(option.max_distance_from_camera_to_vertex),
+                     float(option.max_depth_difference), float(option.eps),
+                     (C.c_float * 3)(0.0, 0.0, 0.0))
+    out = {"vcount": np.zeros(nv, np.int32), "vrec_id": np.zeros((nv, K), np.int32),
+           "vrec": np.zeros((nv, K, 9), np.float32), "vstat_i": np.zeros((nv, 5), np.int32),
+           "vstat": np.zeros((nv, 43), np.float32), "fcount": np.zeros(nf, np.int32),
+           "frec_id": np.zeros((nf, K, 2), np.int32), "frec": np.zeros((nf, K, 9), np.float32),
+           "fstat_i": np.zeros((nf, 6), np.int32), "fstat": np.zeros((nf, 3), np.float32)}
+    f = lib.ref_visibility
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                  C.c_void_p, C.c_int] + [C.c_void_p] * 10
+    rc = f(V.ctypes.data, nv, N.ctypes.data, F.ctypes.data, nf, C.addressof(kfs), K,
+           C.addressof(o), 1 if facewise else 0,
+           *[out[k].ctypes.data for k in ("vcount", "vrec_id", "vrec", "vstat_i", "vstat",
+                                          "fcount", "frec_id", "frec", "fstat_i", "fstat")])
+    out["rc"] = rc
+    return out

@@ -301,19 +301,34 @@ def _area(tri) -> float:
     return float(F32(0.5) * abs(F32(e)))
 
 
+def tester_option(option: VisibilityTesterOption) -> VisibilityTesterOption:
+    """The option a VisibilityTester keeps of `option`: its constructor and
+    set_option copy it with VisibilityTesterOption::CopyTo
+    (visibility_tester.cc:44-53, 297-308), which copies
+    backface_culling_angle_rad_th, use_mask, use_depth, interp and the three
+    statistics switches only.  max_viewing_angle,
+    max_distance_from_camera_to_vertex, max_depth_difference and eps keep
+    their defaults, whatever the caller set."""
+    t = VisibilityTesterOption()
+    for k in ("backface_culling_angle_rad_th", "use_mask", "use_depth", "interp",
+              "calc_stat_vertex_info", "collect_face_info", "calc_stat_face_info"):
+        setattr(t, k, getattr(option, k))
+    return t
+
+
 class VisibilityTester:
     """ugu::VisibilityTester's interface (visibility_tester.h:216-265)."""
 
     def __init__(self, option: VisibilityTesterOption | None = None, device: int = 0):
         self._ctx = Context(device)
-        self._option = option or VisibilityTesterOption()
+        self._option = tester_option(option) if option is not None else VisibilityTesterOption()
         self._mesh = None
         self._normals = None
         self._initialized = False
         self._keyframe = None
 
     def set_option(self, option: VisibilityTesterOption) -> None:
-        self._option = option
+        self._option = tester_option(option)
 
     def set_data(self, vertices, normals, indices) -> None:  # :310-317
         from .scenes import Mesh
@@ -334,8 +349,11 @@ class VisibilityTester:
     def set_keyframe(self, keyframe: Keyframe) -> None:
         self._keyframe = keyframe
 
-    def raw(self, keyframes, facewise: bool) -> dict:
-        """The device results for all keyframes, keyframe-major arrays."""
+    def raw(self, keyframes, facewise: bool, option: VisibilityTesterOption | None = None) -> dict:
+        """The device results for all keyframes, keyframe-major arrays.
+        `option`, when given, goes to the device as it is (every threshold
+        of ugu_gpu_test_visibility); by default the tester's own."""
+        opt = option if option is not None else self._option
         if not self._initialized:
             raise RuntimeError("mesh has not been initialized")
         keep, descs = [], []
@@ -362,8 +380,8 @@ class VisibilityTester:
         out = capi.VisibilityOut(*[res[k].ctypes.data for k in
                                    ("visible", "projected_pos", "viewing_angle", "distance",
                                     "color", "intensity")])
-        self._ctx.check(self._ctx.test_visibility(0, self._normals, descs,
-                                                  self._option.to_struct(), facewise, out))
+        self._ctx.check(self._ctx.test_visibility(0, self._normals, descs, opt.to_struct(),
+                                                  facewise, out))
         return res
 
     def Test(self, info: VisibilityInfo, facewise: bool = True, keyframes=None) -> bool:
@@ -373,65 +391,76 @@ class VisibilityTester:
         if not kfs or any(k is None for k in kfs):
             return False
         res = self.raw(kfs, facewise)
-        F = self._mesh.vertex_indices
-        for k, kf in enumerate(kfs):
-            vis = res["visible"][k]
-
-            def rec(i):
-                return VertexInfoPerKeyframe(int(kf.id), res["color"][k, i].copy(),
-                                             float(res["intensity"][k, i]),
-                                             res["projected_pos"][k, i].copy(),
-                                             float(res["viewing_angle"][k, i]),
-                                             float(res["distance"][k, i]))
-            if not facewise:
-                for i in np.nonzero(vis)[0]:
-                    info.vertex_info_list[i].visible_keyframes.append(rec(i))
-                if self._option.collect_face_info:
-                    for f in range(len(F)):  # TestFaces (:551-604)
-                        vinf = []
-                        for j in range(3):
-                            vi = info.vertex_info_list[F[f, j]]
-                            idx = vi.VisibleFrom(kf.id)
-                            if idx < 0:
-                                break
-                            vinf.append(vi.visible_keyframes[idx])
-                        if len(vinf) < 3:
-                            continue
-                        self._face(info, kf.id, f, vinf)
-            else:  # TestFacewiseVertices (:606-668), faces in order
-                done = np.zeros(len(info.vertex_info_list), bool)
-                for f in range(len(F)):
-                    vinf = []
-                    for j in range(3):
-                        i = 3 * f + j
-                        if not vis[i]:
-                            break
-                        r = rec(i)
-                        if not done[F[f, j]]:
-                            done[F[f, j]] = True
-                            info.vertex_info_list[F[f, j]].visible_keyframes.append(r)
-                        vinf.append(r)
-                    if len(vinf) < 3:
-                        continue
-                    self._face(info, kf.id, f, vinf)
-        if self._option.calc_stat_vertex_info:
-            info.CalcStatVertexInfo()
-        if self._option.calc_stat_face_info:
-            info.CalcStatFaceInfo()
+        assemble_visibility_info(info, [int(kf.id) for kf in kfs], res,
+                                 self._mesh.vertex_indices, self._option, facewise)
         return True
 
-    @staticmethod
-    def _face(info, kf_id, f, vinf):
-        va = F32(0.0)
-        di = F32(0.0)
-        with np.errstate(over="ignore"):  # FLT_MAX distances sum to inf, as in float
-            for v in vinf:
-                va = F32(va + F32(v.viewing_angle))
-                di = F32(di + F32(v.distance))
-        tri = np.array([v.projected_pos for v in vinf], np.float32)
-        info.face_info_list[f].visible_keyframes.append(
-            FaceInfoPerKeyframe(int(kf_id), int(f), _area(tri), float(va / F32(3)),
-                                float(di / F32(3)), tri))
+
+def assemble_visibility_info(info: VisibilityInfo, kf_ids, res: dict, faces,
+                             option: VisibilityTesterOption, facewise: bool) -> None:
+    """The host half of VisibilityTester::Test(keyframes, info, facewise)
+    (visibility_tester.cc:670-731): the per-keyframe results `res`
+    (keyframe-major arrays, as VisibilityTester.raw returns them) appended to
+    `info` keyframe by keyframe as TestVertices / TestFaces (:416-604) or
+    TestFacewiseVertices (:606-668) append them, then the statistics."""
+    F = np.asarray(faces)
+    for k, kid in enumerate(kf_ids):
+        vis = res["visible"][k]
+
+        def rec(i):
+            return VertexInfoPerKeyframe(int(kid), res["color"][k, i].copy(),
+                                         float(res["intensity"][k, i]),
+                                         res["projected_pos"][k, i].copy(),
+                                         float(res["viewing_angle"][k, i]),
+                                         float(res["distance"][k, i]))
+        if not facewise:
+            for i in np.nonzero(vis)[0]:
+                info.vertex_info_list[i].visible_keyframes.append(rec(i))
+            if option.collect_face_info:
+                for f in range(len(F)):  # TestFaces (:551-604)
+                    vinf = []
+                    for j in range(3):
+                        vi = info.vertex_info_list[F[f, j]]
+                        idx = vi.VisibleFrom(kid)
+                        if idx < 0:
+                            break
+                        vinf.append(vi.visible_keyframes[idx])
+                    if len(vinf) < 3:
+                        continue
+                    _face_record(info, kid, f, vinf)
+        else:  # TestFacewiseVertices (:606-668), faces in order
+            done = np.zeros(len(info.vertex_info_list), bool)
+            for f in range(len(F)):
+                vinf = []
+                for j in range(3):
+                    i = 3 * f + j
+                    if not vis[i]:
+                        break
+                    r = rec(i)
+                    if not done[F[f, j]]:
+                        done[F[f, j]] = True
+                        info.vertex_info_list[F[f, j]].visible_keyframes.append(r)
+                    vinf.append(r)
+                if len(vinf) < 3:
+                    continue
+                _face_record(info, kid, f, vinf)
+    if option.calc_stat_vertex_info:
+        info.CalcStatVertexInfo()
+    if option.calc_stat_face_info:
+        info.CalcStatFaceInfo()
+
+
+def _face_record(info, kf_id, f, vinf):
+    va = F32(0.0)
+    di = F32(0.0)
+    with np.errstate(over="ignore"):  # FLT_MAX distances sum to inf, as in float
+        for v in vinf:
+            va = F32(va + F32(v.viewing_angle))
+            di = F32(di + F32(v.distance))
+    tri = np.array([v.projected_pos for v in vinf], np.float32)
+    info.face_info_list[f].visible_keyframes.append(
+        FaceInfoPerKeyframe(int(kf_id), int(f), _area(tri), float(va / F32(3)),
+                            float(di / F32(3)), tri))
 
 
 # --- TextureMapping (include/ugu/texturing/texture_mapper.h,
