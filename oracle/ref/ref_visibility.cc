@@ -1,15 +1,17 @@
 // ref_visibility.cc -- TEST INFRASTRUCTURE ONLY.
 //
-// A C entry point around the reference's own ugu::VisibilityTester
-// (src/texturing/visibility_tester.cc, compiled unmodified against the
-// Eigen-compatible shim): Test(keyframes, info, facewise) on plain arrays,
-// with the resulting VisibilityInfo copied out field by field, so that the
-// oracle's restatement of the per-keyframe test and the host mirror's
-// VisibilityInfo assembly and statistics can be compared with it.
+// C entry points around the reference's own ugu::VisibilityTester and
+// ugu::TextureMapping (src/texturing/visibility_tester.cc and
+// texture_mapper.cc, compiled unmodified against the Eigen-compatible shim),
+// on plain arrays: the VisibilityInfo of Test(keyframes, info, facewise)
+// copied out field by field, and the texture, uv, uv indices and material
+// ids TextureMapping leaves on the mesh, so that the oracle's restatements
+// and the host mirror can be compared with them.
 #include <cstring>
 #include <memory>
 #include <vector>
 
+#include "ugu/texturing/texture_mapper.h"
 #include "ugu/texturing/visibility_tester.h"
 #include "ugu/util/math_util.h"
 
@@ -45,26 +47,17 @@ struct ref_vis_option {
   float invalid_color[3];
 };
 
-// Per-vertex outputs (K = nkf): vcount[V]; vrec_id[V*K]; vrec[V*K*9] = color
-// (3), intensity, projected_pos (2), viewing_angle, distance, 0; vstat_i[V*5]
-// = min_viewing_angle index, id, min_distance index, id, mode_frequency;
-// vstat[V*43] = mean_color, median_color, min_viewing_angle_color,
-// mean_viewing_angle_color, median_viewing_angle_color, min_distance_color,
-// mean_distance_color, median_distance_color, median_intensity_color,
-// min_intensity_color, mode, mode_viewing_angle_color (3 each), then
-// min_intensity, median_intensity, mean_viewing_angle, median_viewing_angle,
-// mean_distance, median_distance, mode_frequency_viewing_angle_color.
-// Per-face outputs: fcount[F]; frec_id[F*K*2] = kf_id, face_id; frec[F*K*9] =
-// area, viewing_angle, distance, projected_tri (6); fstat_i[F*6] = max_area
-// index, id, min_viewing_angle index, id, min_distance index, id; fstat[F*3]
-// = max_area, min_viewing_angle, min_distance.  Statistics of a vertex or
-// face without records are left as they are.  Returns 0, or 1 when Test
-// returns false.
-int ref_visibility(const float* vertices, int nv, const float* normals, const int* indices,
+}  // extern "C"
+
+namespace {
+
+// VisibilityTester(option).set_data(...), PrepareData, then
+// Test(keyframes, info, facewise); 0, 1 when Test returns false, 2 when
+// PrepareData does.
+int run_visibility(const float* vertices, int nv, const float* normals, const int* indices,
                    int nf, const ref_keyframe* kfs, int nkf, const ref_vis_option* o,
-                   int facewise, int* vcount, int* vrec_id, float* vrec, int* vstat_i,
-                   float* vstat, int* fcount, int* frec_id, float* frec, int* fstat_i,
-                   float* fstat) {
+                   int facewise, std::vector<std::shared_ptr<ugu::Keyframe>>* out_keyframes,
+                   ugu::VisibilityInfo* out_info) {
   ugu::set_log_level(ugu::LogLevel::kError);
   std::vector<Eigen::Vector3f> v(nv), n(nv);
   for (int i = 0; i < nv; ++i) {
@@ -118,10 +111,43 @@ int ref_visibility(const float* vertices, int nv, const float* normals, const in
     keyframes.push_back(kf);
   }
 
+  out_info->vertex_info_list.resize(nv);
+  out_info->face_info_list.resize(nf);
+  if (!tester.Test(keyframes, out_info, facewise != 0)) return 1;
+  *out_keyframes = keyframes;
+  return 0;
+}
+
+}  // namespace
+
+
+extern "C" {
+
+// Per-vertex outputs (K = nkf): vcount[V]; vrec_id[V*K]; vrec[V*K*9] = color
+// (3), intensity, projected_pos (2), viewing_angle, distance, 0; vstat_i[V*5]
+// = min_viewing_angle index, id, min_distance index, id, mode_frequency;
+// vstat[V*43] = mean_color, median_color, min_viewing_angle_color,
+// mean_viewing_angle_color, median_viewing_angle_color, min_distance_color,
+// mean_distance_color, median_distance_color, median_intensity_color,
+// min_intensity_color, mode, mode_viewing_angle_color (3 each), then
+// min_intensity, median_intensity, mean_viewing_angle, median_viewing_angle,
+// mean_distance, median_distance, mode_frequency_viewing_angle_color.
+// Per-face outputs: fcount[F]; frec_id[F*K*2] = kf_id, face_id; frec[F*K*9] =
+// area, viewing_angle, distance, projected_tri (6); fstat_i[F*6] = max_area
+// index, id, min_viewing_angle index, id, min_distance index, id; fstat[F*3]
+// = max_area, min_viewing_angle, min_distance.  Statistics of a vertex or
+// face without records are left as they are.  Returns 0, or 1 when Test
+// returns false.
+int ref_visibility(const float* vertices, int nv, const float* normals, const int* indices,
+                   int nf, const ref_keyframe* kfs, int nkf, const ref_vis_option* o,
+                   int facewise, int* vcount, int* vrec_id, float* vrec, int* vstat_i,
+                   float* vstat, int* fcount, int* frec_id, float* frec, int* fstat_i,
+                   float* fstat) {
+  std::vector<std::shared_ptr<ugu::Keyframe>> keyframes;
   ugu::VisibilityInfo info;
-  info.vertex_info_list.resize(nv);
-  info.face_info_list.resize(nf);
-  if (!tester.Test(keyframes, &info, facewise != 0)) return 1;
+  const int rc = run_visibility(vertices, nv, normals, indices, nf, kfs, nkf, o, facewise,
+                                &keyframes, &info);
+  if (rc) return rc;
 
   auto put3 = [](float* d, const Eigen::Vector3f& a) {
     d[0] = a[0];
@@ -204,6 +230,74 @@ int ref_visibility(const float* vertices, int nv, const float* normals, const in
     s[1] = fi.min_viewing_angle;
     s[2] = fi.min_distance;
   }
+  return 0;
+}
+
+// TextureMapping (src/texturing/texture_mapper.cc:1009-1017) after the
+// visibility test above, on a ugu::Mesh of the vertices and faces (and the
+// mesh's own uv and uv indices when uv is not NULL), with
+// TextureMappingOption {criteria, kSimpleProjection, uv_type, tex_w, tex_h,
+// padding_kernel}.  Copies out the first material's texture (tex_wh = its
+// width and height; at most tex_cap bytes), the mesh's uv (*n_uv of them, at
+// most uv_cap), its uv indices (F*3) and material ids (F).  Returns 0; 1 or
+// 2 as run_visibility; 4 when TextureMapping returns false; 3 when the
+// texture or the uv do not fit (tex_wh and *n_uv then say how large they
+// are).
+int ref_texture_mapping(const float* vertices, int nv, const float* normals, const int* indices,
+                        int nf, const float* uv, int nuv, const int* uv_indices,
+                        const ref_keyframe* kfs, int nkf, const ref_vis_option* o, int facewise,
+                        int criteria, int uv_type, int tex_w, int tex_h, int padding_kernel,
+                        unsigned char* tex, long long tex_cap, int* tex_wh, float* uv_out,
+                        int uv_cap, int* n_uv, int* uvi_out, int* mat_ids) {
+  std::vector<std::shared_ptr<ugu::Keyframe>> keyframes;
+  ugu::VisibilityInfo info;
+  int rc = run_visibility(vertices, nv, normals, indices, nf, kfs, nkf, o, facewise,
+                          &keyframes, &info);
+  if (rc) return rc;
+  ugu::Mesh mesh;
+  std::vector<Eigen::Vector3f> v(nv);
+  for (int i = 0; i < nv; ++i)
+    v[i] = Eigen::Vector3f(vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2]);
+  std::vector<Eigen::Vector3i> f(nf);
+  for (int i = 0; i < nf; ++i)
+    f[i] = Eigen::Vector3i(indices[3 * i], indices[3 * i + 1], indices[3 * i + 2]);
+  mesh.set_vertices(v);
+  mesh.set_vertex_indices(f);
+  if (uv) {
+    std::vector<Eigen::Vector2f> u(nuv);
+    for (int i = 0; i < nuv; ++i) u[i] = Eigen::Vector2f(uv[2 * i], uv[2 * i + 1]);
+    std::vector<Eigen::Vector3i> ui(nf);
+    for (int i = 0; i < nf; ++i)
+      ui[i] = Eigen::Vector3i(uv_indices[3 * i], uv_indices[3 * i + 1], uv_indices[3 * i + 2]);
+    mesh.set_uv(u);
+    mesh.set_uv_indices(ui);
+  }
+  ugu::TextureMappingOption opt;
+  opt.criteria = static_cast<ugu::ViewSelectionCriteria>(criteria);
+  opt.type = ugu::TextureMappingType::kSimpleProjection;
+  opt.uv_type = static_cast<ugu::TexturingOutputUvType>(uv_type);
+  opt.tex_w = tex_w;
+  opt.tex_h = tex_h;
+  opt.padding_kernel = padding_kernel;
+  if (!ugu::TextureMapping(keyframes, info, &mesh, opt)) return 4;
+
+  const ugu::Image3b& t = mesh.materials()[0].diffuse_tex;
+  tex_wh[0] = t.cols;
+  tex_wh[1] = t.rows;
+  *n_uv = (int)mesh.uv().size();
+  const long long bytes = (long long)t.cols * t.rows * 3;
+  if (bytes > tex_cap || *n_uv > uv_cap) return 3;
+  for (int y = 0; y < t.rows; ++y)
+    std::memcpy(tex + (size_t)y * t.cols * 3, t.data + t.step[0] * y, (size_t)t.cols * 3);
+  for (int i = 0; i < *n_uv; ++i) {
+    uv_out[2 * i] = mesh.uv()[i][0];
+    uv_out[2 * i + 1] = mesh.uv()[i][1];
+  }
+  const auto& ui = mesh.uv_indices();
+  for (int i = 0; i < nf && i < (int)ui.size(); ++i)
+    for (int k = 0; k < 3; ++k) uvi_out[3 * i + k] = ui[i][k];
+  const auto& mi = mesh.material_ids();
+  for (int i = 0; i < nf && i < (int)mi.size(); ++i) mat_ids[i] = mi[i];
   return 0;
 }
 

@@ -221,3 +221,71 @@ def visibility(vertices, normals, faces, keyframes, option, facewise):
                                           "fcount", "frec_id", "frec", "fstat_i", "fstat")])
     out["rc"] = rc
     return out
+
+
+def texture_mapping(vertices, normals, faces, keyframes, option, facewise, criteria, uv_type,
+                    tex_w, tex_h, padding_kernel=3, uv=None, uv_indices=None):
+    """The reference's own VisibilityTester::Test(keyframes, ...) and then
+    ugu::TextureMapping (src/texturing/texture_mapper.cc) with the given
+    TextureMappingOption fields.  Returns (status, texture H x W x 3 uint8,
+    uv N x 2, uv_indices F x 3, material_ids F), or None without the
+    reference build; status 0 is success."""
+    lib = load()
+    if lib is None:
+        return None
+    V = np.ascontiguousarray(vertices, np.float32)
+    N = np.ascontiguousarray(normals, np.float32)
+    F = np.ascontiguousarray(faces, np.int32)
+    K, nf = len(keyframes), len(F)
+    keep = []
+    kfs = (RefKeyframe * K)()
+    for i, (kid, cam, color, depth, mask) in enumerate(keyframes):
+        k = kfs[i]
+        k.id, k.width, k.height = int(kid), int(cam.width), int(cam.height)
+        k.fx, k.fy, k.cx, k.cy = float(cam.fx), float(cam.fy), float(cam.cx), float(cam.cy)
+        k.c2w[:] = [float(x) for x in np.asarray(cam.c2w, np.float64).reshape(-1)]
+        for name, a, dt in (("color", color, np.uint8), ("depth", depth, np.float32),
+                            ("mask", mask, np.uint8)):
+            if a is not None:
+                a = np.ascontiguousarray(a, dt)
+                keep.append(a)
+                setattr(k, name, a.ctypes.data)
+    o = RefVisOption(float(option.backface_culling_angle_rad_th), int(option.use_mask),
+                     int(option.use_depth), int(option.interp),
+                     int(option.calc_stat_vertex_info), int(option.collect_face_info),
+                     int(option.calc_stat_face_info), float(option.max_viewing_angle),
+                     float(option.max_distance_from_camera_to_vertex),
+                     float(option.max_depth_difference), float(option.eps),
+                     (C.c_float * 3)(0.0, 0.0, 0.0))
+    if uv is not None:
+        U = np.ascontiguousarray(uv, np.float32)
+        UI = np.ascontiguousarray(uv_indices, np.int32)
+        uv_args = (U.ctypes.data, len(U), UI.ctypes.data)
+    else:
+        uv_args = (None, 0, None)
+    f = lib.ref_texture_mapping
+    f.restype = C.c_int
+    f.argtypes = ([C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                   C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p,
+                   C.c_int, C.c_void_p, C.c_void_p, C.c_void_p])
+    tex_cap, uv_cap = 3 * tex_w * tex_h, 3 * nf
+    for _ in range(2):  # once more with the sizes a first call reported
+        tex = np.zeros(max(tex_cap, 1), np.uint8)
+        wh = np.zeros(2, np.int32)
+        uv_out = np.zeros((max(uv_cap, 1), 2), np.float32)
+        n_uv = C.c_int(0)
+        uvi = np.zeros((nf, 3), np.int32)
+        mat = np.zeros(nf, np.int32)
+        rc = f(V.ctypes.data, len(V), N.ctypes.data, F.ctypes.data, nf, *uv_args,
+               C.addressof(kfs), K, C.addressof(o), 1 if facewise else 0, int(criteria),
+               int(uv_type), int(tex_w), int(tex_h), int(padding_kernel), tex.ctypes.data,
+               tex_cap, wh.ctypes.data, uv_out.ctypes.data, uv_cap, C.byref(n_uv),
+               uvi.ctypes.data, mat.ctypes.data)
+        if rc != 3:
+            break
+        tex_cap, uv_cap = 3 * int(wh[0]) * int(wh[1]), int(n_uv.value)
+    if rc:
+        return rc, None, None, None, None
+    w, h = int(wh[0]), int(wh[1])
+    return 0, tex[:3 * w * h].reshape(h, w, 3), uv_out[:n_uv.value], uvi, mat

@@ -9,7 +9,9 @@ ugu_gpu_texture_mapping_targets) and bin-packed charts of keyframe patches
 (kGenerateSimpleCharts, :476-922, host layout and copies, as in the
 reference).  The face arrays are seeded: uv triangles that
 overlap heavily (a later face overwrites an earlier one), source triangles
-reaching outside their keyframe images, faces without a keyframe."""
+reaching outside their keyframe images, faces without a keyframe.  Where
+the reference checkout is present, the restatements are also pinned to the
+reference's own texture_mapper.cc and bin_packer_2d.cc (oracle/_ref)."""
 import numpy as np
 import pytest
 
@@ -407,3 +409,70 @@ def test_gpu_texture_mapping_atlas_pipeline(gpu_lib, oracle_lib, uv_type):
         compare(ref, got, "atlas render")
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("uv_type", [vis.TexturingOutputUvType.kGenerateSimpleTile,
+                                     vis.TexturingOutputUvType.kUseOriginalMeshUv,
+                                     vis.TexturingOutputUvType.kGenerateSimpleTriangles,
+                                     vis.TexturingOutputUvType.kGenerateSimpleCharts])
+@pytest.mark.parametrize("criteria", [vis.ViewSelectionCriteria.kMaxArea,
+                                      vis.ViewSelectionCriteria.kMinViewingAngle])
+@pytest.mark.parametrize("tex,facewise", [(256, False), (64, True)])
+def test_texture_mapping_pinned_to_the_reference(oracle_lib, uv_type, criteria, tex, facewise):
+    """TextureMapping against the reference's own (src/texturing/
+    texture_mapper.cc after its own VisibilityTester, built into
+    oracle/_ref): the oracle's restatements of each uv type, fed by the
+    host mirror's VisibilityInfo (itself pinned) and best keyframes, give
+    the reference's texture, uv, uv indices and material ids, bit for bit
+    (a 64 x 64 texture makes the chart atlas grow).  Runs where the
+    reference checkout is present."""
+    ref_build = pytest.importorskip("oracle.ref_build")
+    if not ref_build.available():
+        pytest.skip("reference sources not present")
+    from test_visibility import keyframes, oracle_run, option
+    T = vis.TexturingOutputUvType
+    m = scenes.icosphere_textured(3, 64)
+    base = 10 if uv_type == T.kGenerateSimpleTile else 0  # other types index the list by id
+    kfs = [(base + i, cam, im) for i, (_, cam, im) in enumerate(keyframes(oracle_lib, m, n=4))]
+    o = option()
+    tex_w = tex_h = tex
+    rc, r_tex, r_uv, r_uvi, r_mat = ref_build.texture_mapping(
+        m.vertices, m.normals, m.vertex_indices,
+        [(kid, cam, im["color"], im["depth"], im["mask"]) for kid, cam, im in kfs], o, facewise,
+        criteria, uv_type, tex_w, tex_h,
+        uv=m.uv if uv_type == T.kUseOriginalMeshUv else None,
+        uv_indices=m.uv_indices if uv_type == T.kUseOriginalMeshUv else None)
+    assert rc in (0, 4)  # 4: the reference's TextureMapping returned false
+    ref_rejects = rc == 4
+    info = vis.VisibilityInfo(m.num_vertices, m.num_faces)
+    vis.assemble_visibility_info(info, [kid for kid, _, _ in kfs],
+                                 oracle_run(oracle_lib, m, kfs, o, facewise), m.vertex_indices,
+                                 o, facewise)
+    face_kf, face_tri = vis.best_keyframes(info, criteria)
+    assert (face_kf >= 0).mean() > 0.3
+    colors = [im["color"] for _, _, im in kfs]
+    F = m.num_faces
+    want_uvi = np.arange(3 * F, dtype=np.int32).reshape(-1, 3)
+    if uv_type == T.kGenerateSimpleTile:
+        rc, want_t, want_uv = oracle_lib.simple_tile([kid for kid, _, _ in kfs], colors,
+                                                     face_kf, face_tri)
+    elif uv_type == T.kGenerateSimpleCharts:
+        rc, want_t, want_uv, want_uvi = oracle_lib.simple_charts(
+            m.vertex_indices, colors, face_kf, face_tri, tex_w, tex_h)
+    elif uv_type == T.kGenerateSimpleTriangles:
+        rc, want_t, _, want_uv = oracle_lib.simple_triangles(colors, face_kf, face_tri,
+                                                             tex_w, tex_h)
+    else:
+        rc, want_t, _ = oracle_lib.texture_mapping(m.uv, m.uv_indices, colors, face_kf,
+                                                   face_tri, tex_w, tex_h)
+        want_uv, want_uvi = m.uv, m.uv_indices
+    if ref_rejects:  # e.g. 640 face-pair rectangles do not fit 64 x 64 texels
+        assert rc != 0
+        return
+    assert rc == 0
+    assert r_tex.shape == want_t.shape
+    assert np.array_equal(r_tex, want_t), f"{(r_tex != want_t).any(-1).sum()} texels differ"
+    assert np.array_equal(np.ascontiguousarray(r_uv, np.float32).view(np.uint32),
+                          np.ascontiguousarray(want_uv, np.float32).view(np.uint32))
+    assert np.array_equal(r_uvi, want_uvi)
+    assert not r_mat.any()
