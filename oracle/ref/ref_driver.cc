@@ -13,6 +13,8 @@
 #include <vector>
 
 #include "ugu/discrete/bin_packer_2d.h"
+#include "ugu/image_proc.h"
+#include "ugu/util/image_util.h"
 #include "ugu/renderer/cpu/rasterizer.h"
 #include "ugu/renderer/cpu/raytracer.h"
 
@@ -220,6 +222,45 @@ int ref_bin_packing_2d(const int* rects, int n, int x_min, int x_max, int y_min,
     free_rects[4 * i + 3] = avail[i].height;
   }
   return ok ? 1 : 0;
+}
+
+// The image helpers after a render (src/util/image_util.cc: Depth2Gray,
+// Normal2Color, FaceId2RandomColor; include/ugu/image_proc.h: ConvertTo to
+// 16 bits) on W x H images; an input or output may be NULL.
+int ref_visualize(int width, int height, const float* depth, const float* normal,
+                  const int* face_id, unsigned char* vis_depth, unsigned short* depth_u16,
+                  unsigned char* vis_normal, unsigned char* vis_face_id, float min_d,
+                  float max_d, int gl_coord) {
+  const size_t px = (size_t)width * height;
+  if (depth) {
+    ugu::Image1f d = ugu::Image1f::zeros(height, width);
+    std::memcpy(d.data, depth, px * 4);
+    if (vis_depth) {
+      ugu::Image1b g;
+      ugu::Depth2Gray(d, &g, min_d, max_d);
+      std::memcpy(vis_depth, g.data, px);
+    }
+    if (depth_u16) {
+      ugu::Image1w w;
+      ugu::ConvertTo(d, &w);
+      std::memcpy(depth_u16, w.data, px * 2);
+    }
+  }
+  if (normal && vis_normal) {
+    ugu::Image3f n = ugu::Image3f::zeros(height, width);
+    std::memcpy(n.data, normal, px * 12);
+    ugu::Image3b c;
+    ugu::Normal2Color(n, &c, gl_coord != 0);
+    std::memcpy(vis_normal, c.data, px * 3);
+  }
+  if (face_id && vis_face_id) {
+    ugu::Image1i f = ugu::Image1i::zeros(height, width);
+    std::memcpy(f.data, face_id, px * 4);
+    ugu::Image3b c;
+    ugu::FaceId2RandomColor(f, &c);
+    std::memcpy(vis_face_id, c.data, px * 3);
+  }
+  return 0;
 }
 
 }  // extern "C"

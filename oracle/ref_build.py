@@ -289,3 +289,35 @@ def texture_mapping(vertices, normals, faces, keyframes, option, facewise, crite
         return rc, None, None, None, None
     w, h = int(wh[0]), int(wh[1])
     return 0, tex[:3 * w * h].reshape(h, w, 3), uv_out[:n_uv.value], uvi, mat
+
+
+def visualize(depth=None, normal=None, face_id=None, min_d=200.0, max_d=1500.0,
+              gl_coord=False):
+    """The reference's own Depth2Gray, ConvertTo<uint16_t>, Normal2Color and
+    FaceId2RandomColor (src/util/image_util.cc, include/ugu/image_proc.h)
+    for the given images; returns a dict like oracle.visualize, or None
+    without the reference build."""
+    lib = load()
+    if lib is None:
+        return None
+    shp = next(a for a in (depth, normal, face_id) if a is not None).shape
+    H, W = shp[0], shp[1]
+    d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+    n = None if normal is None else np.ascontiguousarray(normal, np.float32)
+    f = None if face_id is None else np.ascontiguousarray(face_id, np.int32)
+    out = {}
+    if d is not None:
+        out["vis_depth"] = np.zeros((H, W), np.uint8)
+        out["depth_u16"] = np.zeros((H, W), np.uint16)
+    if n is not None:
+        out["vis_normal"] = np.zeros((H, W, 3), np.uint8)
+    if f is not None:
+        out["vis_face_id"] = np.zeros((H, W, 3), np.uint8)
+    fn = lib.ref_visualize
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 7 + [C.c_float, C.c_float, C.c_int]
+    ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+    fn(W, H, ptr(d), ptr(n), ptr(f), ptr(out.get("vis_depth")), ptr(out.get("depth_u16")),
+       ptr(out.get("vis_normal")), ptr(out.get("vis_face_id")), float(min_d), float(max_d),
+       1 if gl_coord else 0)
+    return out

@@ -114,3 +114,22 @@ def test_gpu_visualize_a_render(gpu_lib, oracle_lib):
     assert np.array_equal(Depth2Gray(out["depth"], 1.0, 4.0), ref["vis_depth"])
     assert np.array_equal(Normal2Color(out["normal"]), ref["vis_normal"])
     assert np.array_equal(FaceId2RandomColor(out["face_id"]), ref["vis_face_id"])
+
+
+@pytest.mark.parametrize("gl_coord", [False, True])
+def test_visualize_pinned_to_the_reference(oracle_lib, gl_coord):
+    """The oracle's image helpers against the reference's own
+    (src/util/image_util.cc and image_proc.h's ConvertTo, built into
+    oracle/_ref), bit for bit, on the edge inputs wherever the reference's
+    float-to-integer casts are defined (depths below 65536, normals in
+    [-1, 1]).  Runs where the reference checkout is present."""
+    ref_build = pytest.importorskip("oracle.ref_build")
+    if not ref_build.available():
+        pytest.skip("reference sources not present")
+    depth, normal, face_id = edge_inputs()
+    depth[0, 5] = 60000.5  # the cast to 16 bits stays defined
+    for kw in ({"min_d": 200.0, "max_d": 1500.0}, {"min_d": 0.5, "max_d": 70000.0}):
+        want = ref_build.visualize(depth, normal, face_id, gl_coord=gl_coord, **kw)
+        got = oracle_lib.visualize(depth, normal, face_id, gl_coord=gl_coord, **kw)
+        for k in want:
+            assert np.array_equal(want[k], got[k]), (k, kw)
