@@ -198,7 +198,10 @@ float nearest_t(const Bvh* b, const float* org, const float* dir) {
 float dot3f(const float* a, const float* b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
 
 // VisibilityTester::TestVertex (visibility_tester.cc:416-529) for one
-// keyframe and world point wp of vertex vid; false when not visible.
+// keyframe and world point wp of vertex vid; false when not visible.  With
+// the host's VisibilityInfo assembly on top, pinned bit for bit to the
+// reference's own visibility_tester.cc built into oracle/_ref
+// (tests/test_visibility.py).
 bool test_vertex(const Bvh* bvh, const float* V, const float* N, int vid, const float* wp,
                  const oracle_keyframe& K, const oracle_vis_option& o, float* proj, float* angle,
                  float* dist_out, float* col, float* inten) {

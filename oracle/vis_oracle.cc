@@ -7,10 +7,13 @@
  *   FaceId2RandomColor  src/util/image_util.cc:448-487 (std::mt19937(fid),
  *                       three draws mod 256, RGB order)
  *   ConvertTo<uint16_t> include/ugu/image_proc.h:453-475 with scale 1
- * (src/util/image_util.cc itself needs Eigen's dynamic matrices, which the
- * Eigen-compatible shim does not provide, so it is not built here.)  The
- * double-to-integer casts, undefined by C++ outside the target range, take
- * the low bits of the truncated int32 value, as the GPU does.
+ * Pinned, where the cast is defined, to src/util/image_util.cc itself,
+ * built into oracle/_ref against the Eigen-compatible shim
+ * (tests/test_vis.py).  The double-to-integer casts, undefined by C++
+ * outside the target range, take the low bits of the truncated int32 value,
+ * as the GPU does.  The texture mapping restatements below are pinned to
+ * the reference's own texture_mapper.cc and bin_packer_2d.cc the same way
+ * (tests/test_texture_mapping.py).
  */
 #include <algorithm>
 #include <array>
