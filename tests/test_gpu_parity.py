@@ -252,6 +252,55 @@ def test_host_outputs_span_copy_chunks(ctx, torch_cuda):
             assert np.array_equal(t.cpu().numpy(), got[i][k]), (i, k)
 
 
+def test_host_outputs_in_one_buffer_per_output(ctx, torch_cuda):
+    """Host buffers that are slices of one buffer per output, view after
+    view, are copied back a run of views at a time: the same batch of three
+    copy chunks equals the device-buffer render, with a view in the middle
+    that asks for fewer outputs (it breaks the runs of the others) and a
+    view whose slices are out of order (never merged)."""
+    torch = torch_cuda
+    m = scenes.icosphere_textured(5, 256)
+    cams = scenes.ring_cameras(6, 3.0, [(1920, 1080), (640, 480), (1920, 1080), (1920, 1080),
+                                        (1280, 720), (320, 240)])
+    ctx.check(ctx.set_mesh(0, m))
+    from gpu_helpers import to_option
+    ctx.check(ctx.set_option(to_option(adv.option(1, 1, 1, 0, True))))
+    outs = [gpu_helpers_outputs(k) for k in range(len(cams))]
+    want, dviews = [], []
+    for cam, o in zip(cams, outs):
+        t, v = device_views(torch, [cam], [0], outputs=o)
+        want += t
+        dviews += v
+    ctx.check(ctx.render_views(dviews, capi.DEVICE_POINTERS))
+    torch.cuda.synchronize()
+    spec = {"color": ((3,), np.uint8), "depth": ((), np.float32), "normal": ((3,), np.float32),
+            "mask": ((), np.uint8), "face_id": ((), np.int32)}
+    order = [0, 1, 2, 3, 5, 4]  # the last two views' slices swapped
+    flat = {k: np.zeros(sum(c.width * c.height * (ch[0] if ch else 1) for c in cams), dt)
+            for k, (ch, dt) in spec.items()}
+    at = {k: 0 for k in spec}
+    sl = [dict() for _ in cams]
+    for i in order:
+        c = cams[i]
+        for k, (ch, dt) in spec.items():
+            n = c.width * c.height * (ch[0] if ch else 1)
+            if k in outs[i]:
+                sl[i][k] = flat[k][at[k]:at[k] + n].reshape((c.height, c.width) + ch)
+            at[k] += n
+    hviews = []
+    for i, cam in enumerate(cams):
+        v = capi.View()
+        v.mesh = 0
+        v.camera = capi.camera_struct(cam)
+        for k, a in sl[i].items():
+            setattr(v.images, k, a.ctypes.data)
+        hviews.append(v)
+    ctx.check(ctx.render_views(hviews, 0))
+    for i in range(len(cams)):
+        for k, t in want[i].items():
+            assert np.array_equal(t.cpu().numpy(), sl[i][k]), (i, k)
+
+
 def gpu_helpers_outputs(k):
     full = ("color", "depth", "normal", "mask", "face_id")
     return ("color", "normal") if k == 3 else full

@@ -748,45 +748,93 @@ void fill_views(ugu_gpu_context* ctx, Scratch& s, const std::vector<Group>& grou
         d.mask = v.images.mask;
         d.face_id = v.images.face_id;
         d.color_f32 = v.images.color_f32;
-      } else {
-        auto take = [&](size_t bytes) {
-          uint8_t* p = s.d_out + off;
-          off += align256(bytes);
-          return p;
-        };
-        if (v.images.color) d.color = take(3 * px);
-        if (v.images.depth) d.depth = reinterpret_cast<float*>(take(4 * px));
-        if (v.images.normal) d.normal = reinterpret_cast<float*>(take(12 * px));
-        if (v.images.mask) d.mask = take(px);
-        if (v.images.face_id) d.face_id = reinterpret_cast<int32_t*>(take(4 * px));
-        if (v.images.color_f32) d.color_f32 = reinterpret_cast<float*>(take(12 * px));
       }
-
     }
+    if (device_ptrs) continue;
+    // Host outputs: the group's staging is laid out output by output, each
+    // output's views back to back in view order, so that views whose host
+    // buffers are back to back as well are copied with one call (copy_back).
+    // The kernels' stores are scalar: 4-byte alignment is all they need.
+    // This packing never takes more than one 256-byte-aligned block per
+    // output and view (host_bytes_of_view).
+    auto stage = [&](size_t bytes_per_px, bool (*wants)(const ugu_gpu_images&),
+                     void (*set)(DevView&, uint8_t*)) {
+      size_t run = 0;
+      for (int i = gr.first; i < gr.first + gr.count; ++i) {
+        if (!wants(views[i].images)) continue;
+        set(s.h_views[i], s.d_out + off + run);
+        run += bytes_per_px * (size_t)views[i].camera.width * views[i].camera.height;
+      }
+      off += align256(run);
+    };
+    stage(3, [](const ugu_gpu_images& m) { return m.color != nullptr; },
+          [](DevView& d, uint8_t* p) { d.color = p; });
+    stage(4, [](const ugu_gpu_images& m) { return m.depth != nullptr; },
+          [](DevView& d, uint8_t* p) { d.depth = reinterpret_cast<float*>(p); });
+    stage(12, [](const ugu_gpu_images& m) { return m.normal != nullptr; },
+          [](DevView& d, uint8_t* p) { d.normal = reinterpret_cast<float*>(p); });
+    stage(1, [](const ugu_gpu_images& m) { return m.mask != nullptr; },
+          [](DevView& d, uint8_t* p) { d.mask = p; });
+    stage(4, [](const ugu_gpu_images& m) { return m.face_id != nullptr; },
+          [](DevView& d, uint8_t* p) { d.face_id = reinterpret_cast<int32_t*>(p); });
+    stage(12, [](const ugu_gpu_images& m) { return m.color_f32 != nullptr; },
+          [](DevView& d, uint8_t* p) { d.color_f32 = reinterpret_cast<float*>(p); });
   }
 }
 
+// The group's outputs to the caller's host buffers, one copy per output and
+// run of views whose host buffers follow one another (their staging does,
+// fill_views), so that a caller with one buffer per output for all views
+// costs one copy per output and group.
 int copy_back(ugu_gpu_context* ctx, const Scratch& s, int first, int count,
               const ugu_gpu_view* views, cudaStream_t stream) {
-  for (int i = first; i < first + count; ++i) {
-    const DevView& d = s.h_views[i];
-    const ugu_gpu_images& im = views[i].images;
-    int64_t px = (int64_t)views[i].camera.width * views[i].camera.height;
-    auto cp = [&](void* dst, const void* src, size_t bytes) -> int {
-      if (!dst) return UGU_GPU_OK;
-      CK(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream),
-         "cudaMemcpyAsync(output)");
+  auto out = [&](size_t bytes_per_px, void* (*host)(const ugu_gpu_images&),
+                 const void* (*dev)(const DevView&)) -> int {
+    uint8_t* dst = nullptr;
+    const uint8_t* src = nullptr;
+    size_t bytes = 0;
+    auto flush = [&]() -> int {
+      if (bytes)
+        CK(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream),
+           "cudaMemcpyAsync(output)");
+      bytes = 0;
       return UGU_GPU_OK;
     };
-    int rc;
-    if ((rc = cp(im.color, d.color, 3 * px))) return rc;
-    if ((rc = cp(im.depth, d.depth, 4 * px))) return rc;
-    if ((rc = cp(im.normal, d.normal, 12 * px))) return rc;
-    if ((rc = cp(im.mask, d.mask, px))) return rc;
-    if ((rc = cp(im.face_id, d.face_id, 4 * px))) return rc;
-    if ((rc = cp(im.color_f32, d.color_f32, 12 * px))) return rc;
-  }
-  return UGU_GPU_OK;
+    for (int i = first; i < first + count; ++i) {
+      uint8_t* h = static_cast<uint8_t*>(host(views[i].images));
+      if (!h) continue;
+      const uint8_t* d = static_cast<const uint8_t*>(dev(s.h_views[i]));
+      const size_t b = bytes_per_px * (size_t)views[i].camera.width * views[i].camera.height;
+      if (bytes && h == dst + bytes && d == src + bytes) {
+        bytes += b;
+        continue;
+      }
+      int rc = flush();
+      if (rc) return rc;
+      dst = h;
+      src = d;
+      bytes = b;
+    }
+    return flush();
+  };
+  int rc;
+  if ((rc = out(3, [](const ugu_gpu_images& m) -> void* { return m.color; },
+                [](const DevView& d) -> const void* { return d.color; })))
+    return rc;
+  if ((rc = out(4, [](const ugu_gpu_images& m) -> void* { return m.depth; },
+                [](const DevView& d) -> const void* { return d.depth; })))
+    return rc;
+  if ((rc = out(12, [](const ugu_gpu_images& m) -> void* { return m.normal; },
+                [](const DevView& d) -> const void* { return d.normal; })))
+    return rc;
+  if ((rc = out(1, [](const ugu_gpu_images& m) -> void* { return m.mask; },
+                [](const DevView& d) -> const void* { return d.mask; })))
+    return rc;
+  if ((rc = out(4, [](const ugu_gpu_images& m) -> void* { return m.face_id; },
+                [](const DevView& d) -> const void* { return d.face_id; })))
+    return rc;
+  return out(12, [](const ugu_gpu_images& m) -> void* { return m.color_f32; },
+             [](const DevView& d) -> const void* { return d.color_f32; });
 }
 
 int check_counters(ugu_gpu_context* ctx, Scratch& s, size_t ngroups) {
