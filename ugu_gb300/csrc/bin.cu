@@ -29,7 +29,6 @@ namespace {
 
 using tiled::copy_words;
 using tiled::kU64;
-using tiled::setup_proj;
 
 constexpr int kBinThreads = 256;
 constexpr int kScanThreads = 256;
@@ -115,6 +114,35 @@ struct FaceBins {
   float zlb;
 };
 
+// Loop B's per-face set-up (rasterizer.cc:163-193) as face_setup computes
+// it, with one more cull first: a bbox holding no integer pixel (most faces
+// of a finely tessellated mesh at these view sizes) is rejected before the
+// area is formed.  Every face it keeps has face_setup's values; every face
+// it rejects, face_setup rejects or gives an empty bbox.
+__device__ __forceinline__ bool bin_setup(const float4* proj, const int4* vidx, int f,
+                                          const Cam& c, FaceSetup& s) {
+  const int4 vi = __ldg(&vidx[f]);
+  const float4 a = __ldg(&proj[vi.x]);
+  const float4 b = __ldg(&proj[vi.y]);
+  const float4 d = __ldg(&proj[vi.z]);
+  if (a.z < 0.0f || b.z < 0.0f || d.z < 0.0f) return false;
+  const float xmin = min3_std(a.x, b.x, d.x), ymin = min3_std(a.y, b.y, d.y);
+  const float xmax = max3_std(a.x, b.x, d.x), ymax = max3_std(a.y, b.y, d.y);
+  if (xmin > (float)(c.width - 1) || xmax < 0.0f || ymin > (float)(c.height - 1) || ymax < 0.0f)
+    return false;
+  s.x0 = max(0, f2i_sat(ceilf(xmin)));
+  s.x1 = min(c.width - 1, f2i_sat(floorf(xmax)));
+  s.y0 = max(0, f2i_sat(ceilf(ymin)));
+  s.y1 = min(c.height - 1, f2i_sat(floorf(ymax)));
+  if (s.x1 < s.x0 || s.y1 < s.y0) return false;
+  s.area = edge_fn(a.x, a.y, b.x, b.y, d.x, d.y);
+  if (fabsf(s.area) < FLT_MIN) return false;
+  s.v0 = make_float3(a.x, a.y, a.z);
+  s.v1 = make_float3(b.x, b.y, b.z);
+  s.v2 = make_float3(d.x, d.y, d.z);
+  return true;
+}
+
 // Face number i of the binning order (DevMesh::order); n = 0 for a face
 // that reaches no pixel.  Faces whose depth lower bound lies behind the
 // split depth are drawn last (cls 1).
@@ -122,9 +150,7 @@ __device__ __forceinline__ FaceBins bin_face(const TileParams& p, const BinShare
   FaceBins b{i, 0, 0, 0, 1, 0, -1.0f};
   if (i >= sb.mesh.num_faces) return b;
   FaceSetup s;
-  if (!setup_proj(p.proj + sb.view.proj_offset, sb.mesh.vidx_morton, i, sb.view.cam, s) ||
-      s.x1 < s.x0 || s.y1 < s.y0)
-    return b;
+  if (!bin_setup(p.proj + sb.view.proj_offset, sb.mesh.vidx_morton, i, sb.view.cam, s)) return b;
   const int ts = sb.view.tile_log2;
   b.tx0 = s.x0 >> ts;
   b.ty0 = s.y0 >> ts;
