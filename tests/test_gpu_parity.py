@@ -519,3 +519,31 @@ def test_views_on_two_tile_sizes(ctx, oracle_lib, torch_cuda):
                 compare(ref, {k: v.cpu().numpy() for k, v in tensors[i].items()}, f"view{i}")
     finally:
         ctx.check(ctx.set_tuning(t0))
+
+
+@pytest.mark.parametrize("sizes", [[(1024, 1024)], [(1024, 1024), (16, 16)],
+                                   [(16, 16), (2048, 1024), (24, 8)]],
+                         ids=["4096_tiles", "4097_tiles", "8195_tiles"])
+def test_tile_scan_chunk_boundaries(ctx, oracle_lib, torch_cuda, sizes):
+    """The tile-count scan runs one block per chunk of 4,096 tiles: batches
+    of exactly one chunk, one chunk and one tile, and two chunks and three
+    tiles (16-pixel tiles throughout) render every view as the oracle does."""
+    torch = torch_cuda
+    m = scenes.icosphere_textured(4, 128)
+    cams = scenes.ring_cameras(len(sizes), 3.0, sizes)
+    ctx.check(ctx.set_mesh(0, m))
+    opt = adv.option(1, 1, 1, 0, True)
+    from gpu_helpers import to_option
+    ctx.check(ctx.set_option(to_option(opt)))
+    t0 = ctx.tuning()
+    ctx.check(ctx.set_tuning(capi.Tuning(capi.PATH_TILED, 4, 0, 256, 1 << 22, 0, 64, 2, 0)))
+    try:
+        tensors, views = device_views(torch, cams, [0] * len(cams))
+        ctx.check(ctx.render_views(views, capi.DEVICE_POINTERS))
+        torch.cuda.synchronize()
+    finally:
+        ctx.check(ctx.set_tuning(t0))
+    for i, cam in enumerate(cams):
+        ref, _ = oracle_render(oracle_lib, m, cam, opt)
+        got = {k: v.cpu().numpy() for k, v in tensors[i].items()}
+        compare(ref, got, f"view {i} {sizes[i]}")
